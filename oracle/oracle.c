@@ -1,0 +1,668 @@
+/*
+ * oracle.c -- CPU restatement of the voxtrees ray/ball search path and of the
+ * BEST-quality render loop.  TEST INFRASTRUCTURE ONLY (see oracle.h): the
+ * product never links this file.
+ *
+ * Reference files restated here (paths within shamazmazum/voxvision):
+ *   src/voxtrees/tree.c      vox_make_tree and its scalar helpers
+ *   src/voxtrees/geom.c      hit_box, hit_plane_within_box, metrics, ...
+ *   src/voxtrees/search.c    vox_ray_tree_intersection, vox_tree_ball_collidep
+ *   src/voxrnd/renderer.c    vox_render (BEST branch), get_color
+ *   src/voxrnd/simple-camera.c, doom-camera.c, vect-ops.c   screen2world
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+static float orc_voxel[3] = {1.0f, 1.0f, 1.0f};   /* tree.c:11 vox_voxel */
+
+void orc_set_voxel(float x, float y, float z)
+{
+    orc_voxel[0] = x; orc_voxel[1] = y; orc_voxel[2] = z;
+}
+
+void orc_get_voxel(float out[3])
+{
+    out[0] = orc_voxel[0]; out[1] = orc_voxel[1]; out[2] = orc_voxel[2];
+}
+
+/* ------------------------------------------------------------------ */
+/* geometry (geom.c, scalar branch)                                    */
+/* ------------------------------------------------------------------ */
+
+/* geom.c:13-31 fit_into_box: clamp, report whether the dot was inside. */
+static int fit_into_box(const struct orc_box *box, const float *dot, float *res)
+{
+    int same = 1;
+    for (int i = 0; i < 3; i++) {
+        if (dot[i] < box->min[i]) { res[i] = box->min[i]; same = 0; }
+        else if (dot[i] > box->max[i]) { res[i] = box->max[i]; same = 0; }
+        else res[i] = dot[i];
+    }
+    return same;
+}
+
+/* geom.c:44-51 */
+static int subspace_idx(const float *center, const float *dot)
+{
+    int r = 0;
+    for (int i = 0; i < 3; i++) r |= (center[i] > dot[i]) << i;
+    return r;
+}
+
+/* geom.c:53-65 */
+static int corrected_subspace_idx(const float *center, const float *dot, const float *dir)
+{
+    int r = 0;
+    for (int i = 0; i < 3; i++) {
+        int a = (center[i] == dot[i]) ? (dir[i] < 0) : (center[i] > dot[i]);
+        r |= a << i;
+    }
+    return r;
+}
+
+/* geom.c:69-99 hit_box: entry point of a ray into a closed box. */
+static int hit_box(const struct orc_box *box, const float *origin, const float *dir, float *res)
+{
+    if (fit_into_box(box, origin, res)) return 1;
+    int plane = 0;
+    float maxd = -1;
+    for (int i = 0; i < 3; i++) {
+        float t = (res[i] - origin[i]) / dir[i];
+        if (t > maxd) { plane = i; maxd = t; }
+    }
+    if (maxd <= 0) return 0;
+    for (int i = 0; i < 3; i++) {
+        if (i == plane) continue;
+        float t = origin[i] + maxd * dir[i];
+        if (t < box->min[i] || t > box->max[i]) return 0;
+        res[i] = t;
+    }
+    return 1;
+}
+
+/* geom.c:101-123 hit_plane_within_box */
+static int hit_plane_within_box(const float *origin, const float *dir, const float *planedot,
+                                int p, float *res, const struct orc_box *box)
+{
+    float k = planedot[p] - origin[p];
+    if (k == 0 || ((dir[p] < 0) != (k < 0))) return 0;
+    k = k / dir[p];
+    for (int i = 0; i < 3; i++) {
+        res[i] = origin[i] + k * dir[i];
+        if (res[i] < box->min[i] || res[i] > box->max[i]) return 0;
+    }
+    return 1;
+}
+
+/* geom.c:125-131: ((0 + |dx|) + |dy|) + |dz| */
+static float abs_metric(const float *a, const float *b)
+{
+    float r = 0;
+    for (int i = 0; i < 3; i++) r += fabsf(a[i] - b[i]);
+    return r;
+}
+
+/* geom.c:133-139 (powf(d, 2.0) is d*d) */
+static float sqr_metric(const float *a, const float *b)
+{
+    float r = 0;
+    for (int i = 0; i < 3; i++) { float d = a[i] - b[i]; r += d * d; }
+    return r;
+}
+
+/* geom.c:149-154 */
+static int box_ball_interp(const struct orc_box *box, const float *center, float radius)
+{
+    float f[3];
+    fit_into_box(box, center, f);
+    return sqr_metric(f, center) < radius * radius;
+}
+
+/* geom.c:157-167 */
+static int dense_set_p(const struct orc_box *box, size_t n)
+{
+    float size[3];
+    for (int i = 0; i < 3; i++) size[i] = box->max[i] - box->min[i];
+    float bbv = size[0] * size[1] * size[2];
+    float vv = orc_voxel[0] * orc_voxel[1] * orc_voxel[2];
+    return fabsf((float)n * vv - bbv) < vv;
+}
+
+/* ------------------------------------------------------------------ */
+/* tree build (tree.c:125-338, scalar branch)                          */
+/* ------------------------------------------------------------------ */
+
+/* tree.c:138-155 */
+static void calc_bounding_box(orc_dot *set, size_t n, struct orc_box *box)
+{
+    memcpy(box->min, set[0], sizeof(orc_dot));
+    memcpy(box->max, set[0], sizeof(orc_dot));
+    for (size_t i = 0; i < n; i++)
+        for (int j = 0; j < 3; j++) {
+            if (set[i][j] < box->min[j]) box->min[j] = set[i][j];
+            else if (set[i][j] > box->max[j]) box->max[j] = set[i][j];
+        }
+    for (int j = 0; j < 3; j++) box->max[j] = box->max[j] + orc_voxel[j];
+}
+
+/* tree.c:125-136: mean of (dot - box.min), then aligned up to the voxel grid */
+static void find_center(orc_dot *set, size_t n, const struct orc_box *box, float *res)
+{
+    res[0] = res[1] = res[2] = 0;
+    for (size_t i = 0; i < n; i++)
+        for (int j = 0; j < 3; j++) {
+            float t = set[i][j] - box->min[j];
+            res[j] = t + res[j];
+        }
+    for (int j = 0; j < 3; j++)
+        res[j] = ceilf((res[j] / (float)n + box->min[j]) / orc_voxel[j]) * orc_voxel[j];
+}
+
+/* tree.c:166-183: stable-for-the-chosen, swapping partition */
+static size_t sort_set(orc_dot *set, size_t n, size_t offset, int sub, const float *center)
+{
+    size_t counter = offset;
+    for (size_t i = offset; i < n; i++) {
+        if (subspace_idx(center, set[i]) == sub) {
+            orc_dot tmp;
+            memcpy(tmp, set[counter], sizeof(orc_dot));
+            memcpy(set[counter], set[i], sizeof(orc_dot));
+            memcpy(set[i], tmp, sizeof(orc_dot));
+            counter++;
+        }
+    }
+    return counter;
+}
+
+static struct orc_node *make_tree(orc_dot *set, size_t n)
+{
+    if (n == 0) return NULL;
+    struct orc_node *node = calloc(1, sizeof(struct orc_node));
+    struct orc_box box;
+    calc_bounding_box(set, n, &box);
+    int densep = dense_set_p(&box, n);
+    int leafp = n <= ORC_MAX_DOTS;
+    node->dots_num = (unsigned)n;
+    node->bounding_box = box;
+    if (densep) {
+        node->flags = ORC_DENSE_LEAF;
+    } else if (leafp) {
+        node->data.dots = malloc(ORC_MAX_DOTS * sizeof(orc_dot));
+        memcpy(node->data.dots, set, n * sizeof(orc_dot));
+        node->flags = ORC_LEAF;
+    } else {
+        orc_inner *inner = &node->data.inner;
+        size_t offset = 0;
+        node->flags = 0;
+        find_center(set, n, &node->bounding_box, inner->center);
+        for (int idx = 0; idx < 8; idx++) {
+            size_t noff = sort_set(set, n, offset, idx, inner->center);
+            if (offset == 0 && noff == n) {
+                /* tree.c:281-305: unsplittable set -> one overflowed leaf */
+                node->flags = ORC_LEAF | ORC_OVERFLOW;
+                node->data.dots = malloc(n * sizeof(orc_dot));
+                memcpy(node->data.dots, set, n * sizeof(orc_dot));
+                break;
+            }
+            inner->children[idx] = make_tree(set + offset, noff - offset);
+            offset = noff;
+        }
+    }
+    return node;
+}
+
+struct orc_node *orc_make_tree(float *set, size_t n)
+{
+    return make_tree((orc_dot *)set, n);
+}
+
+void orc_destroy_tree(struct orc_node *tree)
+{
+    if (!tree) return;
+    if (tree->flags & ORC_LEAF) free(tree->data.dots);
+    else if (!(tree->flags & ORC_LEAF_MASK))
+        for (int i = 0; i < 8; i++) orc_destroy_tree(tree->data.inner.children[i]);
+    free(tree);
+}
+
+/* ------------------------------------------------------------------ */
+/* searches (search.c)                                                 */
+/* ------------------------------------------------------------------ */
+
+/* search.c:8-153 */
+const struct orc_node *orc_ray(const struct orc_node *tree, const float *origin,
+                               const float *dir, float *res, int *slot, orc_counts *cnt)
+{
+    float bb[3];
+    if (!tree) return NULL;
+    if (cnt) cnt->nodes++;
+    if (!hit_box(&tree->bounding_box, origin, dir, bb)) return NULL;
+
+    if (tree->flags & ORC_DENSE_LEAF) {           /* :31-37 */
+        memcpy(res, bb, sizeof(orc_dot));
+        if (slot) *slot = 0xFF;
+        return tree;
+    }
+    if (tree->flags & ORC_LEAF) {                 /* :39-81 */
+        float closest = INFINITY;
+        const struct orc_node *leaf = NULL;
+        struct orc_box vox;
+        float far[3];
+        for (unsigned i = 0; i < tree->dots_num; i++) {
+            if (cnt) cnt->voxels++;
+            for (int j = 0; j < 3; j++) {
+                vox.min[j] = tree->data.dots[i][j];
+                vox.max[j] = vox.min[j] + orc_voxel[j];
+            }
+            if (hit_box(&vox, bb, dir, far)) {
+                float d = abs_metric(bb, far);
+                if (d == 0) {
+                    memcpy(res, far, sizeof(orc_dot));
+                    if (slot) *slot = (int)i;
+                    return tree;
+                }
+                if (d < closest) {
+                    closest = d;
+                    memcpy(res, far, sizeof(orc_dot));
+                    if (slot) *slot = (int)i;
+                    leaf = tree;
+                }
+            }
+        }
+        return leaf;
+    }
+
+    if (cnt) cnt->inner++;
+    const orc_inner *inner = &tree->data.inner;  /* :84-97 */
+    int sub = corrected_subspace_idx(inner->center, bb, dir);
+    const struct orc_node *leaf = orc_ray(inner->children[sub], bb, dir, res, slot, cnt);
+    if (leaf) return leaf;
+
+    float pi[3][3];                               /* :105-113 */
+    int pidx[3];
+    unsigned pc = 0;
+    for (int i = 0; i < 3; i++) {
+        pidx[pc] = i;
+        if (hit_plane_within_box(bb, dir, inner->center, i, pi[pc], &tree->bounding_box)) pc++;
+    }
+    for (unsigned i = 0; i < pc; i++) {           /* :115-148 */
+        for (unsigned j = i + 1; j < pc; j++) {
+            if (abs_metric(bb, pi[j]) < abs_metric(bb, pi[i])) {
+                float t[3];
+                memcpy(t, pi[j], sizeof t);
+                memcpy(pi[j], pi[i], sizeof t);
+                memcpy(pi[i], t, sizeof t);
+                int ti = pidx[j]; pidx[j] = pidx[i]; pidx[i] = ti;
+            }
+        }
+        sub ^= 1 << pidx[i];
+        leaf = orc_ray(inner->children[sub], pi[i], dir, res, slot, cnt);
+        if (leaf) return leaf;
+    }
+    return NULL;
+}
+
+/* search.c:155-183 */
+int orc_ball(const struct orc_node *tree, const float *center, float radius, orc_counts *cnt)
+{
+    if (!tree) return 0;
+    if (cnt) cnt->nodes++;
+    if (box_ball_interp(&tree->bounding_box, center, radius)) {
+        if (tree->flags & ORC_DENSE_LEAF) return 1;
+        if (tree->flags & ORC_LEAF) {
+            struct orc_box vox;
+            for (unsigned i = 0; i < tree->dots_num; i++) {
+                if (cnt) cnt->voxels++;
+                for (int j = 0; j < 3; j++) {
+                    vox.min[j] = tree->data.dots[i][j];
+                    vox.max[j] = vox.min[j] + orc_voxel[j];
+                }
+                if (box_ball_interp(&vox, center, radius)) return 1;
+            }
+        } else {
+            for (int i = 0; i < 8; i++)
+                if (orc_ball(tree->data.inner.children[i], center, radius, cnt)) return 1;
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* pre-order numbering                                                 */
+/* ------------------------------------------------------------------ */
+
+size_t orc_count_nodes(const struct orc_node *tree)
+{
+    if (!tree) return 0;
+    size_t c = 1;
+    if (!(tree->flags & ORC_LEAF_MASK))
+        for (int i = 0; i < 8; i++) c += orc_count_nodes(tree->data.inner.children[i]);
+    return c;
+}
+
+static void preorder_fill(const struct orc_node *t, const struct orc_node **out, size_t *k)
+{
+    if (!t) return;
+    out[(*k)++] = t;
+    if (!(t->flags & ORC_LEAF_MASK))
+        for (int i = 0; i < 8; i++) preorder_fill(t->data.inner.children[i], out, k);
+}
+
+size_t orc_preorder(const struct orc_node *tree, const struct orc_node **out)
+{
+    size_t k = 0;
+    preorder_fill(tree, out, &k);
+    return k;
+}
+
+typedef struct { const struct orc_node *p; uint32_t id; } ptr_id;
+
+static int cmp_ptr(const void *a, const void *b)
+{
+    uintptr_t x = (uintptr_t)((const ptr_id *)a)->p, y = (uintptr_t)((const ptr_id *)b)->p;
+    return (x > y) - (x < y);
+}
+
+static ptr_id *build_index(const struct orc_node *tree, size_t *nn)
+{
+    size_t n = orc_count_nodes(tree);
+    const struct orc_node **pre = malloc((n ? n : 1) * sizeof(*pre));
+    orc_preorder(tree, pre);
+    ptr_id *idx = malloc((n ? n : 1) * sizeof(ptr_id));
+    for (size_t i = 0; i < n; i++) { idx[i].p = pre[i]; idx[i].id = (uint32_t)i; }
+    free(pre);
+    qsort(idx, n, sizeof(ptr_id), cmp_ptr);
+    *nn = n;
+    return idx;
+}
+
+static uint32_t lookup_id(const ptr_id *idx, size_t n, const struct orc_node *p)
+{
+    size_t lo = 0, hi = n;
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if ((uintptr_t)idx[mid].p < (uintptr_t)p) lo = mid + 1; else hi = mid;
+    }
+    return (lo < n && idx[lo].p == p) ? idx[lo].id : UINT32_MAX;
+}
+
+/* ------------------------------------------------------------------ */
+/* threaded batch drivers                                              */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    size_t n, chunk;
+    volatile size_t next;
+    pthread_mutex_t mu;
+    void (*work)(void *ctx, size_t lo, size_t hi, orc_counts *c);
+    void *ctx;
+    uint64_t totals[3];
+} pool_job;
+
+static void *pool_worker(void *arg)
+{
+    pool_job *job = arg;
+    orc_counts c = {0, 0, 0};
+    for (;;) {
+        size_t lo = __atomic_fetch_add(&job->next, job->chunk, __ATOMIC_RELAXED);
+        if (lo >= job->n) break;
+        size_t hi = lo + job->chunk < job->n ? lo + job->chunk : job->n;
+        job->work(job->ctx, lo, hi, &c);
+    }
+    pthread_mutex_lock(&job->mu);
+    job->totals[0] += c.nodes; job->totals[1] += c.inner; job->totals[2] += c.voxels;
+    pthread_mutex_unlock(&job->mu);
+    return NULL;
+}
+
+static void run_pool(size_t n, size_t chunk, int nthreads,
+                     void (*work)(void *, size_t, size_t, orc_counts *), void *ctx,
+                     uint64_t *counts3)
+{
+    pool_job job;
+    job.n = n; job.chunk = chunk ? chunk : 1; job.next = 0;
+    job.work = work; job.ctx = ctx;
+    job.totals[0] = job.totals[1] = job.totals[2] = 0;
+    pthread_mutex_init(&job.mu, NULL);
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads == 1) {
+        pool_worker(&job);
+    } else {
+        pthread_t *th = malloc(sizeof(pthread_t) * (size_t)nthreads);
+        for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, pool_worker, &job);
+        for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+        free(th);
+    }
+    pthread_mutex_destroy(&job.mu);
+    if (counts3) { counts3[0] = job.totals[0]; counts3[1] = job.totals[1]; counts3[2] = job.totals[2]; }
+}
+
+typedef struct {
+    const struct orc_node *root;
+    const ptr_id *idx; size_t nidx;
+    const float *o, *d;
+    uint32_t *leaf; uint8_t *slot; float *pts;
+} ray_ctx;
+
+static void ray_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
+{
+    ray_ctx *x = vctx;
+    for (size_t i = lo; i < hi; i++) {
+        int s = 0xFF;
+        float res[3];
+        const struct orc_node *l = orc_ray(x->root, x->o + 3 * i, x->d + 3 * i, res, &s, c);
+        if (l) {
+            x->leaf[i] = lookup_id(x->idx, x->nidx, l);
+            x->slot[i] = (uint8_t)s;
+            memcpy(x->pts + 3 * i, res, sizeof res);
+        } else {
+            x->leaf[i] = UINT32_MAX;
+            x->slot[i] = 0xFF;
+        }
+    }
+}
+
+int orc_ray_batch(const struct orc_node *tree, const struct orc_node *root,
+                  size_t n, const float *origins, const float *dirs,
+                  uint32_t *leaf_id, uint8_t *slot, float *points,
+                  uint64_t *counts3, int nthreads)
+{
+    ray_ctx x;
+    x.root = root; x.o = origins; x.d = dirs; x.leaf = leaf_id; x.slot = slot; x.pts = points;
+    ptr_id *idx = build_index(tree, &x.nidx);
+    x.idx = idx;
+    run_pool(n, 4096, nthreads, ray_work, &x, counts3);
+    free(idx);
+    return 0;
+}
+
+typedef struct {
+    const struct orc_node *root;
+    const float *c, *r;
+    uint8_t *hit;
+} ball_ctx;
+
+static void ball_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
+{
+    ball_ctx *x = vctx;
+    for (size_t i = lo; i < hi; i++)
+        x->hit[i] = (uint8_t)orc_ball(x->root, x->c + 3 * i, x->r[i], c);
+}
+
+int orc_ball_batch(const struct orc_node *tree, size_t n, const float *centers,
+                   const float *radii, uint8_t *hit, uint64_t *counts3, int nthreads)
+{
+    ball_ctx x = {tree, centers, radii, hit};
+    run_pool(n, 1024, nthreads, ball_work, &x, counts3);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* cameras and the render loop                                         */
+/* ------------------------------------------------------------------ */
+
+/* vect-ops.c:7-15 */
+static void cross(const float *v1, const float *v2, float *r)
+{
+    float i1 = v1[0], j1 = v1[1], k1 = v1[2];
+    float i2 = v2[0], j2 = v2[1], k2 = v2[2];
+    r[0] = j1 * k2 - k1 * j2;
+    r[1] = -i1 * k2 + k1 * i2;
+    r[2] = i1 * j2 - j1 * i2;
+}
+
+/* simple-camera.c:21-31 with vect-ops.c:28-36; doom-camera.c:24-57 */
+void orc_screen2world(const orc_camera *cam, int sx, int sy, float *ray)
+{
+    if (cam->kind == 1) {
+        float d0 = cam->mul * (float)sx - cam->xsub;
+        float d1 = 1;
+        float d2 = cam->ysub - cam->mul * (float)sy;
+        d2 += cam->k;
+        ray[0] = d0 * cam->cosphi - d1 * cam->sinphi;
+        ray[1] = d1 * cam->cosphi + d0 * cam->sinphi;
+        ray[2] = d2;
+        return;
+    }
+    float v[3] = {cam->mul * (float)sx - cam->xsub, 1, cam->ysub - cam->mul * (float)sy};
+    float t[3], t2[3];
+    cross(cam->rotation + 1, v, t);
+    for (int i = 0; i < 3; i++) t[i] = t[i] * 2.0f;
+    cross(cam->rotation + 1, t, t2);
+    for (int i = 0; i < 3; i++) ray[i] = v[i] + cam->rotation[0] * t[i] + t2[i];
+}
+
+/* renderer.c:27-39 get_color, no light manager; SDL_MapRGB on ARGB8888 */
+static uint32_t get_color(const uint8_t *tex, const float *inter)
+{
+    int x = abs((int)(inter[0] / orc_voxel[0])) & 31;
+    int y = abs((int)(inter[1] / orc_voxel[1])) & 31;
+    int z = abs((int)(inter[2] / orc_voxel[2])) & 31;
+    uint32_t c = tex[x * 1024 + y * 32 + z];
+    return 0xFF000000u | (c << 16) | (c << 8) | c;
+}
+
+static const int zorder[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}; /* renderer.c:23-25 */
+
+typedef struct {
+    const struct orc_node *tree;
+    const orc_camera *cam;
+    int w, ws;
+    const uint8_t *tex;
+    uint32_t *argb;
+} render_ctx;
+
+static void render_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
+{
+    render_ctx *x = vctx;
+    for (size_t cs = lo; cs < hi; cs++) {
+        int ys = (int)(cs / (size_t)x->ws) * 4, xs = (int)(cs % (size_t)x->ws) * 4;
+        for (int i = 0; i < 16; i++) {
+            int p = zorder[i], px = xs + p % 4, py = ys + p / 4;
+            float dir[3], inter[3];
+            orc_screen2world(x->cam, px, py, dir);
+            const struct orc_node *l = orc_ray(x->tree, x->cam->position, dir, inter, NULL, c);
+            x->argb[(size_t)py * x->w + px] = l ? get_color(x->tex, inter) : 0u;
+        }
+    }
+}
+
+int orc_render_best(const struct orc_node *tree, const orc_camera *cam,
+                    int w, int h, const uint8_t *texture, uint32_t *argb,
+                    uint64_t *counts3, int nthreads)
+{
+    if ((w & 0xf) || (h & 0x3)) return -1;   /* renderer.c:97-100 bad_geometry */
+    render_ctx x = {tree, cam, w, w / 4, texture, argb};
+    run_pool((size_t)(w / 4) * (size_t)(h / 4), 64, nthreads, render_work, &x, counts3);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* dumps                                                               */
+/* ------------------------------------------------------------------ */
+
+size_t orc_count_stored_dots(const struct orc_node *tree)
+{
+    if (!tree) return 0;
+    if (tree->flags & ORC_DENSE_LEAF) return 0;
+    if (tree->flags & ORC_LEAF) return tree->dots_num;
+    size_t c = 0;
+    for (int i = 0; i < 8; i++) c += orc_count_stored_dots(tree->data.inner.children[i]);
+    return c;
+}
+
+typedef struct {
+    uint32_t *flags, *dots_num; float *boxes, *centers; uint8_t *mask;
+    uint64_t *doff; float *dots; size_t k, nd;
+} dump_ctx;
+
+static void dump_rec(const struct orc_node *t, dump_ctx *d)
+{
+    if (!t) return;
+    size_t k = d->k++;
+    d->flags[k] = t->flags;
+    d->dots_num[k] = t->dots_num;
+    memcpy(d->boxes + 6 * k, &t->bounding_box, 6 * sizeof(float));
+    memset(d->centers + 3 * k, 0, 3 * sizeof(float));
+    d->mask[k] = 0;
+    d->doff[k] = d->nd;
+    if (t->flags & ORC_DENSE_LEAF) return;
+    if (t->flags & ORC_LEAF) {
+        memcpy(d->dots + 3 * d->nd, t->data.dots, t->dots_num * sizeof(orc_dot));
+        d->nd += t->dots_num;
+        return;
+    }
+    memcpy(d->centers + 3 * k, t->data.inner.center, 3 * sizeof(float));
+    for (int i = 0; i < 8; i++)
+        if (t->data.inner.children[i]) d->mask[k] |= (uint8_t)(1u << i);
+    for (int i = 0; i < 8; i++) dump_rec(t->data.inner.children[i], d);
+}
+
+size_t orc_dump(const struct orc_node *tree, uint32_t *flags, uint32_t *dots_num,
+                float *boxes, float *centers, uint8_t *child_mask,
+                uint64_t *dot_offset, float *dots)
+{
+    dump_ctx d = {flags, dots_num, boxes, centers, child_mask, dot_offset, dots, 0, 0};
+    dump_rec(tree, &d);
+    return d.k;
+}
+
+typedef struct {
+    const uint32_t *flags, *dots_num; const float *boxes, *centers; const uint8_t *mask;
+    const uint64_t *doff; const float *dots; size_t k, n;
+} undump_ctx;
+
+static struct orc_node *undump_rec(undump_ctx *u)
+{
+    if (u->k >= u->n) return NULL;
+    size_t k = u->k++;
+    struct orc_node *t = calloc(1, sizeof(struct orc_node));
+    t->flags = u->flags[k];
+    t->dots_num = u->dots_num[k];
+    memcpy(&t->bounding_box, u->boxes + 6 * k, 6 * sizeof(float));
+    if (t->flags & ORC_DENSE_LEAF) return t;
+    if (t->flags & ORC_LEAF) {
+        size_t cap = t->dots_num > ORC_MAX_DOTS ? t->dots_num : ORC_MAX_DOTS;
+        t->data.dots = malloc(cap * sizeof(orc_dot));
+        memcpy(t->data.dots, u->dots + 3 * u->doff[k], t->dots_num * sizeof(orc_dot));
+        return t;
+    }
+    memcpy(t->data.inner.center, u->centers + 3 * k, 3 * sizeof(float));
+    uint8_t m = u->mask[k];
+    for (int i = 0; i < 8; i++)
+        t->data.inner.children[i] = (m >> i & 1) ? undump_rec(u) : NULL;
+    return t;
+}
+
+struct orc_node *orc_from_dump(size_t nnodes, const uint32_t *flags,
+                               const uint32_t *dots_num, const float *boxes,
+                               const float *centers, const uint8_t *child_mask,
+                               const uint64_t *dot_offset, const float *dots)
+{
+    undump_ctx u = {flags, dots_num, boxes, centers, child_mask, dot_offset, dots, 0, nnodes};
+    return nnodes ? undump_rec(&u) : NULL;
+}

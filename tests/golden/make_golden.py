@@ -1,0 +1,386 @@
+"""Generate the golden vectors under tests/golden/ from the reference itself.
+
+Run in a container that has the reference sources (default /root/reference):
+
+    make -C oracle ref            # compiles the reference's own voxtrees and
+                                  # camera sources into oracle/_ref/
+    python tests/golden/make_golden.py
+
+Every expected value here comes from the reference's compiled code:
+vox_make_tree, vox_insert_voxel, vox_ray_tree_intersection,
+vox_tree_ball_collidep (src/voxtrees/tree.c, search.c, geom.c) and the
+simple-camera / doom-camera plugins (src/voxrnd/*-camera.c, vect-ops.c).
+The oracle library is used only to serialise the reference-built trees
+(orc_dump / orc_preorder walk the same struct layout).  The fixtures are
+small .npz files that the tests read on any host; this script is the only
+thing that needs the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import oracle as orc  # noqa: E402
+from voxvision_gb300 import workloads as wl  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+ref = C.CDLL(os.path.join(REF, "libvoxtrees_ref.so"))
+vp = C.c_void_p
+ref.vox_make_tree.argtypes = [vp, C.c_size_t]; ref.vox_make_tree.restype = vp
+ref.vox_destroy_tree.argtypes = [vp]
+ref.vox_ray_tree_intersection.argtypes = [vp, vp, vp, vp]; ref.vox_ray_tree_intersection.restype = vp
+ref.vox_tree_ball_collidep.argtypes = [vp, vp, C.c_float]; ref.vox_tree_ball_collidep.restype = C.c_int
+ref.vox_insert_voxel.argtypes = [C.POINTER(vp), vp]; ref.vox_insert_voxel.restype = C.c_int
+ref.vox_set_voxel_size.argtypes = [C.c_float] * 3
+
+
+def P(a):
+    return a.ctypes.data_as(vp)
+
+
+def set_voxel(v):
+    ref.vox_set_voxel_size(*v)
+    orc.set_voxel(v)
+
+
+def ref_tree_from_voxels(vox):
+    s = np.ascontiguousarray(vox, dtype=np.float32).copy()
+    return ref.vox_make_tree(P(s), s.shape[0])
+
+
+def preorder_map(tree):
+    pre = orc.OracleTree(None)
+    pre.ptr = None
+    n = orc.lib().orc_count_nodes(tree)
+    arr = np.zeros(max(n, 1), np.uint64)
+    orc.lib().orc_preorder(tree, P(arr))
+    return {int(p): i for i, p in enumerate(arr[:n])}, arr[:n]
+
+
+def ref_rays(tree, roots, origins, dirs, pmap):
+    n = origins.shape[0]
+    leaf = np.full(n, 0xFFFFFFFF, np.uint32)
+    pts = np.zeros((n, 3), np.float32)
+    res = np.zeros(3, np.float32)
+    for i in range(n):
+        o = np.ascontiguousarray(origins[i]); d = np.ascontiguousarray(dirs[i])
+        r = ref.vox_ray_tree_intersection(roots[i] if roots is not None else tree, P(o), P(d), P(res))
+        if r:
+            leaf[i] = pmap[int(r)]
+            pts[i] = res
+    return leaf, pts
+
+
+def ref_balls(tree, centres, radii):
+    out = np.zeros(centres.shape[0], np.uint8)
+    for i in range(centres.shape[0]):
+        c = np.ascontiguousarray(centres[i])
+        out[i] = ref.vox_tree_ball_collidep(tree, P(c), C.c_float(float(radii[i])))
+    return out
+
+
+def edge_rays(box_min, box_max, n, seed, voxel):
+    """A mix of random and degenerate rays around a bounding box."""
+    rng = np.random.default_rng(seed)
+    lo = np.asarray(box_min, np.float64); hi = np.asarray(box_max, np.float64)
+    ext = hi - lo
+    o, d = [], []
+    k = n // 8
+    # 1: random origins in a 2x box, random directions
+    o.append(lo - ext / 2 + 2 * ext * rng.random((k, 3))); d.append(rng.normal(size=(k, 3)))
+    # 2: axis-aligned directions from lattice points (voxel corners)
+    g = np.floor(lo / voxel) * voxel + np.round(rng.random((k, 3)) * ext / voxel) * voxel
+    axis = rng.integers(0, 3, k); sign = rng.choice([-1.0, 1.0], k)
+    dd = np.zeros((k, 3)); dd[np.arange(k), axis] = sign
+    g[np.arange(k), axis] = np.where(sign > 0, lo[axis] - 2 * voxel[axis], hi[axis] + 2 * voxel[axis])
+    o.append(g); d.append(dd)
+    # 3: one zero component (with signed zeros)
+    r = rng.normal(size=(k, 3)); z = rng.integers(0, 3, k)
+    r[np.arange(k), z] = np.where(rng.random(k) < 0.5, 0.0, -0.0)
+    o.append(lo - ext / 2 + 2 * ext * rng.random((k, 3))); d.append(r)
+    # 4: origins inside the box
+    o.append(lo + ext * rng.random((k, 3))); d.append(rng.normal(size=(k, 3)))
+    # 5: integer origins inside, integer directions (ties and exact faces)
+    o.append(np.floor(lo + ext * rng.random((k, 3)))); d.append(rng.integers(-2, 3, (k, 3)).astype(np.float64))
+    # 6: diagonal rays aimed at the centre from lattice points outside
+    c = (lo + hi) / 2
+    st = np.floor(lo - ext * rng.random((k, 3)))
+    o.append(st); d.append(np.sign(c - st))
+    # 7: aimed at random voxel corners from far away
+    tgt = np.floor(lo + ext * rng.random((k, 3)))
+    src = tgt + rng.normal(size=(k, 3)) * ext.max()
+    o.append(src); d.append(tgt - src)
+    # 8: two zero components, plus a few all-zero directions
+    m = n - 7 * k
+    dd = np.zeros((m, 3)); ax = rng.integers(0, 3, m)
+    dd[np.arange(m), ax] = rng.normal(size=m)
+    dd[: max(1, m // 50)] = 0.0
+    o.append(lo - ext / 4 + 1.5 * ext * rng.random((m, 3))); d.append(dd)
+    return (np.ascontiguousarray(np.concatenate(o).astype(np.float32)),
+            np.ascontiguousarray(np.concatenate(d).astype(np.float32)))
+
+
+def edge_balls(box_min, box_max, n, seed):
+    rng = np.random.default_rng(seed)
+    lo = np.asarray(box_min, np.float64); hi = np.asarray(box_max, np.float64)
+    ext = hi - lo
+    k = n // 2
+    c1 = lo - ext / 4 + 1.5 * ext * rng.random((k, 3)); r1 = 8 * rng.random(k)
+    c2 = np.round(lo + ext * rng.random((n - k, 3))); r2 = rng.choice([0.0, 0.5, 1.0, 1.5, 2.0, -1.0], n - k)
+    return (np.ascontiguousarray(np.concatenate([c1, c2]).astype(np.float32)),
+            np.ascontiguousarray(np.concatenate([r1, r2]).astype(np.float32)))
+
+
+def save_case(name, tree, voxel, voxels=None, nrays=8000, nballs=4000, seed=0, extra=None,
+              leaf_roots=1000):
+    pmap, pre = preorder_map(tree)
+    dump = orc.dump_tree(tree)
+    out = {f"tree_{k}": v for k, v in dump.items()}
+    out["voxel"] = np.asarray(voxel, np.float32)
+    if voxels is not None:
+        out["voxels"] = np.asarray(voxels, np.float32)
+    if tree:
+        bmin, bmax = dump["boxes"][0][:3], dump["boxes"][0][3:]
+    else:
+        bmin, bmax = np.zeros(3), np.ones(3)
+    o, d = edge_rays(bmin, bmax, nrays, seed, np.asarray(voxel, np.float64))
+    leaf, pts = ref_rays(tree, None, o, d, pmap)
+    out.update(ray_origins=o, ray_dirs=d, ray_leaf=leaf, ray_points=pts)
+    # searches rooted at a leaf (what FAST mode does, renderer.c:297)
+    leaves = [i for i in range(len(pre)) if dump["flags"][i] & 3]
+    if leaves and leaf_roots:
+        rng = np.random.default_rng(seed + 1)
+        ridx = rng.choice(np.asarray(leaves), leaf_roots).astype(np.uint32)
+        lb = dump["boxes"][ridx]
+        lo_, hi_ = lb[:, :3].astype(np.float64), lb[:, 3:].astype(np.float64)
+        src = lo_ - 3 + (hi_ - lo_ + 6) * rng.random((leaf_roots, 3))
+        tgt = lo_ + (hi_ - lo_) * rng.random((leaf_roots, 3))
+        ro = np.ascontiguousarray(src.astype(np.float32))
+        rd = np.ascontiguousarray((tgt - src).astype(np.float32))
+        rl, rp = ref_rays(tree, [int(pre[i]) for i in ridx], ro, rd, pmap)
+        out.update(root_ids=ridx, root_origins=ro, root_dirs=rd, root_leaf=rl, root_points=rp)
+    c, r = edge_balls(bmin, bmax, nballs, seed + 2)
+    out.update(ball_centres=c, ball_radii=r, ball_hit=ref_balls(tree, c, r))
+    if extra:
+        out.update(extra)
+    path = os.path.join(OUT, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: nodes={len(pre)} rays hit={np.mean(leaf != 0xFFFFFFFF):.3f} "
+          f"balls hit={out['ball_hit'].mean():.3f} size={os.path.getsize(path)} B")
+
+
+# ---------------------------------------------------------------- cameras
+
+class SimpleCam(C.Structure):      # simple-camera.c:10-17
+    _fields_ = [("iface", vp), ("xsub", C.c_float), ("ysub", C.c_float), ("position", C.c_float * 3),
+                ("rotation", C.c_float * 4), ("mul", C.c_float), ("fov", C.c_float)]
+
+
+class DoomCam(C.Structure):        # doom-camera.c:8-15
+    _fields_ = [("iface", vp), ("xsub", C.c_float), ("ysub", C.c_float), ("position", C.c_float * 3),
+                ("phi", C.c_float), ("sinphi", C.c_float), ("cosphi", C.c_float), ("k", C.c_float),
+                ("mul", C.c_float), ("fov", C.c_float)]
+
+
+class Module(C.Structure):
+    _fields_ = [("type", C.c_int), ("methods", vp)]
+
+
+S2W = C.CFUNCTYPE(None, vp, vp, C.c_int, C.c_int)
+SETDOT = C.CFUNCTYPE(None, vp, C.c_char_p, vp)
+SETNUM = C.CFUNCTYPE(None, vp, C.c_char_p, C.c_float)
+DOTM = C.CFUNCTYPE(None, vp, vp)
+WS = C.CFUNCTYPE(None, vp, C.c_int, C.c_int)
+CONS = C.CFUNCTYPE(vp, vp)
+
+
+class RefCamera:
+    """A camera object from the reference plugin, driven through its vtable
+    (camera.h:17-117: set_property_number, set_property_dot, screen2world,
+    rotate_camera, move_camera, look_at, get_position, set_window_size,
+    construct_camera, destroy_camera)."""
+
+    def __init__(self, kind):
+        self.kind = kind
+        lib = C.CDLL(os.path.join(REF, f"lib{'simple' if kind == 0 else 'doom'}cam_ref.so"))
+        lib.module_init.restype = C.POINTER(Module)
+        meth = lib.module_init().contents.methods
+        tbl = C.cast(meth, C.POINTER(vp * 10)).contents
+        self.obj = CONS(tbl[8])(None)
+        self.lib = lib
+        itbl = C.cast(C.cast(self.obj, C.POINTER(vp))[0], C.POINTER(vp * 10)).contents
+        self.set_num = SETNUM(itbl[0]); self.set_dot = SETDOT(itbl[1]); self.s2w = S2W(itbl[2])
+        self.rotate = DOTM(itbl[3]); self.move = DOTM(itbl[4]); self.look_at = DOTM(itbl[5])
+        self.set_ws = WS(itbl[7])
+
+    def dot(self, name, v):
+        a = np.asarray(v, np.float32)
+        self.set_dot(self.obj, name.encode(), P(a))
+
+    def state(self):
+        st = C.cast(self.obj, C.POINTER(SimpleCam if self.kind == 0 else DoomCam)).contents
+        s = dict(kind=self.kind, position=np.array(st.position[:], np.float32),
+                 mul=st.mul, xsub=st.xsub, ysub=st.ysub, fov=st.fov)
+        if self.kind == 0:
+            s["rotation"] = np.array(st.rotation[:], np.float32)
+        else:
+            s.update(sinphi=st.sinphi, cosphi=st.cosphi, k=st.k, phi=st.phi)
+        return s
+
+    def ray(self, sx, sy):
+        out = np.zeros(3, np.float32)
+        self.s2w(self.obj, P(out), sx, sy)
+        return out
+
+
+def camera_cases():
+    """Camera states after the reference's own set-up calls, plus screen2world
+    outputs on a pixel sample."""
+    rng = np.random.default_rng(5)
+    recs = []
+    setups = [
+        (256, 256, (160, -96, 112), (32, 32, 32), None, 1.0),
+        (1920, 1080, (128 + 665, 128, 350), (128, 128, 128), None, 1.0),
+        (100, 100, (0, 0, 0), None, (0, 0, np.pi / 2), 1.0),
+        (640, 480, (-100, 20, -20), (0, 0, 0), None, 0.8),
+        (240, 320, (10, 300, 40), (5, 6, 7), None, 1.2),
+        (3840, 2160, (500, 500, 500), (0, 0, 0), None, 1.0),
+    ]
+    for kind in (0, 1):
+        for (w, h, pos, at, rot, fov) in setups:
+            cam = RefCamera(kind)
+            cam.set_num(cam.obj, b"fov", C.c_float(fov))
+            cam.set_ws(cam.obj, w, h)
+            cam.dot("position", pos)
+            if rot is not None:
+                cam.dot("rotation", rot)
+            if at is not None:
+                a = np.asarray(at, np.float32)
+                cam.look_at(cam.obj, P(a))
+            st = cam.state()
+            px = np.stack([rng.integers(0, w, 64), rng.integers(0, h, 64)], 1)
+            px = np.concatenate([px, [[0, 0], [w - 1, h - 1], [w // 2, h // 2], [w, h]]]).astype(np.int32)
+            rays = np.stack([cam.ray(int(x), int(y)) for x, y in px])
+            recs.append((st, w, h, pos, at, rot, fov, px, rays))
+    out = {}
+    for i, (st, w, h, pos, at, rot, fov, px, rays) in enumerate(recs):
+        out[f"c{i}_kind"] = np.int32(st["kind"])
+        out[f"c{i}_wh"] = np.array([w, h], np.int32)
+        out[f"c{i}_fov"] = np.float32(fov)
+        out[f"c{i}_setpos"] = np.asarray(pos, np.float32)
+        out[f"c{i}_lookat"] = np.asarray(at if at is not None else (np.nan,) * 3, np.float32)
+        out[f"c{i}_setrot"] = np.asarray(rot if rot is not None else (np.nan,) * 3, np.float32)
+        for k in ("position", "rotation", "mul", "xsub", "ysub", "sinphi", "cosphi", "k", "fov"):
+            if k in st:
+                out[f"c{i}_{k}"] = np.asarray(st[k], np.float32)
+        out[f"c{i}_pixels"] = px
+        out[f"c{i}_rays"] = rays
+    out["ncams"] = np.int32(len(recs))
+    np.savez_compressed(os.path.join(OUT, "cameras.npz"), **out)
+    print("cameras:", len(recs))
+
+
+def render_case():
+    """Config-1 workload (64^3 blobs, 256x256, camera at (160,-96,112) looking at
+    (32,32,32)): per-pixel rays from the reference simple camera, hits from the
+    reference search."""
+    set_voxel((1.0, 1.0, 1.0))
+    mask = wl.blobs_volume(64, 20, 1, 0.20)
+    vox = wl.voxels_from_mask(mask)
+    tree = ref_tree_from_voxels(vox)
+    pmap, pre = preorder_map(tree)
+    cam = RefCamera(0)
+    w = h = 256
+    cam.set_ws(cam.obj, w, h)
+    cam.dot("position", (160, -96, 112))
+    cam.look_at(cam.obj, P(np.asarray((32, 32, 32), np.float32)))
+    st = cam.state()
+    ys, xs = np.mgrid[0:h, 0:w]
+    dirs = np.stack([cam.ray(int(x), int(y)) for x, y in zip(xs.ravel(), ys.ravel())]).astype(np.float32)
+    orig = np.repeat(st["position"][None, :], w * h, 0).astype(np.float32)
+    leaf, pts = ref_rays(tree, None, orig, dirs, pmap)
+    dump = orc.dump_tree(tree)
+    out = {f"tree_{k}": v for k, v in dump.items()}
+    out.update(voxels=vox.astype(np.int16), voxel=np.ones(3, np.float32), w=np.int32(w), h=np.int32(h),
+               cam_position=st["position"], cam_rotation=st["rotation"],
+               cam_mul=np.float32(st["mul"]), cam_xsub=np.float32(st["xsub"]), cam_ysub=np.float32(st["ysub"]),
+               pix_dirs=dirs, pix_leaf=leaf, pix_points=pts)
+    np.savez_compressed(os.path.join(OUT, "render64.npz"), **out)
+    print(f"render64: voxels={len(vox)} nodes={len(pre)} hits={np.mean(leaf != 0xFFFFFFFF):.3f} "
+          f"size={os.path.getsize(os.path.join(OUT, 'render64.npz'))}")
+    ref.vox_destroy_tree(tree)
+
+
+def main():
+    # 1. ball of radius 12 (the reference's own tree fixture, tests.c:214-237, scaled down)
+    set_voxel((1.0, 1.0, 1.0))
+    g = np.mgrid[-12:12, -12:12, -12:12].reshape(3, -1).T
+    ball = g[(g ** 2).sum(1) < 144].astype(np.float32)
+    t = ref_tree_from_voxels(ball)
+    save_case("ball12", t, (1, 1, 1), ball, seed=10)
+    ref.vox_destroy_tree(t)
+
+    # 2. the regression tree of tests.c:600-659, built by insertion
+    t = vp(None)
+    pts = [(0, 0, 0), (0, 0, -1), (0, 0, -2), (0, 0, 1), (0, 0, 2)]
+    pts += [(-i, 0, 0) for i in range(1, 5)] + [(i, 0, 0) for i in range(1, 5)]
+    pts += [(0, -i, 0) for i in range(1, 5)] + [(0, i, 0) for i in range(1, 5)]
+    for p in pts:
+        a = np.asarray(p, np.float32)
+        ref.vox_insert_voxel(C.byref(t), P(a))
+    pmap, pre = preorder_map(t.value)
+    o = np.asarray([[-2, -2, 0]], np.float32); d = np.asarray([[1, 1, -1]], np.float32)
+    l, p = ref_rays(t.value, None, o, d, pmap)
+    assert l[0] != 0xFFFFFFFF, "regression ray of tests.c:655-658 must hit"
+    save_case("g676d50c", t.value, (1, 1, 1), None, nrays=4000, nballs=2000, seed=20,
+              extra=dict(regress_origin=o, regress_dir=d, regress_leaf=l, regress_point=p), leaf_roots=200)
+
+    # 3. duplicates -> overflowed leaf (tree.c:281-305); plus a small blob around it
+    dup = np.concatenate([np.tile([[3, 3, 3]], (12, 1)), np.mgrid[0:3, 0:3, 0:2].reshape(3, -1).T,
+                          [[9, 1, 4], [9, 2, 4], [10, 2, 4]]]).astype(np.float32)
+    t = ref_tree_from_voxels(dup)
+    save_case("overflow", t, (1, 1, 1), dup, nrays=4000, nballs=2000, seed=30, leaf_roots=200)
+    ref.vox_destroy_tree(t)
+
+    # 4. non-unit voxel size
+    v = (0.5, 1.0, 2.0)
+    set_voxel(v)
+    g = np.mgrid[-8:8, -8:8, -8:8].reshape(3, -1).T
+    sel = g[((g ** 2).sum(1) < 64) & ((g[:, 0] + g[:, 1]) % 3 != 0)]
+    vv = (sel * np.asarray(v)).astype(np.float32)
+    t = ref_tree_from_voxels(vv)
+    save_case("voxsize", t, v, vv, nrays=6000, nballs=3000, seed=40)
+    ref.vox_destroy_tree(t)
+    set_voxel((1.0, 1.0, 1.0))
+
+    # 5. a full cube (one dense leaf) and a cube with holes (dense sub-leaves)
+    cube = np.mgrid[0:8, 0:8, 0:8].reshape(3, -1).T.astype(np.float32)
+    t = ref_tree_from_voxels(cube)
+    save_case("dense", t, (1, 1, 1), cube, nrays=3000, nballs=1500, seed=50, leaf_roots=50)
+    ref.vox_destroy_tree(t)
+    holes = cube[(cube.sum(1) % 5) != 0]
+    t = ref_tree_from_voxels(holes)
+    save_case("holes", t, (1, 1, 1), holes, nrays=4000, nballs=2000, seed=60)
+    ref.vox_destroy_tree(t)
+
+    # 6. random sparse cloud in a 48^3 box
+    rng = np.random.default_rng(70)
+    cloud = np.unique(rng.integers(0, 48, (3000, 3)), axis=0).astype(np.float32)
+    rng.shuffle(cloud)
+    t = ref_tree_from_voxels(cloud)
+    save_case("cloud48", t, (1, 1, 1), cloud, nrays=8000, nballs=4000, seed=70)
+    ref.vox_destroy_tree(t)
+
+    camera_cases()
+    render_case()
+
+
+if __name__ == "__main__":
+    main()
