@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark: Mrays/s of the BEST-quality frame path at 1920x1080 over a
+256^3 volume, along a 120-frame orbit.
+
+Workload (one "step" = one full orbit = 120 frames = 248,832,000 rays):
+256^3 u8 value noise (17^3 lattice, spacing 16, seed 2), band-thresholded to
+~8% solid, built into a tree by the library's vox_make_tree; camera
+simple-camera, fov 1.0 (90 degrees), orbit radius 1.5 x the bounding-box
+diagonal (665.1) at 20 degrees elevation around (128, 128, 128); texture
+32^3 u8 from splitmix64 seed 7.
+
+  value  device throughput: 120 vox_cuda_render_device launches per step,
+         tree, texture and frame resident in HBM, timed with CUDA events on
+         the launching stream; L2 flushed (256 MiB write) between steps,
+         outside the timed events.
+  e2e    the same orbit through vox_cuda_render with host buffers: every
+         frame copies the texture in and the 8.3 MB frame out (pinned host
+         memory), timed on the host.
+  roofline  algorithmic bytes per frame (32 B per node visited, 16 B per
+         inner node entered, 16 B per voxel tested, 4 B per pixel stored;
+         counted by the counting kernel) over the mean launch time, against
+         the measured HBM copy bandwidth; a measured L2 read bandwidth is
+         reported beside it.
+  cpu_baseline  the CPU oracle (C restatement of the reference's search and
+         render loop) on all host cores over a bounded sample of orbit frames.
+
+--impl reference times that CPU implementation on the full orbit instead.
+Under torchrun each rank renders its own replica of the workload (the path
+has no exchange step); value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+W, H = 1920, 1080
+NFRAMES = 120
+VOLUME, SEED, SOLID = 256, 2, 0.08
+CENTRE = (128.0, 128.0, 128.0)
+RADIUS = 1.5 * 256 * math.sqrt(3.0)
+METRIC = "Mrays/s at 1080p on 256^3"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "render_best_1080p_256.md")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--frames", type=int, default=NFRAMES,
+                   help="orbit frames per step (profiling runs only; the benchmark uses 120)")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def workload_config(info=None, voxels=None):
+    cfg = {"workload": "orbit-1080p-256^3-best", "volume": "256^3 u8 value noise, seed 2, band ~8% solid",
+           "frames_per_step": NFRAMES, "resolution": f"{W}x{H}", "quality": "BEST",
+           "camera": "simple-camera fov 1.0, orbit r=665.1 elev 20deg",
+           "rays_per_step": NFRAMES * W * H, "l2": "flushed between steps (256 MiB write)"}
+    if voxels is not None:
+        cfg["voxels"] = int(voxels)
+    if info:
+        cfg.update({"tree_nodes": info["nodes"], "tree_depth": info["depth"],
+                    "tree_bytes": info["device_bytes"]})
+    return cfg
+
+
+def make_workload(build_tree):
+    from voxvision_gb300 import workloads as wl
+    vox = wl.voxels_from_mask(wl.noise_volume(VOLUME, SEED, SOLID))
+    tree = build_tree(vox)
+    return vox, tree, wl.texture32(7)
+
+
+def orbit_states():
+    from voxvision_gb300.cameras import orbit_camera
+    return [orbit_camera(f, NFRAMES, W, H, CENTRE, RADIUS).state() for f in range(NFRAMES)]
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken while the timed region runs."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """dram bytes per render launch from the committed ncu summary, if any."""
+    try:
+        txt = open(TRAFFIC_SUMMARY).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def l2_read_gbs(torch):
+    """Read bandwidth of an L2-resident 48 MiB buffer (torch sum), best of 30."""
+    x = torch.ones(12 << 20, dtype=torch.float32, device="cuda")
+    for _ in range(5):
+        x.sum()
+    best = 0.0
+    for _ in range(30):
+        a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+        a.record(); x.sum(); b.record(); b.synchronize()
+        best = max(best, x.numel() * 4 / (a.elapsed_time(b) * 1e-3) / 1e9)
+    return best
+
+
+def cpu_baseline_sample(tree_ptr, states, tex, budget_s=3.0):
+    """The oracle's BEST render on every host core over orbit frames (every
+    7th) until ~budget_s of wall time has passed."""
+    from oracle import oracle as orc
+    n = orc.nthreads_default()
+    frames, t0 = 0, time.perf_counter()
+    order = list(range(0, NFRAMES, 7)) + [f for f in range(NFRAMES) if f % 7]
+    for f in order:
+        orc.render_best(tree_ptr, states[f], W, H, tex, nthreads=n)
+        frames += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": frames * W * H / dt / 1e6, "unit": "Mrays/s", "cores": n, "kind": "port",
+            "sample": f"{frames} of the {NFRAMES} orbit frames at {W}x{H}, BEST, {dt:.2f} s wall"}
+
+
+# ------------------------------------------------------------------ our arm
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+    import torch.distributed as dist
+
+    import voxvision_gb300 as vg
+    from voxvision_gb300.build import build
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    if rank == 0 or not os.path.exists(vg._lib.LIB_PATH):
+        build()
+    if world > 1:
+        dist.barrier()
+    L = vg.lib()
+    vg.set_voxel_size((1, 1, 1))
+    vox, ht, tex = make_workload(vg.HostTree.from_voxels)
+    states = orbit_states()
+    cams = [vg.camera_struct(s) for s in states[:args.frames]]
+    nf = len(cams)
+    dt = vg.DeviceTree(ht.ptr)
+    info = dt.info()
+
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    d_tex = torch.from_numpy(tex).cuda()
+    frame = torch.empty(H * W, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # algorithmic work of one orbit (untimed)
+    counts = torch.zeros(3, dtype=torch.int64, device="cuda")
+    for c in cams:
+        dt.render_counts_device(c, W, H, counts, stream=sp)
+    torch.cuda.synchronize()
+    nodes, inner, voxels = (int(x) for x in counts.cpu().tolist())
+    rays_step = nf * W * H
+    alg_bytes_step = 32 * nodes + 16 * inner + 16 * voxels + 4 * rays_step
+
+    fn = L.vox_cuda_render_device
+    tex_p, frame_p = C.c_void_p(d_tex.data_ptr()), C.c_void_p(frame.data_ptr())
+    cam_refs = [C.byref(c) for c in cams]
+
+    def step(evs=None):
+        for i, cr in enumerate(cam_refs):
+            if evs is not None:
+                evs[i].record(stream)
+            rc = fn(dt.h, cr, W, H, tex_p, frame_p, sp)
+            if rc:
+                raise vg.VoxCudaError(rc, "vox_cuda_render_device")
+        if evs is not None:
+            evs[-1].record(stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = L.vox_cuda_launch_count()
+    all_evs = []
+    for _ in range(args.steps):
+        flush.zero_()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(nf + 1)]
+        step(evs)
+        all_evs.append(evs)
+    torch.cuda.synchronize()
+    launches = L.vox_cuda_launch_count() - launches0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [evs[0].elapsed_time(evs[-1]) for evs in all_evs]
+    launch_ms = [evs[i].elapsed_time(evs[i + 1]) for evs in all_evs for i in range(nf)]
+    total_s = sum(step_ms) * 1e-3
+    if world > 1:
+        t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * rays_step * args.steps / total_s / 1e6
+
+    # e2e: the host-buffer entry point, texture in and frame out every call
+    host_frame = torch.empty(H * W, dtype=torch.int32).pin_memory()
+    hf_p = C.c_void_p(host_frame.data_ptr())
+    htex = np.ascontiguousarray(tex)
+    htex_p = htex.ctypes.data_as(C.c_void_p)
+    fn_h = L.vox_cuda_render
+    for cr in cam_refs[:8]:
+        fn_h(dt.h, cr, W, H, htex_p, hf_p, sp)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for cr in cam_refs:
+            rc = fn_h(dt.h, cr, W, H, htex_p, hf_p, sp)
+            if rc:
+                raise vg.VoxCudaError(rc, "vox_cuda_render")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * rays_step * args.steps / e2e_s / 1e6, "unit": "Mrays/s",
+           "h2d_bytes_per_step": nf * 32768, "d2h_bytes_per_step": nf * W * H * 4,
+           "call": "vox_cuda_render (host texture in, host ARGB frame out, pinned)"}
+
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    peak, peak_kind = measured_peaks()
+    mean_launch_s = float(np.mean(launch_ms)) * 1e-3
+    achieved = alg_bytes_step / nf / mean_launch_s / 1e9
+    traffic = traffic_per_launch()
+    l2 = l2_read_gbs(torch)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "traffic": traffic, "kernel": "render_kernel (BEST, fused ray gen + search + colour)",
+                "alg_bytes_per_launch": alg_bytes_step / nf,
+                "mean_launch_ms": mean_launch_s * 1e3,
+                "bytes_per_ray": alg_bytes_step / rays_step,
+                "visits_per_ray": {"nodes": nodes / rays_step, "inner": inner / rays_step,
+                                   "voxels": voxels / rays_step},
+                "l2_read_gbs_measured": l2, "l2_frac": achieved / l2}
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sum(step_ms) / len(step_ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(workload_config(info, len(vox)), frames_per_step=nf, rays_per_step=rays_step), "roofline": roofline, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk}
+    if not args.no_cpu_baseline and world >= 1:
+        line["cpu_baseline"] = cpu_baseline_sample(ht.ptr, states, tex)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------ reference arm
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    orc.set_voxel((1, 1, 1))
+    vox, tree, tex = make_workload(orc.OracleTree.from_voxels)
+    states = orbit_states()
+    n = orc.nthreads_default()
+
+    def step():
+        for st in states:
+            orc.render_best(tree.ptr, st, W, H, tex, nthreads=n)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = NFRAMES * W * H * args.steps / dt / 1e6
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(None, len(vox)), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": n, "kind": "port",
+                             "sample": f"full {NFRAMES}-frame orbit per step, {W}x{H}, BEST, "
+                                       f"C restatement of search.c/renderer.c on {n} threads"},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

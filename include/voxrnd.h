@@ -1,0 +1,95 @@
+/*
+ * voxrnd.h -- the renderer and camera part of the reference API, as
+ * libvoxtrees_cuda exports it (drop-in for src/voxrnd/camera.h and
+ * src/voxrnd/renderer.h of shamazmazum/voxvision).
+ *
+ * Cameras are the reference's two classes, "simple-camera" and
+ * "doom-camera", with the same object layout, vtable order and arithmetic
+ * (simple-camera.c, doom-camera.c, vect-ops.c); they are built into the
+ * library instead of being loaded as plugins.  The renderer keeps the
+ * reference's context calls but draws into a headless ARGB8888 frame on the
+ * GPU: there is no SDL window or surface (no graphics stack is involved).
+ */
+#ifndef VOXRND_GB300_H
+#define VOXRND_GB300_H
+
+#include <stdint.h>
+
+#include "voxtrees.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct vox_camera;
+
+/* camera.h:17-117 (VOX_OBJECT's two property setters come first, object.h). */
+struct vox_camera_interface {
+    void (*set_property_number)(struct vox_camera *obj, const char *name, float value);
+    void (*set_property_dot)(struct vox_camera *obj, const char *name, const vox_dot value);
+    void (*screen2world)(const struct vox_camera *camera, vox_dot ray, int sx, int sy);
+    void (*rotate_camera)(struct vox_camera *camera, const vox_dot delta);
+    void (*move_camera)(struct vox_camera *camera, const vox_dot delta);
+    void (*look_at)(struct vox_camera *camera, const vox_dot coord);
+    void (*get_position)(const struct vox_camera *camera, vox_dot res);
+    void (*set_window_size)(struct vox_camera *camera, int w, int h);
+    struct vox_camera *(*construct_camera)(const struct vox_camera *camera);
+    void (*destroy_camera)(struct vox_camera *camera);
+};
+
+/* camera.h:133-136 */
+struct vox_camera {
+    struct vox_camera_interface *iface;
+};
+
+/* camera.h:175: methods of a camera class by name ("simple-camera",
+ * "doom-camera"); NULL for any other name. */
+struct vox_camera_interface *vox_camera_methods(const char *name);
+/* camera.h:146 */
+void vox_use_camera_methods(struct vox_camera *camera, const struct vox_camera_interface *iface);
+/* camera.h:160 */
+void vox_init_camera(struct vox_camera *camera);
+
+/* renderer.h quality flags */
+#define VOX_QUALITY_BEST 0x0
+#define VOX_QUALITY_FAST 0x1
+#define VOX_QUALITY_ADAPTIVE 0x2
+#define VOX_QUALITY_RAY_MERGE 0x4
+#define VOX_QUALITY_RAY_MERGE_ACCURATE 0x8
+#define VOX_QUALITY_RM_MASK 0xC
+#define VOX_QUALITY_MODE_MASK 0x3
+
+struct vox_rnd_ctx;
+
+/* Replaces vox_make_context_from_surface / vox_make_context_and_window
+ * (renderer.h:145,161): a context drawing into a w x h ARGB8888 frame held
+ * by the context (w a multiple of 16, h of 4, else NULL, renderer.c:97-100).
+ * The colour texture starts as the 32^3 splitmix64(seed 7) texture; see
+ * vox_context_set_texture. */
+struct vox_rnd_ctx *vox_make_context_headless(unsigned int width, unsigned int height);
+/* renderer.h:201 */
+void vox_destroy_context(struct vox_rnd_ctx *ctx);
+/* renderer.h:174 */
+void vox_context_set_scene(struct vox_rnd_ctx *ctx, struct vox_node *scene);
+/* renderer.h:179 (also calls the camera's set_window_size) */
+void vox_context_set_camera(struct vox_rnd_ctx *ctx, struct vox_camera *camera);
+/* renderer.h:196: 1 if accepted, 0 for an invalid combination */
+int vox_context_set_quality(struct vox_rnd_ctx *ctx, unsigned int quality);
+/* The 32^3 u8 colour texture (index x*1024 + y*32 + z); the reference
+ * generates it with vn3d (renderer.c:54-71), which is not part of this
+ * library. */
+void vox_context_set_texture(struct vox_rnd_ctx *ctx, const uint8_t *texture);
+/* renderer.h:208: render one frame on the GPU into the context's frame. */
+void vox_render(struct vox_rnd_ctx *ctx);
+/* renderer.h:169: makes the frame of the last vox_render visible through
+ * vox_context_pixels. */
+void vox_redraw(struct vox_rnd_ctx *ctx);
+/* The ARGB8888 frame, pixel (x, y) at [y * width + x]; misses are 0. */
+const uint32_t *vox_context_pixels(const struct vox_rnd_ctx *ctx);
+/* VOX_CUDA_OK or the error of the last vox_render / vox_redraw. */
+int vox_context_status(const struct vox_rnd_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,81 @@
+/*
+ * voxtrees.h -- the voxtrees part of the reference API, as libvoxtrees_cuda
+ * exports it (drop-in for src/voxtrees/tree.h and src/voxtrees/search.h of
+ * shamazmazum/voxvision, scalar build).
+ *
+ * The node layout is the reference's own (tree.h:13-38 with the scalar
+ * vox_dot of voxvision.h.in:57) so that trees built by either library can be
+ * handed to vox_cuda_tree_upload.  Tree construction stays on the host and
+ * follows tree.c:249-338 step for step; the searches run on the GPU.
+ */
+#ifndef VOXTREES_GB300_H
+#define VOXTREES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef float vox_dot[3];     /* voxvision.h.in:57 (SSE_INTRIN off) */
+typedef float vox_quat[4];    /* voxvision.h.in:58 */
+
+struct vox_box {              /* voxvision.h.in:79-83 */
+    vox_dot min;
+    vox_dot max;
+};
+
+#define VOX_LEAF 1            /* tree.h:15-18 */
+#define VOX_DENSE_LEAF 2
+#define VOX_LEAF_MASK 3
+#define VOX_OVERFLOW 4
+#define VOX_MAX_DOTS 7        /* params.h:29 */
+
+typedef struct {              /* tree.h:22-26 */
+    vox_dot center;
+    struct vox_node *children[8];
+} vox_inner_data;
+
+struct vox_node {             /* tree.h:28-38 */
+    struct vox_box bounding_box;
+    unsigned int flags;
+    unsigned int dots_num;
+    union {
+        vox_dot *dots;
+        vox_inner_data inner;
+    } data;
+};
+
+/* Voxel size (tree.c:11).  Read by vox_make_tree and by vox_cuda_tree_upload. */
+extern vox_dot vox_voxel;
+
+/* tree.h:60 -- build a tree; `set` is reordered in place and may be freed after. */
+struct vox_node *vox_make_tree(vox_dot set[], size_t n);
+/* tree.h:67 */
+void vox_destroy_tree(struct vox_node *tree);
+/* tree.h:72 */
+size_t vox_voxels_in_tree(const struct vox_node *tree);
+/* tree.h:77 */
+void vox_bounding_box(const struct vox_node *tree, struct vox_box *box);
+/* tree.h:140 */
+struct vox_node *vox_make_dense_leaf(const struct vox_box *box);
+/* tree.h:149 */
+void vox_set_voxel_size(float x, float y, float z);
+
+/* search.h:24-26 -- one ray, run on the GPU.  The tree (or the tree that
+ * contains `tree`, which may be any of its nodes) is uploaded on first use and
+ * kept until vox_cuda_forget_tree; after editing a tree, call that before the
+ * next search.  Returns the leaf the reference returns, or NULL; `res` is
+ * written on a hit only. */
+const struct vox_node *vox_ray_tree_intersection(const struct vox_node *tree, const vox_dot origin,
+                                                 const vox_dot dir, vox_dot res);
+/* search.h:36-37 -- one ball query, run on the GPU (same caching). */
+int vox_tree_ball_collidep(const struct vox_node *tree, const vox_dot center, float radius);
+
+/* Drop the cached device copy of the tree rooted at `root` (no-op if none). */
+void vox_cuda_forget_tree(const struct vox_node *root);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,179 @@
+/*
+ * voxtrees_cuda.h -- C ABI of libvoxtrees_cuda, the GB300 (sm_103a) ray and
+ * ball search over voxtrees octrees.
+ *
+ * A host tree (struct vox_node, as built by vox_make_tree) is flattened once
+ * into one device pool (vox_cuda_tree_upload); batched entry points then run
+ * the reference's searches on the GPU:
+ *
+ *   vox_cuda_ray_batch*   <- vox_ray_tree_intersection  (src/voxtrees/search.h:24-26)
+ *   vox_cuda_ball_batch*  <- vox_tree_ball_collidep     (src/voxtrees/search.h:36-37)
+ *   vox_cuda_render*      <- vox_render, BEST quality   (src/voxrnd/renderer.h:208,
+ *                                                        renderer.c:200-319)
+ *
+ * Results are bit-identical to the reference's CPU code: the same leaf, the
+ * same winning voxel, the same float bits of the intersection point.
+ *
+ * Conventions.  Every function returns VOX_CUDA_OK (0) or a negative
+ * VOX_CUDA_E* code and never aborts.  `stream` is a cudaStream_t passed as
+ * void* (NULL = the legacy default stream).  Functions named *_device take
+ * device pointers and only enqueue work on `stream`; the others take host
+ * pointers, copy inside the call and return when the results are in host
+ * memory.  The caller owns host buffers; the library owns the device pool of
+ * each uploaded tree.  A tree handle may be used from several threads and
+ * streams at once (it is read-only after upload).
+ *
+ * Leaf identity.  A leaf is reported as its pre-order index among the
+ * non-NULL nodes of the uploaded tree (node first, then children 0..7);
+ * vox_cuda_tree_node maps it back to the host struct vox_node pointer that
+ * vox_ray_tree_intersection would have returned.  VOX_CUDA_MISS marks a miss.
+ */
+#ifndef VOXTREES_CUDA_H
+#define VOXTREES_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VOX_CUDA_OK          0
+#define VOX_CUDA_EINVAL     -1   /* bad argument                                   */
+#define VOX_CUDA_ENOMEM     -2   /* host or device allocation failed               */
+#define VOX_CUDA_ECUDA      -3   /* a CUDA runtime call failed                     */
+#define VOX_CUDA_EDEPTH     -4   /* tree deeper than the traversal stack supports  */
+#define VOX_CUDA_ESTACK     -5   /* a kernel reported a traversal-stack overflow   */
+#define VOX_CUDA_ETOOBIG    -6   /* flattened tree exceeds the 4 GiB pool limit    */
+#define VOX_CUDA_EGEOMETRY  -7   /* frame size not a multiple of 16 x 4            */
+#define VOX_CUDA_EBUDGET    -8   /* admission budget exceeded                      */
+#define VOX_CUDA_ETIMEOUT   -9   /* a bounded wait gave up                         */
+#define VOX_CUDA_ENODEV    -10   /* no usable CUDA device                          */
+
+#define VOX_CUDA_MISS       0xFFFFFFFFu
+#define VOX_CUDA_SLOT_DENSE 0xFFu
+
+#define VOX_CUDA_CAMERA_SIMPLE 0   /* simple-camera.c: quaternion rotation      */
+#define VOX_CUDA_CAMERA_DOOM   1   /* doom-camera.c: yaw + vertical shift k     */
+
+struct vox_node;
+typedef struct vox_cuda_tree vox_cuda_tree;
+
+/* The state screen2world reads, for the two camera classes the reference
+ * ships (simple-camera.c:10-17, doom-camera.c:8-15). */
+typedef struct {
+    int32_t kind;
+    float position[3];
+    float rotation[4];           /* simple: unit quaternion (w, i, j, k)      */
+    float mul, xsub, ysub;       /* set_window_size (simple-camera.c:120-136) */
+    float sinphi, cosphi, k;     /* doom only                                 */
+} vox_cuda_camera;
+
+typedef struct {
+    uint64_t nodes;          /* non-NULL nodes                            */
+    uint64_t inner;          /* inner nodes                               */
+    uint64_t leaves;         /* regular (incl. overflowed) leaves         */
+    uint64_t dense_leaves;   /* dense leaves                              */
+    uint64_t dots;           /* voxels stored in regular leaves           */
+    uint64_t depth;          /* inner nodes on the longest root-leaf path */
+    uint64_t device_bytes;   /* bytes of the device pool                  */
+} vox_cuda_tree_info;
+
+const char *vox_cuda_strerror(int code);
+
+/* Flatten `root` (any tree built with the reference node layout; NULL is the
+ * empty tree) into a device pool on the current device.  The voxel size is
+ * read from vox_voxel now and embedded in the pool.  Replaces: nothing in the
+ * reference (the reference searches host memory directly). */
+int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out);
+int vox_cuda_tree_free(vox_cuda_tree *tree);
+/* Flatten and check `root` on the host only (no device needed) and report
+ * what vox_cuda_tree_upload would allocate: the basis of memory budgets.
+ * VOX_CUDA_EDEPTH / ETOOBIG as the upload would return them. */
+int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info *info);
+int vox_cuda_tree_get_info(const vox_cuda_tree *tree, vox_cuda_tree_info *info);
+/* Pre-order index -> host node (NULL when out of range). */
+const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *tree, uint32_t id);
+/* Host node -> pre-order index; VOX_CUDA_EINVAL when the node is not in the tree. */
+int vox_cuda_tree_node_id(const vox_cuda_tree *tree, const struct vox_node *node, uint32_t *id);
+
+/* Ray batch.  origins, dirs: n x 3 floats.  Outputs per ray: leaf_id
+ * (pre-order index or VOX_CUDA_MISS), slot (index of the winning voxel in a
+ * regular leaf, VOX_CUDA_SLOT_DENSE for a dense leaf or a miss), points
+ * (n x 3, written only on a hit, like `res`).  roots: NULL to start every
+ * ray at the tree's root, else n pre-order indices of the node each search
+ * starts from (vox_ray_tree_intersection accepts any node as its root;
+ * renderer.c:297).  slot and points may be NULL.
+ * Replaces vox_ray_tree_intersection (src/voxtrees/search.h:24-26). */
+int vox_cuda_ray_batch(const vox_cuda_tree *tree, const float *origins, const float *dirs,
+                       const uint32_t *roots, size_t n, uint32_t *leaf_id, uint8_t *slot,
+                       float *points, void *stream);
+int vox_cuda_ray_batch_device(const vox_cuda_tree *tree, const float *origins, const float *dirs,
+                              const uint32_t *roots, size_t n, uint32_t *leaf_id, uint8_t *slot,
+                              float *points, void *stream);
+
+/* Ball batch.  centres: n x 3 floats, radii: n floats -> hit[i] = 0 / 1.
+ * Replaces vox_tree_ball_collidep (src/voxtrees/search.h:36-37). */
+int vox_cuda_ball_batch(const vox_cuda_tree *tree, const float *centres, const float *radii,
+                        size_t n, uint8_t *hit, void *stream);
+int vox_cuda_ball_batch_device(const vox_cuda_tree *tree, const float *centres,
+                               const float *radii, size_t n, uint8_t *hit, void *stream);
+
+/* One BEST-quality frame: camera ray generation, search and the colour
+ * lookup fused in one kernel, written to a linear w x h ARGB8888 frame
+ * (pixel (x, y) at argb[y * w + x]; misses are 0).  texture: the 32^3 u8
+ * colour texture (index x*1024 + y*32 + z).  w must be a multiple of 16 and
+ * h of 4 (renderer.c:97-100).
+ * Replaces vox_render + vox_redraw with quality VOX_QUALITY_BEST
+ * (src/voxrnd/renderer.c:200-327). */
+int vox_cuda_render(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
+                    uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
+                    void *stream);
+int vox_cuda_render_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
+                           uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
+                           void *stream);
+
+/* Quality values of vox_context_set_quality (src/voxrnd/renderer.h). */
+#define VOX_CUDA_QUALITY_BEST                0x0
+#define VOX_CUDA_QUALITY_FAST                0x1
+#define VOX_CUDA_QUALITY_ADAPTIVE            0x2
+#define VOX_CUDA_QUALITY_RAY_MERGE           0x4
+#define VOX_CUDA_QUALITY_RAY_MERGE_ACCURATE  0x8
+#define VOX_CUDA_QUALITY_RM_MASK             0xC
+#define VOX_CUDA_QUALITY_MODE_MASK           0x3
+
+/* One frame in any quality the reference accepts (renderer.c:179-195):
+ * BEST runs the per-pixel kernel above; FAST and ADAPTIVE (with or without
+ * ray merging) run one thread per 4x4 square in the reference's Z-order,
+ * reusing the previous pixel's leaf as the search root (renderer.c:215-318).
+ * Pixels the reference leaves undrawn are 0.  EINVAL for a combination
+ * vox_context_set_quality rejects.
+ * Replaces vox_render + vox_redraw (src/voxrnd/renderer.c:200-327). */
+int vox_cuda_render_quality(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
+                            uint32_t w, uint32_t h, unsigned int quality, const uint8_t *texture,
+                            uint32_t *argb, void *stream);
+int vox_cuda_render_quality_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
+                                   uint32_t w, uint32_t h, unsigned int quality,
+                                   const uint8_t *texture, uint32_t *argb, void *stream);
+
+/* Work counters of the same searches (no results): counts[0] = nodes whose
+ * box was tested, counts[1] = inner nodes entered, counts[2] = voxels
+ * tested, summed over the batch or frame (the reference's probes
+ * rti__voxels__traversed etc., src/voxtrees/voxtrees-dtrace.d).  counts is a
+ * device pointer to 3 uint64 that the call adds to. */
+int vox_cuda_render_counts_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
+                                  uint32_t w, uint32_t h, uint64_t *counts, void *stream);
+int vox_cuda_ray_counts_device(const vox_cuda_tree *tree, const float *origins, const float *dirs,
+                               size_t n, uint64_t *counts, void *stream);
+int vox_cuda_ball_counts_device(const vox_cuda_tree *tree, const float *centres,
+                                const float *radii, size_t n, uint64_t *counts, void *stream);
+
+/* Library version and the number of kernel launches made so far by this
+ * process (all entry points); used to report launch counts. */
+const char *vox_cuda_version(void);
+uint64_t vox_cuda_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

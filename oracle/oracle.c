@@ -581,6 +581,92 @@ int orc_render_best(const struct orc_node *tree, const orc_camera *cam,
     return 0;
 }
 
+/* renderer.c:215-318 for any quality: per 4x4 square, Z-order, FAST leaf
+ * reuse, ADAPTIVE corner test, ray merging.  Undrawn pixels stay 0. */
+typedef struct {
+    const struct orc_node *tree;
+    const orc_camera *cam;
+    int w, ws;
+    unsigned quality;
+    const uint8_t *tex;
+    uint32_t *argb;
+} quality_ctx;
+
+static float sqr_norm(const float *a)
+{
+    float r = 0;
+    for (int i = 0; i < 3; i++) r += a[i] * a[i];
+    return r;
+}
+
+static void quality_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
+{
+    quality_ctx *x = vctx;
+    int rnd_mode = x->quality & 3, merge_mode = x->quality & 12;
+    const float *origin = x->cam->position;
+    for (size_t cs = lo; cs < hi; cs++) {
+        int ystart = (int)(cs / (size_t)x->ws) * 4, xstart = (int)(cs % (size_t)x->ws) * 4;
+        uint32_t out[16] = {0};
+        const struct orc_node *leaf = NULL;
+        float dir1[3], dir2[3], inter1[3], inter2[3];
+        int block_mode = rnd_mode, istart = 0, iend = 16, block_merge = 0;
+        if (block_mode == 2) {
+            block_merge = (merge_mode == 4);
+            istart = 1;
+            orc_screen2world(x->cam, xstart, ystart, dir1);
+            const struct orc_node *c1 = orc_ray(x->tree, origin, dir1, inter1, NULL, c);
+            block_mode = 1;
+            leaf = c1;
+            if (c1) {
+                iend = 15;
+                out[0] = get_color(x->tex, inter1);
+                orc_screen2world(x->cam, xstart + 3, ystart + 3, dir2);
+                const struct orc_node *c2 = orc_ray(x->tree, origin, dir2, inter2, NULL, c);
+                if (c2) {
+                    out[15] = get_color(x->tex, inter2);
+                    float d1 = sqr_metric(inter1, origin);
+                    float d2 = sqr_norm(dir1);
+                    float criteria = d1 / d2 * sqr_metric(dir1, dir2);
+                    float dist = sqr_metric(inter1, inter2);
+                    if (dist / criteria > 1.69) block_mode = 0;
+                    if (d1 > 150 * 150)
+                        block_merge = (block_mode == 1 && merge_mode == 8) ? 1 : block_merge;
+                    else
+                        block_merge = 0;
+                }
+            }
+        }
+        int prev_p = 0;
+        for (int i = istart; i < iend; i++) {
+            int p = zorder[i];
+            int merge = block_merge && (i & 1);
+            orc_screen2world(x->cam, p % 4 + xstart, p / 4 + ystart, dir1);
+            if (!merge) {
+                if (block_mode == 1) {
+                    if (leaf) leaf = orc_ray(leaf, origin, dir1, inter1, NULL, c);
+                    if (!leaf) leaf = orc_ray(x->tree, origin, dir1, inter1, NULL, c);
+                } else {
+                    leaf = orc_ray(x->tree, origin, dir1, inter1, NULL, c);
+                }
+            }
+            if (leaf) out[p] = merge ? out[prev_p] : get_color(x->tex, inter1);
+            prev_p = p;
+        }
+        for (int i = 0; i < 16; i++)
+            x->argb[(size_t)(ystart + i / 4) * x->w + xstart + i % 4] = out[i];
+    }
+}
+
+int orc_render_quality(const struct orc_node *tree, const orc_camera *cam, int w, int h,
+                       unsigned quality, const uint8_t *texture, uint32_t *argb,
+                       uint64_t *counts3, int nthreads)
+{
+    if ((w & 0xf) || (h & 0x3)) return -1;
+    quality_ctx x = {tree, cam, w, w / 4, quality, texture, argb};
+    run_pool((size_t)(w / 4) * (size_t)(h / 4), 64, nthreads, quality_work, &x, counts3);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* dumps                                                               */
 /* ------------------------------------------------------------------ */

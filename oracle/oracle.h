@@ -100,6 +100,12 @@ int orc_render_best(const struct orc_node *tree, const orc_camera *cam,
                     int w, int h, const uint8_t *texture, uint32_t *argb,
                     uint64_t *counts3, int nthreads);
 
+/* vox_render in any quality (renderer.c:215-318): BEST, FAST, ADAPTIVE,
+ * ADAPTIVE with ray merging.  Pixels the reference leaves undrawn are 0. */
+int orc_render_quality(const struct orc_node *tree, const orc_camera *cam,
+                       int w, int h, unsigned quality, const uint8_t *texture,
+                       uint32_t *argb, uint64_t *counts3, int nthreads);
+
 /* Pre-order dump of a tree: per node flags, dots_num, box (6 floats), centre
  * (3 floats, inner nodes), child mask (inner nodes) and an offset into the
  * dots array (leaves).  Returns the node count; arrays must be sized by

@@ -52,6 +52,9 @@ def lib():
         L.orc_screen2world.argtypes = [C.POINTER(OrcCamera), C.c_int, C.c_int, fp]
         L.orc_render_best.argtypes = [vp, C.POINTER(OrcCamera), C.c_int, C.c_int, vp, vp, vp, C.c_int]
         L.orc_render_best.restype = C.c_int
+        L.orc_render_quality.argtypes = [vp, C.POINTER(OrcCamera), C.c_int, C.c_int, C.c_uint, vp, vp,
+                                         vp, C.c_int]
+        L.orc_render_quality.restype = C.c_int
         L.orc_dump.argtypes = [vp] * 8; L.orc_dump.restype = sz
         L.orc_from_dump.argtypes = [sz] + [vp] * 7; L.orc_from_dump.restype = vp
         _lib = L
@@ -172,6 +175,18 @@ def render_best(tree_ptr, state: dict, w: int, h: int, texture: np.ndarray, nthr
     cnt = np.zeros(3, np.uint64)
     rc = lib().orc_render_best(tree_ptr, C.byref(camera(state)), w, h, _p(tex), _p(out), _p(cnt),
                                nthreads or nthreads_default())
+    if rc != 0:
+        raise ValueError("bad geometry: width must be a multiple of 16 and height of 4")
+    return out.reshape(h, w), cnt
+
+
+def render_quality(tree_ptr, state: dict, w: int, h: int, quality: int, texture: np.ndarray,
+                   nthreads=None):
+    tex = np.ascontiguousarray(texture, dtype=np.uint8)
+    out = np.zeros(w * h, np.uint32)
+    cnt = np.zeros(3, np.uint64)
+    rc = lib().orc_render_quality(tree_ptr, C.byref(camera(state)), w, h, quality, _p(tex), _p(out),
+                                  _p(cnt), nthreads or nthreads_default())
     if rc != 0:
         raise ValueError("bad geometry: width must be a multiple of 16 and height of 4")
     return out.reshape(h, w), cnt

@@ -1,0 +1,188 @@
+"""voxvision_gb300: the voxtrees ray/ball search path of shamazmazum/voxvision
+on GB300 (sm_103a), behind the reference's C API.
+
+Python here is a thin host layer over the C ABI of libvoxtrees_cuda.so
+(include/voxtrees_cuda.h, include/voxtrees.h): tests and the benchmark call
+the library exactly as a C program would.  numpy arrays are host buffers;
+torch tensors (or raw integers) are device pointers for the *_device entry
+points.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, CameraStruct,
+                   TreeInfo, VoxCudaError, available, check, lib)
+
+__all__ = ["HostTree", "DeviceTree", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
+           "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size"]
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _dptr(x):
+    """Device pointer of a torch tensor, an int, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return C.c_void_p(x)
+    return C.c_void_p(x.data_ptr())
+
+
+def set_voxel_size(v=(1.0, 1.0, 1.0)):
+    lib().vox_set_voxel_size(*[float(a) for a in v])
+
+
+class HostTree:
+    """A host octree built by the library's vox_make_tree (tree.c:249-338 order)."""
+
+    def __init__(self, ptr: int | None, owned: bool = True):
+        self.ptr = ptr
+        self.owned = owned
+
+    @classmethod
+    def from_voxels(cls, voxels: np.ndarray) -> "HostTree":
+        s = np.ascontiguousarray(voxels, dtype=np.float32).copy()   # the build reorders its input
+        if s.ndim != 2 or s.shape[1] != 3:
+            raise ValueError("voxels must be (n, 3)")
+        return cls(lib().vox_make_tree(_p(s), s.shape[0]))
+
+    def voxels(self) -> int:
+        return int(lib().vox_voxels_in_tree(self.ptr)) if self.ptr else 0
+
+    def close(self):
+        if self.ptr and self.owned:
+            lib().vox_destroy_tree(self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def measure_tree(host_ptr) -> dict:
+    """vox_cuda_tree_measure: flatten and check on the host, report sizes."""
+    i = TreeInfo()
+    check(lib().vox_cuda_tree_measure(host_ptr, C.byref(i)), "vox_cuda_tree_measure")
+    return {k: int(getattr(i, k)) for k, _ in TreeInfo._fields_}
+
+
+class DeviceTree:
+    """A tree uploaded with vox_cuda_tree_upload."""
+
+    def __init__(self, host_ptr):
+        h = C.c_void_p()
+        check(lib().vox_cuda_tree_upload(host_ptr, C.byref(h)), "vox_cuda_tree_upload")
+        self.h = h
+
+    def info(self) -> dict:
+        i = TreeInfo()
+        check(lib().vox_cuda_tree_get_info(self.h, C.byref(i)), "vox_cuda_tree_get_info")
+        return {k: int(getattr(i, k)) for k, _ in TreeInfo._fields_}
+
+    def node(self, preorder_id: int):
+        return lib().vox_cuda_tree_node(self.h, preorder_id)
+
+    def node_id(self, host_node_ptr) -> int:
+        v = C.c_uint32()
+        check(lib().vox_cuda_tree_node_id(self.h, host_node_ptr, C.byref(v)), "vox_cuda_tree_node_id")
+        return int(v.value)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().vox_cuda_tree_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------- host buffers
+    def rays(self, origins, dirs, roots=None, stream=None):
+        o = np.ascontiguousarray(origins, dtype=np.float32)
+        d = np.ascontiguousarray(dirs, dtype=np.float32)
+        n = o.shape[0]
+        leaf = np.empty(n, np.uint32)
+        slot = np.empty(n, np.uint8)
+        pts = np.zeros((n, 3), np.float32)
+        r = None if roots is None else np.ascontiguousarray(roots, dtype=np.uint32)
+        check(lib().vox_cuda_ray_batch(self.h, _p(o), _p(d), None if r is None else _p(r), n,
+                                       _p(leaf), _p(slot), _p(pts), stream),
+              "vox_cuda_ray_batch")
+        return leaf, slot, pts
+
+    def balls(self, centres, radii, stream=None):
+        c = np.ascontiguousarray(centres, dtype=np.float32)
+        r = np.ascontiguousarray(radii, dtype=np.float32)
+        hit = np.empty(c.shape[0], np.uint8)
+        check(lib().vox_cuda_ball_batch(self.h, _p(c), _p(r), c.shape[0], _p(hit), stream),
+              "vox_cuda_ball_batch")
+        return hit
+
+    def render(self, camera: CameraStruct, w: int, h: int, texture: np.ndarray, stream=None):
+        tex = np.ascontiguousarray(texture, dtype=np.uint8)
+        out = np.empty((h, w), np.uint32)
+        check(lib().vox_cuda_render(self.h, C.byref(camera), w, h, _p(tex), _p(out), stream),
+              "vox_cuda_render")
+        return out
+
+    def render_quality(self, camera: CameraStruct, w: int, h: int, quality: int, texture: np.ndarray,
+                       stream=None):
+        tex = np.ascontiguousarray(texture, dtype=np.uint8)
+        out = np.empty((h, w), np.uint32)
+        check(lib().vox_cuda_render_quality(self.h, C.byref(camera), w, h, quality, _p(tex), _p(out),
+                                            stream), "vox_cuda_render_quality")
+        return out
+
+    # -------------------------------------------------------- device buffers
+    def rays_device(self, origins, dirs, leaf, slot=None, points=None, roots=None, n=None, stream=None):
+        n = int(origins.shape[0]) if n is None else n
+        check(lib().vox_cuda_ray_batch_device(self.h, _dptr(origins), _dptr(dirs), _dptr(roots), n,
+                                              _dptr(leaf), _dptr(slot), _dptr(points), stream),
+              "vox_cuda_ray_batch_device")
+
+    def balls_device(self, centres, radii, hit, n=None, stream=None):
+        n = int(centres.shape[0]) if n is None else n
+        check(lib().vox_cuda_ball_batch_device(self.h, _dptr(centres), _dptr(radii), n, _dptr(hit),
+                                               stream), "vox_cuda_ball_batch_device")
+
+    def render_device(self, camera: CameraStruct, w: int, h: int, texture, argb, stream=None):
+        check(lib().vox_cuda_render_device(self.h, C.byref(camera), w, h, _dptr(texture), _dptr(argb),
+                                           stream), "vox_cuda_render_device")
+
+    def render_counts_device(self, camera: CameraStruct, w: int, h: int, counts, stream=None):
+        check(lib().vox_cuda_render_counts_device(self.h, C.byref(camera), w, h, _dptr(counts), stream),
+              "vox_cuda_render_counts_device")
+
+    def ray_counts_device(self, origins, dirs, counts, n=None, stream=None):
+        n = int(origins.shape[0]) if n is None else n
+        check(lib().vox_cuda_ray_counts_device(self.h, _dptr(origins), _dptr(dirs), n, _dptr(counts),
+                                               stream), "vox_cuda_ray_counts_device")
+
+    def ball_counts_device(self, centres, radii, counts, n=None, stream=None):
+        n = int(centres.shape[0]) if n is None else n
+        check(lib().vox_cuda_ball_counts_device(self.h, _dptr(centres), _dptr(radii), n, _dptr(counts),
+                                                stream), "vox_cuda_ball_counts_device")
+
+
+def camera_struct(state: dict) -> CameraStruct:
+    """vox_cuda_camera from a dict of camera state (position, rotation, mul,
+    xsub, ysub; sinphi, cosphi, k for the doom camera)."""
+    cam = CameraStruct()
+    cam.kind = int(state.get("kind", CAMERA_SIMPLE))
+    cam.position[:] = [float(x) for x in state["position"]]
+    cam.rotation[:] = [float(x) for x in state.get("rotation", (1.0, 0.0, 0.0, 0.0))]
+    for k in ("mul", "xsub", "ysub", "sinphi", "cosphi", "k"):
+        setattr(cam, k, float(state.get(k, 0.0)))
+    return cam
+
+
+Camera = CameraStruct

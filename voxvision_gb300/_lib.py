@@ -1,0 +1,121 @@
+"""ctypes binding of libvoxtrees_cuda.so (the C ABI in include/voxtrees_cuda.h,
+include/voxtrees.h and include/voxrnd.h).
+
+The library is built in-tree by voxvision_gb300.build; importing this module
+never builds and never falls back to anything: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvoxtrees_cuda.so")
+
+VOX_CUDA_MISS = 0xFFFFFFFF
+VOX_CUDA_SLOT_DENSE = 0xFF
+CAMERA_SIMPLE = 0
+CAMERA_DOOM = 1
+
+ERRORS = {
+    0: "ok", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EDEPTH", -5: "ESTACK",
+    -6: "ETOOBIG", -7: "EGEOMETRY", -8: "EBUDGET", -9: "ETIMEOUT", -10: "ENODEV",
+}
+
+
+class VoxCudaError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"{what}: {ERRORS.get(code, code)} ({code})")
+
+
+class CameraStruct(C.Structure):
+    """vox_cuda_camera (include/voxtrees_cuda.h)."""
+    _fields_ = [("kind", C.c_int32), ("position", C.c_float * 3), ("rotation", C.c_float * 4),
+                ("mul", C.c_float), ("xsub", C.c_float), ("ysub", C.c_float),
+                ("sinphi", C.c_float), ("cosphi", C.c_float), ("k", C.c_float)]
+
+
+class TreeInfo(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in
+                ("nodes", "inner", "leaves", "dense_leaves", "dots", "depth", "device_bytes")]
+
+
+_lib = None
+
+# name -> (restype, argtypes)
+_vp, _sz, _u32, _f = C.c_void_p, C.c_size_t, C.c_uint32, C.c_float
+SIGNATURES = {
+    "vox_cuda_strerror": (C.c_char_p, [C.c_int]),
+    "vox_cuda_version": (C.c_char_p, []),
+    "vox_cuda_launch_count": (C.c_uint64, []),
+    "vox_cuda_tree_upload": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "vox_cuda_tree_free": (C.c_int, [_vp]),
+    "vox_cuda_tree_measure": (C.c_int, [_vp, C.POINTER(TreeInfo)]),
+    "vox_cuda_tree_get_info": (C.c_int, [_vp, C.POINTER(TreeInfo)]),
+    "vox_cuda_tree_node": (_vp, [_vp, _u32]),
+    "vox_cuda_tree_node_id": (C.c_int, [_vp, _vp, C.POINTER(_u32)]),
+    "vox_cuda_ray_batch": (C.c_int, [_vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp]),
+    "vox_cuda_ray_batch_device": (C.c_int, [_vp, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp]),
+    "vox_cuda_ball_batch": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
+    "vox_cuda_ball_batch_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
+    "vox_cuda_render": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp, _vp]),
+    "vox_cuda_render_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp, _vp]),
+    "vox_cuda_render_quality": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp, _vp,
+                                          _vp]),
+    "vox_cuda_render_quality_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp,
+                                                 _vp, _vp]),
+    "vox_cuda_render_counts_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp]),
+    "vox_cuda_ray_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
+    "vox_cuda_ball_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
+    # voxtrees.h
+    "vox_make_tree": (_vp, [_vp, _sz]),
+    "vox_destroy_tree": (None, [_vp]),
+    "vox_voxels_in_tree": (_sz, [_vp]),
+    "vox_bounding_box": (None, [_vp, _vp]),
+    "vox_make_dense_leaf": (_vp, [_vp]),
+    "vox_set_voxel_size": (None, [_f, _f, _f]),
+    "vox_ray_tree_intersection": (_vp, [_vp, _vp, _vp, _vp]),
+    "vox_tree_ball_collidep": (C.c_int, [_vp, _vp, _f]),
+    "vox_cuda_forget_tree": (None, [_vp]),
+    # voxrnd.h (cameras)
+    "vox_camera_methods": (_vp, [C.c_char_p]),
+    "vox_init_camera": (None, [_vp]),
+    "vox_use_camera_methods": (None, [_vp, _vp]),
+    # voxrnd.h (renderer)
+    "vox_make_context_headless": (_vp, [C.c_uint, C.c_uint]),
+    "vox_destroy_context": (None, [_vp]),
+    "vox_context_set_scene": (None, [_vp, _vp]),
+    "vox_context_set_camera": (None, [_vp, _vp]),
+    "vox_context_set_quality": (C.c_int, [_vp, C.c_uint]),
+    "vox_context_set_texture": (None, [_vp, _vp]),
+    "vox_render": (None, [_vp]),
+    "vox_redraw": (None, [_vp]),
+    "vox_context_pixels": (_vp, [_vp]),
+    "vox_context_status": (C.c_int, [_vp]),
+}
+
+
+def available() -> bool:
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run voxvision_gb300.build.build() first "
+                               "(there is no fallback implementation)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        raise VoxCudaError(rc, what)

@@ -1,0 +1,97 @@
+/*
+ * dropin_search.cpp -- vox_ray_tree_intersection and vox_tree_ball_collidep
+ * with the reference's signatures (src/voxtrees/search.h:24-26, :36-37),
+ * answered on the GPU.
+ *
+ * The reference accepts any node as the search root (renderer.c:297 passes a
+ * leaf).  A registry of uploaded trees maps a node pointer to (device tree,
+ * pre-order id); a pointer found in no registered tree is taken as the root
+ * of a new tree and uploaded.  Edited trees must be dropped with
+ * vox_cuda_forget_tree before the next search.  These single-query calls
+ * cost a round trip each; batches belong in vox_cuda_ray_batch.
+ */
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/voxtrees.h"
+#include "../../include/voxtrees_cuda.h"
+
+#define EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+struct Entry {
+    const vox_node *root;
+    vox_cuda_tree *tree;
+};
+
+std::mutex g_mu;
+std::vector<Entry> g_trees;
+
+// Device tree holding `node` and the node's pre-order id, uploading a new
+// tree rooted at `node` when no registered tree contains it.
+bool resolve(const vox_node *node, vox_cuda_tree **tree, uint32_t *id)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (const Entry &e : g_trees) {
+        if (vox_cuda_tree_node_id(e.tree, node, id) == VOX_CUDA_OK) {
+            *tree = e.tree;
+            return true;
+        }
+    }
+    vox_cuda_tree *t = nullptr;
+    if (vox_cuda_tree_upload(node, &t) != VOX_CUDA_OK) return false;
+    g_trees.push_back({node, t});
+    *tree = t;
+    *id = 0;
+    return true;
+}
+
+}  // namespace
+
+EXPORT const struct vox_node *vox_ray_tree_intersection(const struct vox_node *tree, const vox_dot origin,
+                                                        const vox_dot dir, vox_dot res)
+{
+    if (!tree) return nullptr;
+    vox_cuda_tree *t;
+    uint32_t id;
+    if (!resolve(tree, &t, &id)) return nullptr;
+    uint32_t leaf = VOX_CUDA_MISS;
+    if (vox_cuda_ray_batch(t, origin, dir, id ? &id : nullptr, 1, &leaf, nullptr, res, nullptr) != VOX_CUDA_OK)
+        return nullptr;
+    return leaf == VOX_CUDA_MISS ? nullptr : vox_cuda_tree_node(t, leaf);
+}
+
+EXPORT int vox_tree_ball_collidep(const struct vox_node *tree, const vox_dot center, float radius)
+{
+    if (!tree) return 0;
+    vox_cuda_tree *t;
+    uint32_t id;
+    if (!resolve(tree, &t, &id)) return 0;
+    if (id != 0) {
+        // A ball query below the root: upload that subtree on its own.
+        std::lock_guard<std::mutex> lock(g_mu);
+        vox_cuda_tree *sub = nullptr;
+        if (vox_cuda_tree_upload(tree, &sub) != VOX_CUDA_OK) return 0;
+        uint8_t hit = 0;
+        int rc = vox_cuda_ball_batch(sub, center, &radius, 1, &hit, nullptr);
+        vox_cuda_tree_free(sub);
+        return rc == VOX_CUDA_OK ? hit : 0;
+    }
+    uint8_t hit = 0;
+    if (vox_cuda_ball_batch(t, center, &radius, 1, &hit, nullptr) != VOX_CUDA_OK) return 0;
+    return hit;
+}
+
+EXPORT void vox_cuda_forget_tree(const struct vox_node *root)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (size_t i = 0; i < g_trees.size(); i++) {
+        if (g_trees[i].root == root) {
+            vox_cuda_tree_free(g_trees[i].tree);
+            g_trees.erase(g_trees.begin() + (long)i);
+            return;
+        }
+    }
+}

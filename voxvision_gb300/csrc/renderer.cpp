@@ -1,0 +1,172 @@
+/*
+ * renderer.cpp -- the vox_render context API (src/voxrnd/renderer.h) over the
+ * GPU render path of voxtrees_cuda.cu.
+ *
+ * vox_render (renderer.c:200-319) draws a whole frame: the scene tree is
+ * uploaded once per vox_context_set_scene, the camera state is read from the
+ * built-in camera object, and one fused kernel produces the ARGB frame in
+ * device memory.  vox_redraw (renderer.c:321-327) then brings the frame to
+ * the host buffer returned by vox_context_pixels.  Instead of an SDL
+ * surface the context owns a headless frame.
+ */
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "../../include/voxrnd.h"
+#include "../../include/voxtrees_cuda.h"
+
+#define EXPORT extern "C" __attribute__((visibility("default")))
+
+extern "C" int vox_camera_gpu_state(const struct vox_camera *cam, float *position, float *rotation,
+                                    float *mul, float *xsub, float *ysub, float *sinphi, float *cosphi,
+                                    float *k);
+extern "C" int vox_cuda_render_quality_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
+                                              uint32_t w, uint32_t h, unsigned int quality,
+                                              const uint8_t *texture, uint32_t *argb, void *stream);
+
+struct vox_rnd_ctx {
+    unsigned int w = 0, h = 0;
+    struct vox_node *scene = nullptr;
+    struct vox_camera *camera = nullptr;
+    unsigned int quality = VOX_QUALITY_ADAPTIVE;   // renderer.c:78
+    vox_cuda_tree *tree = nullptr;
+    bool tex_dirty = true;
+    uint8_t texture[32768];
+    uint8_t *d_tex = nullptr;
+    uint32_t *d_frame = nullptr;
+    uint32_t *h_stage = nullptr;                   // pinned copy of the frame
+    uint32_t *pixels = nullptr;                    // what vox_context_pixels returns
+    cudaStream_t stream = nullptr;
+    int status = VOX_CUDA_OK;
+};
+
+namespace {
+
+// splitmix64, seed 7: the default texture (the reference's vn3d noise is not
+// part of this library).
+void default_texture(uint8_t *tex)
+{
+    uint64_t s = 7;
+    for (int i = 0; i < 32768; i++) {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        tex[i] = (uint8_t)(z >> 56);
+    }
+}
+
+void release(vox_rnd_ctx *c)
+{
+    if (c->tree) vox_cuda_tree_free(c->tree);
+    if (c->d_tex) cudaFree(c->d_tex);
+    if (c->d_frame) cudaFree(c->d_frame);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    std::free(c->pixels);
+}
+
+}  // namespace
+
+EXPORT struct vox_rnd_ctx *vox_make_context_headless(unsigned int width, unsigned int height)
+{
+    if (width == 0 || height == 0 || (width & 0xF) || (height & 0x3)) return nullptr;  // renderer.c:97-100
+    vox_rnd_ctx *c = new (std::nothrow) vox_rnd_ctx();
+    if (!c) return nullptr;
+    c->w = width;
+    c->h = height;
+    default_texture(c->texture);
+    size_t bytes = (size_t)width * height * 4;
+    c->pixels = static_cast<uint32_t *>(std::calloc((size_t)width * height, 4));
+    if (!c->pixels || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c->d_tex, 32768) != cudaSuccess || cudaMalloc(&c->d_frame, bytes) != cudaSuccess ||
+        cudaMallocHost(&c->h_stage, bytes) != cudaSuccess) {
+        release(c);
+        delete c;
+        return nullptr;
+    }
+    return c;
+}
+
+EXPORT void vox_destroy_context(struct vox_rnd_ctx *ctx)
+{
+    if (!ctx) return;
+    release(ctx);
+    delete ctx;
+}
+
+EXPORT void vox_context_set_scene(struct vox_rnd_ctx *ctx, struct vox_node *scene)
+{
+    ctx->scene = scene;
+    if (ctx->tree) {
+        vox_cuda_tree_free(ctx->tree);
+        ctx->tree = nullptr;
+    }
+}
+
+EXPORT void vox_context_set_camera(struct vox_rnd_ctx *ctx, struct vox_camera *camera)
+{
+    ctx->camera = camera;
+    camera->iface->set_window_size(camera, (int)ctx->w, (int)ctx->h);   // renderer.c:163-167
+}
+
+/* renderer.c:179-195 */
+EXPORT int vox_context_set_quality(struct vox_rnd_ctx *ctx, unsigned int quality)
+{
+    if ((quality & VOX_QUALITY_RM_MASK) && ((quality & VOX_QUALITY_MODE_MASK) != VOX_QUALITY_ADAPTIVE))
+        return 0;
+    if ((quality & VOX_QUALITY_MODE_MASK) > VOX_QUALITY_ADAPTIVE) return 0;
+    if ((quality & VOX_QUALITY_RM_MASK) > VOX_QUALITY_RAY_MERGE_ACCURATE) return 0;
+    ctx->quality = quality;
+    return 1;
+}
+
+EXPORT void vox_context_set_texture(struct vox_rnd_ctx *ctx, const uint8_t *texture)
+{
+    std::memcpy(ctx->texture, texture, 32768);
+    ctx->tex_dirty = true;
+}
+
+EXPORT void vox_render(struct vox_rnd_ctx *ctx)
+{
+    ctx->status = VOX_CUDA_EINVAL;
+    if (!ctx->camera) return;
+    vox_cuda_camera cam;
+    std::memset(&cam, 0, sizeof cam);
+    int kind = vox_camera_gpu_state(ctx->camera, cam.position, cam.rotation, &cam.mul, &cam.xsub, &cam.ysub,
+                                    &cam.sinphi, &cam.cosphi, &cam.k);
+    if (kind < 0) return;   // only the built-in camera classes run on the GPU
+    cam.kind = kind;
+    if (!ctx->tree) {
+        int rc = vox_cuda_tree_upload(ctx->scene, &ctx->tree);
+        if (rc) { ctx->status = rc; return; }
+    }
+    if (ctx->tex_dirty) {
+        if (cudaMemcpyAsync(ctx->d_tex, ctx->texture, 32768, cudaMemcpyHostToDevice, ctx->stream) !=
+            cudaSuccess) { ctx->status = VOX_CUDA_ECUDA; return; }
+        ctx->tex_dirty = false;
+    }
+    int rc = vox_cuda_render_quality_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
+                                            ctx->d_frame, ctx->stream);
+    if (rc) { ctx->status = rc; return; }
+    size_t bytes = (size_t)ctx->w * ctx->h * 4;
+    if (cudaMemcpyAsync(ctx->h_stage, ctx->d_frame, bytes, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        ctx->status = VOX_CUDA_ECUDA;
+        return;
+    }
+    ctx->status = VOX_CUDA_OK;
+}
+
+EXPORT void vox_redraw(struct vox_rnd_ctx *ctx)
+{
+    std::memcpy(ctx->pixels, ctx->h_stage, (size_t)ctx->w * ctx->h * 4);
+}
+
+EXPORT const uint32_t *vox_context_pixels(const struct vox_rnd_ctx *ctx) { return ctx->pixels; }
+
+EXPORT int vox_context_status(const struct vox_rnd_ctx *ctx) { return ctx->status; }

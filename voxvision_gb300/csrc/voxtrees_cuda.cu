@@ -1,0 +1,663 @@
+/*
+ * voxtrees_cuda.cu -- kernels and the C ABI of libvoxtrees_cuda
+ * (declared in include/voxtrees_cuda.h).
+ *
+ * Kernels (one thread per query, traversal in traverse.cuh):
+ *   ray_kernel     batched vox_ray_tree_intersection, optional per-ray roots
+ *   ball_kernel    batched vox_tree_ball_collidep
+ *   render_kernel  vox_render BEST: camera ray, search and colour fused; a
+ *                  warp covers an 8x4 pixel tile, a block 16x8 pixels, so the
+ *                  rays of a warp are neighbours and walk the same nodes.
+ * Each has a counting twin (COUNT=true) that only tallies the work.
+ *
+ * The stack capacity is a template parameter picked from the tree depth at
+ * upload time, so a kernel never needs more stack than it has.
+ */
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "flatten.h"
+#include "pool_layout.h"
+#include "traverse.cuh"
+#include "../../include/voxtrees_cuda.h"
+
+#define EXPORT extern "C" __attribute__((visibility("default")))
+
+using vox::Counts;
+using vox::DevTree;
+using vox::RayHit;
+
+struct vox_cuda_tree {
+    int device;
+    uint4 *d_pool;
+    uint32_t *d_rec_of_id;
+    uint32_t *d_status;      // bit 0: a traversal stack overflowed
+    DevTree dev;
+    int cap_class;           // 0: 24 entries, 1: 64, 2: 256
+    FlatTree flat;           // host copy: pre-order table and maps
+    size_t pool_bytes;
+};
+
+namespace {
+
+std::atomic<uint64_t> g_launches{0};
+
+constexpr int CAP0 = 24, CAP1 = 64, CAP2 = 256;
+
+int cap_class_for_depth(uint64_t depth)
+{
+    uint64_t need = 2 * depth + 2;
+    if (need <= (uint64_t)CAP0) return 0;
+    if (need <= (uint64_t)CAP1) return 1;
+    if (need <= (uint64_t)CAP2) return 2;
+    return -1;
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+__device__ __forceinline__ void add_counts(unsigned long long *counts, const Counts &c)
+{
+    unsigned long long n = c.nodes, i = c.inner, v = c.voxels;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n += __shfl_down_sync(0xffffffffu, n, o);
+        i += __shfl_down_sync(0xffffffffu, i, o);
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counts + 0, n);
+        atomicAdd(counts + 1, i);
+        atomicAdd(counts + 2, v);
+    }
+}
+
+template <int CAP, bool COUNT>
+__global__ void __launch_bounds__(256) ray_kernel(DevTree t, const float *__restrict__ o,
+                                                  const float *__restrict__ d,
+                                                  const uint32_t *__restrict__ roots, size_t n,
+                                                  uint32_t *__restrict__ leaf, uint8_t *__restrict__ slot,
+                                                  float *__restrict__ pts,
+                                                  unsigned long long *__restrict__ counts,
+                                                  uint32_t *__restrict__ status)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    Counts c{0, 0, 0};
+    bool overflow = false;
+    if (i < n) {
+        uint32_t start = t.root;
+        if (roots) {
+            uint32_t id = roots[i];
+            start = (id < t.n_nodes) ? t.rec_of_id[id] : (id == VOX_CUDA_MISS ? t.root : VOXP_EMPTY);
+        }
+        RayHit h;
+        bool hit = false;
+        if (start != VOXP_EMPTY)
+            hit = vox::trace_ray<CAP, COUNT>(t, start, o[3 * i], o[3 * i + 1], o[3 * i + 2],
+                                             d[3 * i], d[3 * i + 1], d[3 * i + 2], h, c, overflow);
+        if (!COUNT) {
+            leaf[i] = hit ? h.leaf : VOX_CUDA_MISS;
+            if (slot) slot[i] = hit ? (uint8_t)h.slot : (uint8_t)0xFF;
+            if (hit && pts) {
+                pts[3 * i] = h.x; pts[3 * i + 1] = h.y; pts[3 * i + 2] = h.z;
+            }
+        }
+        if (overflow) atomicOr(status, 1u);
+    }
+    if (COUNT) add_counts(counts, c);
+}
+
+template <int CAP, bool COUNT>
+__global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__restrict__ ctr,
+                                                   const float *__restrict__ rad, size_t n,
+                                                   uint8_t *__restrict__ hit,
+                                                   unsigned long long *__restrict__ counts,
+                                                   uint32_t *__restrict__ status)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    Counts c{0, 0, 0};
+    bool overflow = false;
+    if (i < n) {
+        bool h = vox::trace_ball<4 * CAP, COUNT>(t, ctr[3 * i], ctr[3 * i + 1], ctr[3 * i + 2], rad[i],
+                                                 c, overflow);
+        if (!COUNT) hit[i] = h ? 1 : 0;
+        if (overflow) atomicOr(status, 1u);
+    }
+    if (COUNT) add_counts(counts, c);
+}
+
+constexpr int TILE_W = 16, TILE_H = 8;   // block tile; warps are 8x4
+
+template <int CAP, bool COUNT>
+__global__ void __launch_bounds__(128) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
+                                                     uint32_t h, const uint8_t *__restrict__ tex,
+                                                     uint32_t *__restrict__ argb,
+                                                     unsigned long long *__restrict__ counts,
+                                                     uint32_t *__restrict__ status)
+{
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t px = blockIdx.x * TILE_W + (warp & 1) * 8 + (lane & 7);
+    uint32_t py = blockIdx.y * TILE_H + (warp >> 1) * 4 + (lane >> 3);
+    Counts c{0, 0, 0};
+    bool overflow = false;
+    if (px < w && py < h) {
+        float dx, dy, dz;
+        vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
+        RayHit hh;
+        bool hit = false;
+        if (t.root != VOXP_EMPTY)
+            hit = vox::trace_ray<CAP, COUNT>(t, t.root, cam.position[0], cam.position[1],
+                                             cam.position[2], dx, dy, dz, hh, c, overflow);
+        if (!COUNT) argb[(size_t)py * w + px] = hit ? vox::texel_color(tex, t, hh.x, hh.y, hh.z) : 0u;
+        if (overflow) atomicOr(status, 1u);
+    }
+    if (COUNT) add_counts(counts, c);
+}
+
+// vox_render in FAST / ADAPTIVE quality (renderer.c:215-318): one thread per
+// 4x4 square, its 16 pixels in the reference's Z-order, reusing the previous
+// pixel's leaf as the search root (FAST) and choosing the mode per square
+// from the two corner rays (ADAPTIVE), with optional ray merging.  A warp
+// covers 8x4 squares (32x16 pixels).
+__device__ __forceinline__ float sqr3(float ax, float ay, float az, float bx, float by, float bz)
+{
+    float x = __fsub_rn(ax, bx), y = __fsub_rn(ay, by), z = __fsub_rn(az, bz);
+    return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+}
+
+template <int CAP>
+__global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
+                                                             uint32_t h, unsigned int quality,
+                                                             const uint8_t *__restrict__ tex,
+                                                             uint32_t *__restrict__ argb,
+                                                             uint32_t *__restrict__ status)
+{
+    const int order[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};   // renderer.c:23-25
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t sx = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);     // square coordinates
+    uint32_t sy = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    uint32_t ws = w >> 2, hs = h >> 2;
+    if (sx >= ws || sy >= hs) return;
+    int xstart = (int)sx * 4, ystart = (int)sy * 4;
+    const float ox = cam.position[0], oy = cam.position[1], oz = cam.position[2];
+    const int rnd_mode = quality & VOX_CUDA_QUALITY_MODE_MASK;
+    const int merge_mode = quality & VOX_CUDA_QUALITY_RM_MASK;
+    uint32_t out[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) out[i] = 0u;
+    Counts c{0, 0, 0};
+    bool overflow = false;
+    bool have_leaf = false;
+    uint32_t leaf_rec = 0;
+    float ix = 0.f, iy = 0.f, iz = 0.f;       // inter1
+    int block_mode = rnd_mode;
+    int istart = 0, iend = 16;
+    bool block_merge = false;
+    bool empty = t.root == VOXP_EMPTY;
+
+    if (block_mode == VOX_CUDA_QUALITY_ADAPTIVE) {
+        block_merge = (merge_mode == VOX_CUDA_QUALITY_RAY_MERGE);
+        istart = 1;
+        float d1x, d1y, d1z;
+        vox::screen2world(cam, xstart, ystart, d1x, d1y, d1z);
+        RayHit h1;
+        bool c1 = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d1x, d1y, d1z, h1, c, overflow);
+        block_mode = VOX_CUDA_QUALITY_FAST;
+        have_leaf = c1;
+        if (c1) {
+            leaf_rec = h1.rec;
+            ix = h1.x; iy = h1.y; iz = h1.z;
+            iend = 15;
+            out[0] = vox::texel_color(tex, t, h1.x, h1.y, h1.z);
+            float d2x, d2y, d2z;
+            vox::screen2world(cam, xstart + 3, ystart + 3, d2x, d2y, d2z);
+            RayHit h2;
+            bool c2 = vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d2x, d2y, d2z, h2, c, overflow);
+            if (c2) {
+                out[15] = vox::texel_color(tex, t, h2.x, h2.y, h2.z);
+                float d1 = sqr3(h1.x, h1.y, h1.z, ox, oy, oz);
+                float d2 = sqr3(d1x, d1y, d1z, 0.f, 0.f, 0.f);
+                float criteria = __fmul_rn(__fdiv_rn(d1, d2), sqr3(d1x, d1y, d1z, d2x, d2y, d2z));
+                float dist = sqr3(h1.x, h1.y, h1.z, h2.x, h2.y, h2.z);
+                if ((double)__fdiv_rn(dist, criteria) > 1.69)          // LENGTH_THRESHOLD, renderer.c:197
+                    block_mode = VOX_CUDA_QUALITY_BEST;
+                if (d1 > 22500.0f)                                       // MAX_DIST^2, renderer.c:198
+                    block_merge = (block_mode == VOX_CUDA_QUALITY_FAST &&
+                                   merge_mode == VOX_CUDA_QUALITY_RAY_MERGE_ACCURATE) ? true : block_merge;
+                else
+                    block_merge = false;
+            }
+        }
+    }
+
+    int prev_p = 0;
+    for (int i = istart; i < iend; i++) {
+        int p = order[i];
+        int py = p >> 2, px = p & 3;
+        bool merge = block_merge && (i & 1);
+        float dx, dy, dz;
+        vox::screen2world(cam, px + xstart, py + ystart, dx, dy, dz);
+        if (!merge) {
+            RayHit hh;
+            if (block_mode == VOX_CUDA_QUALITY_FAST) {
+                if (have_leaf)
+                    have_leaf = vox::trace_ray<CAP, false>(t, leaf_rec, ox, oy, oz, dx, dy, dz, hh, c, overflow);
+                if (!have_leaf)
+                    have_leaf = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, dx, dy, dz, hh, c,
+                                                                     overflow);
+            } else {
+                have_leaf = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, dx, dy, dz, hh, c,
+                                                                 overflow);
+            }
+            if (have_leaf) {
+                leaf_rec = hh.rec;
+                ix = hh.x; iy = hh.y; iz = hh.z;
+            }
+        }
+        if (have_leaf) out[p] = merge ? out[prev_p] : vox::texel_color(tex, t, ix, iy, iz);
+        prev_p = p;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        argb[(size_t)(ystart + (i >> 2)) * w + xstart + (i & 3)] = out[i];
+    if (overflow) atomicOr(status, 1u);
+}
+
+// ---------------------------------------------------------------- launchers
+
+template <bool COUNT>
+cudaError_t launch_rays(const vox_cuda_tree *t, const float *o, const float *d, const uint32_t *roots,
+                        size_t n, uint32_t *leaf, uint8_t *slot, float *pts,
+                        unsigned long long *counts, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    dim3 block(256), grid((unsigned)((n + 255) / 256));
+    switch (t->cap_class) {
+    case 0: ray_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
+    case 1: ray_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
+    default: ray_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
+    }
+    g_launches++;
+    return cudaGetLastError();
+}
+
+template <bool COUNT>
+cudaError_t launch_balls(const vox_cuda_tree *t, const float *c, const float *r, size_t n, uint8_t *hit,
+                         unsigned long long *counts, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    dim3 block(256), grid((unsigned)((n + 255) / 256));
+    switch (t->cap_class) {
+    case 0: ball_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
+    case 1: ball_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
+    default: ball_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
+    }
+    g_launches++;
+    return cudaGetLastError();
+}
+
+template <bool COUNT>
+cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
+                          const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s)
+{
+    dim3 block(128), grid((w + TILE_W - 1) / TILE_W, (h + TILE_H - 1) / TILE_H);
+    switch (t->cap_class) {
+    case 0: render_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, tex, argb, counts, t->d_status); break;
+    case 1: render_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, tex, argb, counts, t->d_status); break;
+    default: render_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, tex, argb, counts, t->d_status); break;
+    }
+    g_launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
+                                  unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s)
+{
+    uint32_t ws = w / 4, hs = h / 4;
+    dim3 block(128), grid((ws + 15) / 16, (hs + 7) / 8);
+    switch (t->cap_class) {
+    case 0: render_squares_kernel<CAP0><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
+    case 1: render_squares_kernel<CAP1><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
+    default: render_squares_kernel<CAP2><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
+    }
+    g_launches++;
+    return cudaGetLastError();
+}
+
+int status_of(cudaError_t e) { return e == cudaSuccess ? VOX_CUDA_OK : VOX_CUDA_ECUDA; }
+
+// Reads and clears the tree's overflow flag after a synchronous call.
+int check_tree_status(const vox_cuda_tree *t, cudaStream_t s)
+{
+    uint32_t st = 0;
+    if (cudaMemcpyAsync(&st, t->d_status, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return VOX_CUDA_ECUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return VOX_CUDA_ECUDA;
+    if (st) {
+        cudaMemsetAsync(t->d_status, 0, 4, s);
+        cudaStreamSynchronize(s);
+        return VOX_CUDA_ESTACK;
+    }
+    return VOX_CUDA_OK;
+}
+
+// Stream-ordered scratch for the host-buffer entry points.
+struct Scratch {
+    cudaStream_t s;
+    void *p = nullptr;
+    explicit Scratch(cudaStream_t st) : s(st) {}
+    cudaError_t get(size_t bytes) { return cudaMallocAsync(&p, bytes ? bytes : 16, s); }
+    ~Scratch() { if (p) cudaFreeAsync(p, s); }
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+// ======================================================================== API
+
+EXPORT const char *vox_cuda_strerror(int code)
+{
+    switch (code) {
+    case VOX_CUDA_OK: return "ok";
+    case VOX_CUDA_EINVAL: return "invalid argument";
+    case VOX_CUDA_ENOMEM: return "out of memory";
+    case VOX_CUDA_ECUDA: return "CUDA runtime error";
+    case VOX_CUDA_EDEPTH: return "tree deeper than the traversal stack supports";
+    case VOX_CUDA_ESTACK: return "traversal stack overflow";
+    case VOX_CUDA_ETOOBIG: return "flattened tree exceeds the pool limit";
+    case VOX_CUDA_EGEOMETRY: return "frame width must be a multiple of 16 and height of 4";
+    case VOX_CUDA_EBUDGET: return "admission budget exceeded";
+    case VOX_CUDA_ETIMEOUT: return "bounded wait timed out";
+    case VOX_CUDA_ENODEV: return "no CUDA device";
+    default: return "unknown error";
+    }
+}
+
+EXPORT const char *vox_cuda_version(void) { return "voxtrees_cuda 0.1 (sm_103a)"; }
+
+EXPORT uint64_t vox_cuda_launch_count(void) { return g_launches.load(); }
+
+EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out)
+{
+    if (!out) return VOX_CUDA_EINVAL;
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return VOX_CUDA_ENODEV;
+    vox_cuda_tree *t = new (std::nothrow) vox_cuda_tree();
+    if (!t) return VOX_CUDA_ENOMEM;
+    t->device = dev;
+    int rc = vox_flatten(root, vox_voxel, &t->flat);
+    if (rc == -2 || rc == -1) { delete t; return VOX_CUDA_ETOOBIG; }
+    if (vox_flatten_validate(t->flat) != 0) { delete t; return VOX_CUDA_EINVAL; }
+    int cls = cap_class_for_depth(t->flat.depth);
+    if (cls < 0) { delete t; return VOX_CUDA_EDEPTH; }
+    t->cap_class = cls;
+    size_t units = t->flat.units.size() ? t->flat.units.size() : 2;
+    size_t nodes = t->flat.preorder.size();
+    t->pool_bytes = units * 16;
+    if (cudaMalloc(&t->d_pool, t->pool_bytes) != cudaSuccess) { delete t; return VOX_CUDA_ENOMEM; }
+    if (cudaMalloc(&t->d_rec_of_id, (nodes ? nodes : 1) * 4) != cudaSuccess ||
+        cudaMalloc(&t->d_status, 4) != cudaSuccess) {
+        cudaFree(t->d_pool); cudaFree(t->d_rec_of_id);
+        delete t;
+        return VOX_CUDA_ENOMEM;
+    }
+    cudaError_t e = cudaMemset(t->d_status, 0, 4);
+    if (e == cudaSuccess && t->flat.units.size())
+        e = cudaMemcpy(t->d_pool, t->flat.units.data(), t->pool_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nodes)
+        e = cudaMemcpy(t->d_rec_of_id, t->flat.rec_of_id.data(), nodes * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(t->d_pool); cudaFree(t->d_rec_of_id); cudaFree(t->d_status);
+        delete t;
+        return VOX_CUDA_ECUDA;
+    }
+    t->dev.pool = t->d_pool;
+    t->dev.rec_of_id = t->d_rec_of_id;
+    t->dev.root = root ? 0u : VOXP_EMPTY;
+    t->dev.n_nodes = (uint32_t)nodes;
+    t->dev.vx = t->flat.voxel[0];
+    t->dev.vy = t->flat.voxel[1];
+    t->dev.vz = t->flat.voxel[2];
+    // The flattened image is on the device now; keep only the maps.
+    std::vector<uint4_host>().swap(t->flat.units);
+    *out = t;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info *info)
+{
+    if (!info) return VOX_CUDA_EINVAL;
+    FlatTree f;
+    int rc = vox_flatten(root, vox_voxel, &f);
+    if (rc) return VOX_CUDA_ETOOBIG;
+    if (vox_flatten_validate(f) != 0) return VOX_CUDA_EINVAL;
+    if (cap_class_for_depth(f.depth) < 0) return VOX_CUDA_EDEPTH;
+    info->nodes = f.preorder.size();
+    info->inner = f.n_inner;
+    info->leaves = f.n_leaf;
+    info->dense_leaves = f.n_dense;
+    info->dots = f.n_dots;
+    info->depth = f.depth;
+    info->device_bytes = (f.units.size() ? f.units.size() : 2) * 16 + 4 * f.preorder.size() + 4;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_tree_free(vox_cuda_tree *t)
+{
+    if (!t) return VOX_CUDA_EINVAL;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != t->device) cudaSetDevice(t->device);
+    cudaFree(t->d_pool);
+    cudaFree(t->d_rec_of_id);
+    cudaFree(t->d_status);
+    if (cur != t->device) cudaSetDevice(cur);
+    delete t;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_tree_get_info(const vox_cuda_tree *t, vox_cuda_tree_info *info)
+{
+    if (!t || !info) return VOX_CUDA_EINVAL;
+    info->nodes = t->flat.preorder.size();
+    info->inner = t->flat.n_inner;
+    info->leaves = t->flat.n_leaf;
+    info->dense_leaves = t->flat.n_dense;
+    info->dots = t->flat.n_dots;
+    info->depth = t->flat.depth;
+    info->device_bytes = t->pool_bytes + 4 * t->flat.preorder.size() + 4;
+    return VOX_CUDA_OK;
+}
+
+EXPORT const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *t, uint32_t id)
+{
+    if (!t || id >= t->flat.preorder.size()) return nullptr;
+    return t->flat.preorder[id];
+}
+
+EXPORT int vox_cuda_tree_node_id(const vox_cuda_tree *t, const struct vox_node *node, uint32_t *id)
+{
+    if (!t || !id) return VOX_CUDA_EINVAL;
+    auto it = t->flat.index.find(node);
+    if (it == t->flat.index.end()) return VOX_CUDA_EINVAL;
+    *id = it->second;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_ray_batch_device(const vox_cuda_tree *t, const float *o, const float *d,
+                                     const uint32_t *roots, size_t n, uint32_t *leaf, uint8_t *slot,
+                                     float *pts, void *stream)
+{
+    if (!t || (n && (!o || !d || !leaf))) return VOX_CUDA_EINVAL;
+    return status_of(launch_rays<false>(t, o, d, roots, n, leaf, slot, pts, nullptr, as_stream(stream)));
+}
+
+EXPORT int vox_cuda_ray_batch(const vox_cuda_tree *t, const float *o, const float *d,
+                              const uint32_t *roots, size_t n, uint32_t *leaf, uint8_t *slot,
+                              float *pts, void *stream)
+{
+    if (!t || (n && (!o || !d || !leaf))) return VOX_CUDA_EINVAL;
+    if (n == 0) return VOX_CUDA_OK;
+    cudaStream_t s = as_stream(stream);
+    size_t b_in = align256(n * 12), b_root = roots ? align256(n * 4) : 0;
+    size_t b_leaf = align256(n * 4), b_slot = align256(n), b_pts = align256(n * 12);
+    Scratch sc(s);
+    if (sc.get(2 * b_in + b_root + b_leaf + b_slot + b_pts) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    char *base = static_cast<char *>(sc.p);
+    float *d_o = reinterpret_cast<float *>(base);
+    float *d_d = reinterpret_cast<float *>(base + b_in);
+    uint32_t *d_roots = roots ? reinterpret_cast<uint32_t *>(base + 2 * b_in) : nullptr;
+    uint32_t *d_leaf = reinterpret_cast<uint32_t *>(base + 2 * b_in + b_root);
+    uint8_t *d_slot = reinterpret_cast<uint8_t *>(base + 2 * b_in + b_root + b_leaf);
+    float *d_pts = reinterpret_cast<float *>(base + 2 * b_in + b_root + b_leaf + b_slot);
+    cudaError_t e = cudaMemcpyAsync(d_o, o, n * 12, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_d, d, n * 12, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && roots) e = cudaMemcpyAsync(d_roots, roots, n * 4, cudaMemcpyHostToDevice, s);
+    // points are written on hits only: start from the caller's values
+    if (e == cudaSuccess && pts) e = cudaMemcpyAsync(d_pts, pts, n * 12, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = launch_rays<false>(t, d_o, d_d, d_roots, n, d_leaf, d_slot, pts ? d_pts : nullptr, nullptr, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(leaf, d_leaf, n * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && slot) e = cudaMemcpyAsync(slot, d_slot, n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && pts) e = cudaMemcpyAsync(pts, d_pts, n * 12, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return VOX_CUDA_ECUDA;
+    return check_tree_status(t, s);
+}
+
+EXPORT int vox_cuda_ball_batch_device(const vox_cuda_tree *t, const float *c, const float *r, size_t n,
+                                      uint8_t *hit, void *stream)
+{
+    if (!t || (n && (!c || !r || !hit))) return VOX_CUDA_EINVAL;
+    return status_of(launch_balls<false>(t, c, r, n, hit, nullptr, as_stream(stream)));
+}
+
+EXPORT int vox_cuda_ball_batch(const vox_cuda_tree *t, const float *c, const float *r, size_t n,
+                               uint8_t *hit, void *stream)
+{
+    if (!t || (n && (!c || !r || !hit))) return VOX_CUDA_EINVAL;
+    if (n == 0) return VOX_CUDA_OK;
+    cudaStream_t s = as_stream(stream);
+    size_t b_c = align256(n * 12), b_r = align256(n * 4), b_h = align256(n);
+    Scratch sc(s);
+    if (sc.get(b_c + b_r + b_h) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    char *base = static_cast<char *>(sc.p);
+    float *d_c = reinterpret_cast<float *>(base);
+    float *d_r = reinterpret_cast<float *>(base + b_c);
+    uint8_t *d_h = reinterpret_cast<uint8_t *>(base + b_c + b_r);
+    cudaError_t e = cudaMemcpyAsync(d_c, c, n * 12, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_r, r, n * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_balls<false>(t, d_c, d_r, n, d_h, nullptr, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hit, d_h, n, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return VOX_CUDA_ECUDA;
+    return check_tree_status(t, s);
+}
+
+static int check_render_args(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                             const uint8_t *tex, const uint32_t *argb)
+{
+    if (!t || !cam || !tex || !argb) return VOX_CUDA_EINVAL;
+    if (cam->kind != VOX_CUDA_CAMERA_SIMPLE && cam->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+    if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_render_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                                  const uint8_t *tex, uint32_t *argb, void *stream)
+{
+    int rc = check_render_args(t, cam, w, h, tex, argb);
+    if (rc) return rc;
+    return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream)));
+}
+
+EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                           const uint8_t *tex, uint32_t *argb, void *stream)
+{
+    int rc = check_render_args(t, cam, w, h, tex, argb);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    size_t npx = (size_t)w * h;
+    size_t b_tex = align256(32768);
+    Scratch sc(s);
+    if (sc.get(b_tex + npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    uint8_t *d_tex = static_cast<uint8_t *>(sc.p);
+    uint32_t *d_argb = reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
+    cudaError_t e = cudaMemcpyAsync(d_tex, tex, 32768, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, d_tex, d_argb, nullptr, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return VOX_CUDA_ECUDA;
+    return check_tree_status(t, s);
+}
+
+EXPORT int vox_cuda_render_counts_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
+                                         uint32_t h, uint64_t *counts, void *stream)
+{
+    if (!t || !cam || !counts) return VOX_CUDA_EINVAL;
+    if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
+    return status_of(launch_render<true>(t, *cam, w, h, nullptr, nullptr,
+                                         reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
+}
+
+EXPORT int vox_cuda_ray_counts_device(const vox_cuda_tree *t, const float *o, const float *d, size_t n,
+                                      uint64_t *counts, void *stream)
+{
+    if (!t || !counts || (n && (!o || !d))) return VOX_CUDA_EINVAL;
+    return status_of(launch_rays<true>(t, o, d, nullptr, n, nullptr, nullptr, nullptr,
+                                       reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
+}
+
+EXPORT int vox_cuda_ball_counts_device(const vox_cuda_tree *t, const float *c, const float *r, size_t n,
+                                       uint64_t *counts, void *stream)
+{
+    if (!t || !counts || (n && (!c || !r))) return VOX_CUDA_EINVAL;
+    return status_of(launch_balls<true>(t, c, r, n, nullptr,
+                                        reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
+}
+
+static bool valid_quality(unsigned int q)
+{
+    if ((q & VOX_CUDA_QUALITY_RM_MASK) && ((q & VOX_CUDA_QUALITY_MODE_MASK) != VOX_CUDA_QUALITY_ADAPTIVE))
+        return false;
+    if ((q & VOX_CUDA_QUALITY_MODE_MASK) > VOX_CUDA_QUALITY_ADAPTIVE) return false;
+    if ((q & VOX_CUDA_QUALITY_RM_MASK) > VOX_CUDA_QUALITY_RAY_MERGE_ACCURATE) return false;
+    return true;
+}
+
+EXPORT int vox_cuda_render_quality_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
+                                          uint32_t h, unsigned int quality, const uint8_t *tex, uint32_t *argb,
+                                          void *stream)
+{
+    int rc = check_render_args(t, cam, w, h, tex, argb);
+    if (rc) return rc;
+    if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
+    if ((quality & VOX_CUDA_QUALITY_MODE_MASK) == VOX_CUDA_QUALITY_BEST)
+        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream)));
+    return status_of(launch_render_squares(t, *cam, w, h, quality, tex, argb, as_stream(stream)));
+}
+
+EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, void *stream)
+{
+    int rc = check_render_args(t, cam, w, h, tex, argb);
+    if (rc) return rc;
+    if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
+    cudaStream_t s = as_stream(stream);
+    size_t npx = (size_t)w * h;
+    size_t b_tex = align256(32768);
+    Scratch sc(s);
+    if (sc.get(b_tex + npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    uint8_t *d_tex = static_cast<uint8_t *>(sc.p);
+    uint32_t *d_argb = reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
+    cudaError_t e = cudaMemcpyAsync(d_tex, tex, 32768, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        rc = vox_cuda_render_quality_device(t, cam, w, h, quality, d_tex, d_argb, stream);
+        if (rc) return rc;
+        e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+    }
+    if (e != cudaSuccess) return VOX_CUDA_ECUDA;
+    return check_tree_status(t, s);
+}
