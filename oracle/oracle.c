@@ -482,6 +482,34 @@ int orc_ray_batch(const struct orc_node *tree, const struct orc_node *root,
 
 typedef struct {
     const struct orc_node *root;
+    const float *o, *d;
+    uint32_t *per_ray;   /* 3 counters per ray */
+} rcount_ctx;
+
+static void rcount_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
+{
+    rcount_ctx *x = vctx;
+    for (size_t i = lo; i < hi; i++) {
+        orc_counts k = {0, 0, 0};
+        float res[3];
+        orc_ray(x->root, x->o + 3 * i, x->d + 3 * i, res, NULL, &k);
+        x->per_ray[3 * i] = (uint32_t)k.nodes;
+        x->per_ray[3 * i + 1] = (uint32_t)k.inner;
+        x->per_ray[3 * i + 2] = (uint32_t)k.voxels;
+        c->nodes += k.nodes; c->inner += k.inner; c->voxels += k.voxels;
+    }
+}
+
+int orc_ray_counts_per_ray(const struct orc_node *root, size_t n, const float *origins,
+                           const float *dirs, uint32_t *per_ray, int nthreads)
+{
+    rcount_ctx x = {root, origins, dirs, per_ray};
+    run_pool(n, 4096, nthreads, rcount_work, &x, NULL);
+    return 0;
+}
+
+typedef struct {
+    const struct orc_node *root;
     const float *c, *r;
     uint8_t *hit;
 } ball_ctx;

@@ -92,6 +92,10 @@ int orc_ball_batch(const struct orc_node *tree, size_t n, const float *centers,
                    const float *radii, uint8_t *hit, uint64_t *counts3,
                    int nthreads);
 
+/* Per-ray work counters (nodes, inner, voxels), for cost distributions. */
+int orc_ray_counts_per_ray(const struct orc_node *root, size_t n, const float *origins,
+                           const float *dirs, uint32_t *per_ray, int nthreads);
+
 void orc_screen2world(const orc_camera *cam, int sx, int sy, float *ray);
 
 /* vox_render, quality BEST (renderer.c:200-319, branch :308) into a linear

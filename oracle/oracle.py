@@ -55,6 +55,7 @@ def lib():
         L.orc_render_quality.argtypes = [vp, C.POINTER(OrcCamera), C.c_int, C.c_int, C.c_uint, vp, vp,
                                          vp, C.c_int]
         L.orc_render_quality.restype = C.c_int
+        L.orc_ray_counts_per_ray.argtypes = [vp, sz, fp, fp, vp, C.c_int]
         L.orc_dump.argtypes = [vp] * 8; L.orc_dump.restype = sz
         L.orc_from_dump.argtypes = [sz] + [vp] * 7; L.orc_from_dump.restype = vp
         _lib = L
@@ -190,3 +191,11 @@ def render_quality(tree_ptr, state: dict, w: int, h: int, quality: int, texture:
     if rc != 0:
         raise ValueError("bad geometry: width must be a multiple of 16 and height of 4")
     return out.reshape(h, w), cnt
+
+
+def ray_counts_per_ray(root_ptr, origins, dirs, nthreads=None):
+    o = np.ascontiguousarray(origins, dtype=np.float32)
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    out = np.zeros((o.shape[0], 3), np.uint32)
+    lib().orc_ray_counts_per_ray(root_ptr, o.shape[0], _p(o), _p(d), _p(out), nthreads or nthreads_default())
+    return out

@@ -61,10 +61,10 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
     }
     out->rec_of_id.assign(out->preorder.size(), 0);
 
-    // Pass 2: depth-first placement.
+    // Pass 2: depth-first placement of 3-unit records.
     std::vector<uint4_host> &u = out->units;
-    u.reserve(out->preorder.size() * 3);
-    u.resize(2);
+    u.reserve(out->preorder.size() * 4);
+    u.resize(VOXP_REC_UNITS);
     std::vector<Placement> work{{root, 0, 0}};
     while (!work.empty()) {
         Placement p = work.back();
@@ -73,6 +73,7 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
         uint32_t id = out->index[n];
         out->rec_of_id[id] = p.rec;
         uint32_t meta, link;
+        uint4_host extra{0u, 0u, 0u, 0u};
         if (n->flags & VOX_DENSE_LEAF) {
             meta = VOXP_KIND_DENSE;
             link = id;
@@ -80,24 +81,21 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
         } else if (n->flags & VOX_LEAF) {
             uint32_t cnt = n->dots_num;
             if (cnt >= (1u << 30)) return -1;
-            size_t hdr = u.size();
-            u.push_back({id, cnt, 0u, 0u});
+            link = (uint32_t)u.size();
             for (uint32_t i = 0; i < cnt; i++)
                 u.push_back({fbits(n->data.dots[i][0]), fbits(n->data.dots[i][1]),
                              fbits(n->data.dots[i][2]), 0u});
             meta = VOXP_KIND_LEAF | (cnt << 2);
-            link = (uint32_t)(hdr + 1);
+            extra = {id, cnt, 0u, 0u};
             out->n_leaf++;
             out->n_dots += cnt;
         } else {
             uint32_t mask = 0;
             for (int o = 0; o < 8; o++)
                 if (n->data.inner.children[o]) mask |= 1u << o;
-            size_t blk = u.size();
-            const float *c = n->data.inner.center;
-            u.push_back({fbits(c[0]), fbits(c[1]), fbits(c[2]), 0u});
+            link = (uint32_t)u.size();
             uint32_t nchild = (uint32_t)__builtin_popcount(mask);
-            u.resize(u.size() + 2 * nchild);
+            u.resize(u.size() + VOXP_REC_UNITS * nchild);
             uint32_t d = p.depth + 1;
             if (d > out->depth) out->depth = d;
             // Children are placed after this block; push in reverse so octant 0's
@@ -106,16 +104,18 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
                 const vox_node *ch = n->data.inner.children[o];
                 if (!ch) continue;
                 uint32_t rank = (uint32_t)__builtin_popcount(mask & ((1u << o) - 1u));
-                work.push_back({ch, (uint32_t)(blk + 1 + 2 * rank), d});
+                work.push_back({ch, link + VOXP_REC_UNITS * rank, d});
             }
             meta = VOXP_KIND_INNER | (mask << 8);
-            link = (uint32_t)blk;
+            const float *c = n->data.inner.center;
+            extra = {fbits(c[0]), fbits(c[1]), fbits(c[2]), 0u};
             out->n_inner++;
         }
         if (u.size() >= VOXP_MAX_UNITS) return -2;
         const vox_box &b = n->bounding_box;
         u[p.rec] = {fbits(b.min[0]), fbits(b.min[1]), fbits(b.min[2]), fbits(b.max[0])};
         u[p.rec + 1] = {fbits(b.max[1]), fbits(b.max[2]), meta, link};
+        u[p.rec + 2] = extra;
     }
     return 0;
 }
@@ -125,13 +125,13 @@ int vox_flatten_validate(const FlatTree &f)
     const std::vector<uint4_host> &u = f.units;
     size_t n = u.size();
     if (f.preorder.empty()) return 0;
-    if (n < 2) return -1;
+    if (n < VOXP_REC_UNITS) return -1;
     std::vector<uint32_t> work{0};
     size_t seen = 0;
     while (!work.empty()) {
         uint32_t rec = work.back();
         work.pop_back();
-        if ((size_t)rec + 2 > n) return -1;
+        if ((size_t)rec + VOXP_REC_UNITS > n) return -1;
         seen++;
         uint32_t meta = u[rec + 1].z, link = u[rec + 1].w;
         uint32_t kind = meta & 3u;
@@ -139,13 +139,13 @@ int vox_flatten_validate(const FlatTree &f)
             if (link >= f.preorder.size()) return -1;
         } else if (kind == VOXP_KIND_LEAF) {
             uint64_t cnt = meta >> 2;
-            if (link < 1 || (uint64_t)link + cnt > n) return -1;
-            if (u[link - 1].x >= f.preorder.size() || u[link - 1].y != cnt) return -1;
+            if ((uint64_t)link + cnt > n) return -1;
+            if (u[rec + 2].x >= f.preorder.size() || u[rec + 2].y != cnt) return -1;
         } else if (kind == VOXP_KIND_INNER) {
             uint32_t mask = (meta >> 8) & 0xFFu;
             uint32_t k = (uint32_t)__builtin_popcount(mask);
-            if ((uint64_t)link + 1 + 2ull * k > n) return -1;
-            for (uint32_t i = 0; i < k; i++) work.push_back(link + 1 + 2 * i);
+            if ((uint64_t)link + (uint64_t)VOXP_REC_UNITS * k > n) return -1;
+            for (uint32_t i = 0; i < k; i++) work.push_back(link + VOXP_REC_UNITS * i);
         } else {
             return -1;
         }

@@ -8,15 +8,8 @@
  * contracts into FMAs.  Comparisons keep the reference's NaN behaviour.  The
  * result is the reference's leaf, voxel and intersection point, bit for bit.
  *
- * Recursion becomes an explicit per-thread stack of tasks {record offset,
- * ray origin}.  vox_ray_tree_intersection (search.c:8-153) explores, for an
- * inner node, the child holding the entry point first and then -- only if
- * that found nothing -- the children behind each dividing plane the ray
- * crosses, nearest plane first.  The second half is deferred as a
- * "continuation" task {record offset | CONT | first octant << 28, entry
- * point}; popping it computes the plane crossings and pushes the children in
- * visiting order.  The first hit ends the search, exactly as the recursion
- * returns on its first non-NULL result.
+ * Recursion becomes an explicit per-thread stack of pending tasks {record
+ * offset, ray origin} (see trace_ray).
  */
 #ifndef VOX_TRAVERSE_CUH
 #define VOX_TRAVERSE_CUH
@@ -28,8 +21,6 @@
 #include "../../include/voxtrees_cuda.h"
 
 namespace vox {
-
-constexpr uint32_t CONT_BIT = 0x80000000u;
 
 struct DevTree {
     const uint4 *pool;
@@ -120,10 +111,24 @@ struct RayHit {
     uint32_t rec;     // record offset of the leaf
 };
 
-/* vox_ray_tree_intersection (search.c:8-153) from the node whose record is at
- * `start`.  Returns true on a hit.  `overflow` is set (and the search ends
- * as a miss) if the stack would exceed CAP entries, which the upload-time
- * depth check rules out. */
+/* vox_ray_tree_intersection (search.c:8-153) from the node whose record is
+ * at `start`.
+ *
+ * Every loop iteration makes one 16..48-byte load (a node record, or one
+ * voxel of the leaf being scanned) and one box test, so the lanes of a warp
+ * stay in step whatever mix of nodes and voxels they are on.  The box test
+ * of a node is search.c:22-23; of a voxel, the leaf loop's test at :55.
+ * When an inner node's box is entered, its plane crossings (:105-148) are
+ * computed at once: the children behind the crossings are pushed in visiting
+ * order and the search continues in the entry octant (:86-97).  Computing
+ * the crossings before the entry octant has been searched changes nothing:
+ * they depend only on the node and the ray, and they are used only if that
+ * octant finds nothing.  The first hit ends the search, as the first
+ * non-NULL return ends the recursion.
+ *
+ * Returns true on a hit.  `overflow` is set (and the search ends as a miss)
+ * if the stack would exceed CAP entries, which the upload-time depth check
+ * rules out (3 entries per inner level suffice). */
 template <int CAP, bool COUNT>
 __device__ __forceinline__ bool trace_ray(const DevTree &t, uint32_t start,
                                           float ox0, float oy0, float oz0,
@@ -132,150 +137,142 @@ __device__ __forceinline__ bool trace_ray(const DevTree &t, uint32_t start,
 {
     uint4 stack[CAP];
     int sp = 0;
-    uint32_t cur = start;
-    float ox = ox0, oy = oy0, oz = oz0;
     const uint4 *pool = t.pool;
+    uint32_t cur = start;                 // node mode: record offset; voxel mode: first voxel
+    float ox = ox0, oy = oy0, oz = oz0;   // origin of the next box test
+    bool scan = false;                    // scanning the voxels of a leaf
+    uint32_t vi = 0, vn = 0, vrec = 0, vid = 0;
+    float best = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
+    int win = -1;
 
     for (;;) {
-        if (!(cur & CONT_BIT)) {
-            // ---- visit a node: search.c:22-97
-            uint4 a = ld16(pool + cur);
-            uint4 b = ld16(pool + cur + 1);
+        uint4 u0 = ld16(pool + (scan ? cur + vi : cur));
+        uint4 u1 = make_uint4(0u, 0u, 0u, 0u), u2 = make_uint4(0u, 0u, 0u, 0u);
+        if (!scan) {
+            u1 = ld16(pool + cur + 1);
+            u2 = ld16(pool + cur + 2);
+        }
+        float lx = ubf(u0.x), ly = ubf(u0.y), lz = ubf(u0.z), hx, hy, hz;
+        if (scan) {   // voxel box [dot, dot + vox_voxel] (search.c:53-54)
+            hx = __fadd_rn(lx, t.vx); hy = __fadd_rn(ly, t.vy); hz = __fadd_rn(lz, t.vz);
+            if (COUNT) cnt.voxels++;
+        } else {
+            hx = ubf(u0.w); hy = ubf(u1.x); hz = ubf(u1.y);
             if (COUNT) cnt.nodes++;
-            float lx = ubf(a.x), ly = ubf(a.y), lz = ubf(a.z);
-            float hx = ubf(a.w), hy = ubf(b.x), hz = ubf(b.y);
-            uint32_t meta = b.z, link = b.w;
-            float ex, ey, ez;
-            if (hit_box(lx, ly, lz, hx, hy, hz, ox, oy, oz, dx, dy, dz, ex, ey, ez)) {
-                uint32_t kind = meta & 3u;
-                if (kind == VOXP_KIND_DENSE) {              // :31-37
-                    hit.x = ex; hit.y = ey; hit.z = ez;
-                    hit.leaf = link; hit.slot = 0xFFu; hit.rec = cur;
+        }
+        float ex, ey, ez;
+        bool in = hit_box(lx, ly, lz, hx, hy, hz, ox, oy, oz, dx, dy, dz, ex, ey, ez);
+        bool resume = false;
+
+        if (scan) {
+            // leaf loop body, search.c:55-78: nearest voxel by L1 distance from
+            // the leaf's entry point, first one at distance 0 wins at once
+            bool stop = false;
+            if (in) {
+                float dist = l1(ox, oy, oz, ex, ey, ez);
+                if (dist == 0.0f) {
+                    bx = ex; by = ey; bz = ez; win = (int)vi; stop = true;
+                } else if (dist < best) {
+                    best = dist; bx = ex; by = ey; bz = ez; win = (int)vi;
+                }
+            }
+            vi++;
+            if (stop || vi == vn) {
+                if (win >= 0) {
+                    hit.x = bx; hit.y = by; hit.z = bz;
+                    hit.leaf = vid; hit.slot = (uint32_t)win; hit.rec = vrec;
                     return true;
                 }
-                if (kind == VOXP_KIND_LEAF) {               // :39-81
-                    uint32_t n = meta >> 2;
-                    float best = __int_as_float(0x7f800000);
-                    int win = -1;
-                    float bx = 0.f, by = 0.f, bz = 0.f;
-                    for (uint32_t i = 0; i < n; i++) {
-                        uint4 v = ld16(pool + link + i);
-                        if (COUNT) cnt.voxels++;
-                        float vx = ubf(v.x), vy = ubf(v.y), vz = ubf(v.z);
-                        float fx, fy, fz;
-                        if (hit_box(vx, vy, vz, __fadd_rn(vx, t.vx), __fadd_rn(vy, t.vy),
-                                    __fadd_rn(vz, t.vz), ex, ey, ez, dx, dy, dz, fx, fy, fz)) {
-                            float dist = l1(ex, ey, ez, fx, fy, fz);
-                            if (dist == 0.0f) {
-                                bx = fx; by = fy; bz = fz; win = (int)i;
-                                break;
-                            }
-                            if (dist < best) {
-                                best = dist;
-                                bx = fx; by = fy; bz = fz; win = (int)i;
-                            }
-                        }
-                    }
-                    if (win >= 0) {
-                        hit.x = bx; hit.y = by; hit.z = bz;
-                        hit.leaf = ld16(pool + link - 1).x;
-                        hit.slot = (uint32_t)win; hit.rec = cur;
-                        return true;
-                    }
-                } else {                                    // inner, :84-97
-                    if (COUNT) cnt.inner++;
-                    uint4 c = ld16(pool + link);
-                    float cx = ubf(c.x), cy = ubf(c.y), cz = ubf(c.z);
-                    // geom.c:53-65 get_corrected_subspace_idx
-                    uint32_t sub = ((cx == ex) ? (dx < 0.0f) : (cx > ex))
-                                 | (((cy == ey) ? (dy < 0.0f) : (cy > ey)) << 1)
-                                 | (((cz == ez) ? (dz < 0.0f) : (cz > ez)) << 2);
-                    uint32_t mask = (meta >> 8) & 0xFFu;
-                    if (sp >= CAP) { overflow = true; return false; }
-                    stack[sp++] = make_uint4(cur | CONT_BIT | (sub << VOXP_OFF_BITS),
-                                             __float_as_uint(ex), __float_as_uint(ey),
-                                             __float_as_uint(ez));
-                    if ((mask >> sub) & 1u) {
-                        cur = link + 1u + 2u * (uint32_t)__popc(mask & ((1u << sub) - 1u));
-                        ox = ex; oy = ey; oz = ez;
-                        continue;
-                    }
-                }
+                scan = false;
+                resume = true;
             }
+        } else if (!in) {
+            resume = true;
         } else {
-            // ---- the entry octant found nothing: planes, search.c:105-148
-            uint32_t node = cur & VOXP_OFF_MASK;
-            uint32_t sub = (cur >> VOXP_OFF_BITS) & 7u;
-            uint4 a = ld16(pool + node);
-            uint4 b = ld16(pool + node + 1);
-            uint32_t link = b.w, mask = (b.z >> 8) & 0xFFu;
-            uint4 c = ld16(pool + link);
-            float lx = ubf(a.x), ly = ubf(a.y), lz = ubf(a.z);
-            float hx = ubf(a.w), hy = ubf(b.x), hz = ubf(b.y);
-            float px[3], py[3], pz[3];
-            int pidx[3];
-            int pc = 0;
-#pragma unroll
-            for (int p = 0; p < 3; p++) {
-                float cp = p == 0 ? ubf(c.x) : (p == 1 ? ubf(c.y) : ubf(c.z));
-                float rx, ry, rz;
-                if (hit_plane(p, ox, oy, oz, dx, dy, dz, cp, lx, ly, lz, hx, hy, hz, rx, ry, rz)) {
-                    px[pc] = rx; py[pc] = ry; pz[pc] = rz; pidx[pc] = p; pc++;
-                }
+            uint32_t meta = u1.z, link = u1.w, kind = meta & 3u;
+            if (kind == VOXP_KIND_DENSE) {                      // search.c:31-37
+                hit.x = ex; hit.y = ey; hit.z = ez;
+                hit.leaf = link; hit.slot = 0xFFu; hit.rec = cur;
+                return true;
             }
-            // The reference's in-place selection sort (search.c:115-134): strict
-            // '<' and immediate swaps, reproduced exactly including its order
-            // among equal distances.
-            float m[3];
-#pragma unroll
-            for (int i = 0; i < 3; i++) m[i] = i < pc ? l1(ox, oy, oz, px[i], py[i], pz[i]) : 0.0f;
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-#pragma unroll
-                for (int j = i + 1; j < 3; j++) {
-                    if (j < pc && m[j] < m[i]) {
-                        float tx = px[i], ty = py[i], tz = pz[i], tm = m[i];
-                        int ti = pidx[i];
-                        px[i] = px[j]; py[i] = py[j]; pz[i] = pz[j]; m[i] = m[j]; pidx[i] = pidx[j];
-                        px[j] = tx; py[j] = ty; pz[j] = tz; m[j] = tm; pidx[j] = ti;
-                    }
+            if (kind == VOXP_KIND_LEAF) {                       // search.c:39-50
+                vn = meta >> 2;
+                if (vn == 0) {
+                    resume = true;
+                } else {
+                    scan = true; vrec = cur; vid = u2.x; cur = link; vi = 0;
+                    best = __int_as_float(0x7f800000); win = -1;
+                    ox = ex; oy = ey; oz = ez;
                 }
-            }
-            // Octants visited after each crossing (search.c:137) and their
-            // records; NULL children are skipped (they return NULL at once).
-            uint32_t recs[3];
-            int nt = 0;
-            uint32_t s = sub;
-            float qx[3], qy[3], qz[3];
-#pragma unroll
-            for (int i = 0; i < 3; i++) {
-                if (i < pc) {
-                    s ^= 1u << pidx[i];
-                    if ((mask >> s) & 1u) {
-                        recs[nt] = link + 1u + 2u * (uint32_t)__popc(mask & ((1u << s) - 1u));
-                        qx[nt] = px[i]; qy[nt] = py[i]; qz[nt] = pz[i];
-                        nt++;
-                    }
+            } else {                                            // inner node
+                if (COUNT) cnt.inner++;
+                float cx = ubf(u2.x), cy = ubf(u2.y), cz = ubf(u2.z);
+                // geom.c:53-65 get_corrected_subspace_idx
+                uint32_t sub = ((cx == ex) ? (dx < 0.0f) : (cx > ex))
+                             | (((cy == ey) ? (dy < 0.0f) : (cy > ey)) << 1)
+                             | (((cz == ez) ? (dz < 0.0f) : (cz > ez)) << 2);
+                uint32_t mask = (meta >> 8) & 0xFFu;
+                // search.c:105-113: the crossings with the three dividing
+                // planes that lie in the box, kept in axis order
+                float qx0, qy0, qz0, qx1, qy1, qz1, qx2, qy2, qz2;
+                bool v0 = hit_plane(0, ex, ey, ez, dx, dy, dz, cx, lx, ly, lz, hx, hy, hz, qx0, qy0, qz0);
+                bool v1 = hit_plane(1, ex, ey, ez, dx, dy, dz, cy, lx, ly, lz, hx, hy, hz, qx1, qy1, qz1);
+                bool v2 = hit_plane(2, ex, ey, ez, dx, dy, dz, cz, lx, ly, lz, hx, hy, hz, qx2, qy2, qz2);
+                int pc = (int)v0 + (int)v1 + (int)v2;
+                // compacted slots a, b, c = first, second, third valid crossing
+                float ax = v0 ? qx0 : (v1 ? qx1 : qx2);
+                float ay = v0 ? qy0 : (v1 ? qy1 : qy2);
+                float az = v0 ? qz0 : (v1 ? qz1 : qz2);
+                int ai = v0 ? 0 : (v1 ? 1 : 2);
+                bool ab1 = v0 && v1;
+                float bxp = ab1 ? qx1 : qx2, byp = ab1 ? qy1 : qy2, bzp = ab1 ? qz1 : qz2;
+                int bi = ab1 ? 1 : 2;
+                float cxp = qx2, cyp = qy2, czp = qz2;
+                int ci = 2;
+                float ma = l1(ex, ey, ez, ax, ay, az);
+                float mb = l1(ex, ey, ez, bxp, byp, bzp);
+                float mc = l1(ex, ey, ez, cxp, cyp, czp);
+                // search.c:115-134: selection sort with immediate swaps on '<'
+                if (pc > 1 && mb < ma) {
+                    float t0 = ax; ax = bxp; bxp = t0; t0 = ay; ay = byp; byp = t0; t0 = az; az = bzp; bzp = t0;
+                    t0 = ma; ma = mb; mb = t0; int ti = ai; ai = bi; bi = ti;
                 }
-            }
-            if (nt > 0) {
-                if (sp + nt - 1 > CAP) { overflow = true; return false; }
-#pragma unroll
-                for (int i = 2; i >= 1; i--) {
-                    if (i < nt)
-                        stack[sp++] = make_uint4(recs[i], __float_as_uint(qx[i]),
-                                                 __float_as_uint(qy[i]), __float_as_uint(qz[i]));
+                if (pc > 2 && mc < ma) {
+                    float t0 = ax; ax = cxp; cxp = t0; t0 = ay; ay = cyp; cyp = t0; t0 = az; az = czp; czp = t0;
+                    t0 = ma; ma = mc; mc = t0; int ti = ai; ai = ci; ci = ti;
                 }
-                cur = recs[0];
-                ox = qx[0]; oy = qy[0]; oz = qz[0];
-                continue;
+                if (pc > 2 && mc < mb) {
+                    float t0 = bxp; bxp = cxp; cxp = t0; t0 = byp; byp = cyp; cyp = t0; t0 = bzp; bzp = czp; czp = t0;
+                    t0 = mb; mb = mc; mc = t0; int ti = bi; bi = ci; ci = ti;
+                }
+                // search.c:137: each crossing flips one octant bit; NULL
+                // children are skipped (they return NULL at once)
+                uint32_t s1 = sub ^ (1u << ai), s2 = s1 ^ (1u << bi), s3 = s2 ^ (1u << ci);
+                bool w1 = pc > 0 && ((mask >> s1) & 1u);
+                bool w2 = pc > 1 && ((mask >> s2) & 1u);
+                bool w3 = pc > 2 && ((mask >> s3) & 1u);
+                int npush = (int)w1 + (int)w2 + (int)w3;
+                if (sp + npush > CAP) { overflow = true; return false; }
+                if (w3) stack[sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s3) - 1u)),
+                                                 __float_as_uint(cxp), __float_as_uint(cyp), __float_as_uint(czp));
+                if (w2) stack[sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s2) - 1u)),
+                                                 __float_as_uint(bxp), __float_as_uint(byp), __float_as_uint(bzp));
+                if (w1) stack[sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s1) - 1u)),
+                                                 __float_as_uint(ax), __float_as_uint(ay), __float_as_uint(az));
+                if ((mask >> sub) & 1u) {                       // search.c:92-93
+                    cur = link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << sub) - 1u));
+                    ox = ex; oy = ey; oz = ez;
+                } else {
+                    resume = true;
+                }
             }
         }
-        // ---- nothing found below this task: resume the deferred work
-        if (sp == 0) return false;
-        uint4 e = stack[--sp];
-        cur = e.x;
-        ox = ubf(e.y); oy = ubf(e.z); oz = ubf(e.w);
+        if (resume) {
+            if (sp == 0) return false;
+            uint4 e = stack[--sp];
+            cur = e.x;
+            ox = ubf(e.y); oy = ubf(e.z); oz = ubf(e.w);
+        }
     }
 }
 
@@ -322,14 +319,15 @@ __device__ __forceinline__ bool trace_ball(const DevTree &t, float cx, float cy,
                         return true;
                 }
             } else {
+                if (COUNT) cnt.inner++;
                 uint32_t mask = (b.z >> 8) & 0xFFu;
                 int k = __popc(mask);
                 if (k > 0) {
                     if (sp + k - 1 > CAP) { overflow = true; return false; }
                     // children in octant order = consecutive records; push in
                     // reverse so octant order is the pop order.
-                    for (int i = k - 1; i >= 1; i--) stack[sp++] = link + 1u + 2u * (uint32_t)i;
-                    cur = link + 1u;
+                    for (int i = k - 1; i >= 1; i--) stack[sp++] = link + VOXP_REC_UNITS * (uint32_t)i;
+                    cur = link;
                     continue;
                 }
             }

@@ -38,7 +38,7 @@ struct vox_cuda_tree {
     uint32_t *d_rec_of_id;
     uint32_t *d_status;      // bit 0: a traversal stack overflowed
     DevTree dev;
-    int cap_class;           // 0: 24 entries, 1: 64, 2: 256
+    int cap_class;           // 0: 28 stack entries, 1: 64, 2: 256
     FlatTree flat;           // host copy: pre-order table and maps
     size_t pool_bytes;
 };
@@ -47,11 +47,12 @@ namespace {
 
 std::atomic<uint64_t> g_launches{0};
 
-constexpr int CAP0 = 24, CAP1 = 64, CAP2 = 256;
+// Ray stacks hold at most 3 pending children per inner level on the path.
+constexpr int CAP0 = 28, CAP1 = 64, CAP2 = 256;
 
 int cap_class_for_depth(uint64_t depth)
 {
-    uint64_t need = 2 * depth + 2;
+    uint64_t need = 3 * depth + 1;
     if (need <= (uint64_t)CAP0) return 0;
     if (need <= (uint64_t)CAP1) return 1;
     if (need <= (uint64_t)CAP2) return 2;
@@ -396,7 +397,7 @@ EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out
     int cls = cap_class_for_depth(t->flat.depth);
     if (cls < 0) { delete t; return VOX_CUDA_EDEPTH; }
     t->cap_class = cls;
-    size_t units = t->flat.units.size() ? t->flat.units.size() : 2;
+    size_t units = t->flat.units.size() ? t->flat.units.size() : VOXP_REC_UNITS;
     size_t nodes = t->flat.preorder.size();
     t->pool_bytes = units * 16;
     if (cudaMalloc(&t->d_pool, t->pool_bytes) != cudaSuccess) { delete t; return VOX_CUDA_ENOMEM; }
@@ -443,7 +444,7 @@ EXPORT int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info
     info->dense_leaves = f.n_dense;
     info->dots = f.n_dots;
     info->depth = f.depth;
-    info->device_bytes = (f.units.size() ? f.units.size() : 2) * 16 + 4 * f.preorder.size() + 4;
+    info->device_bytes = (f.units.size() ? f.units.size() : VOXP_REC_UNITS) * 16 + 4 * f.preorder.size() + 4;
     return VOX_CUDA_OK;
 }
 
