@@ -34,6 +34,7 @@ using vox::RayHit;
 
 struct vox_cuda_tree {
     int device;
+    float bbox[6];           // root bounding box (for scheduling only)
     uint4 *d_pool;
     uint32_t *d_rec_of_id;
     uint32_t *d_status;      // bit 0: a traversal stack overflowed
@@ -133,16 +134,36 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
 
 constexpr int TILE_W = 16, TILE_H = 8;   // block tile; warps are 8x4
 
+// k-th index of 0..n-1 taken outward from c: c, c+1, c-1, c+2, ... then the
+// rest of the longer side.
+__device__ __forceinline__ uint32_t centre_out(uint32_t k, uint32_t c, uint32_t n)
+{
+    uint32_t m = min(c, n - 1 - c);
+    if (k <= 2 * m) return (k & 1) ? c + (k + 1) / 2 : c - k / 2;
+    uint32_t j = k - (2 * m + 1);
+    return (c < n - 1 - c) ? c + m + 1 + j : c - m - 1 - j;
+}
+
+// Block tiles are issued rows-first outward from the tile where the tree's
+// centre projects: the rays that walk the tree longest start first, so the
+// frame does not wait on late starters.  Every tile is drawn exactly once.
+struct TileOrder {
+    uint32_t nbx, nby, cbx, cby;
+};
+
 template <int CAP, bool COUNT>
 __global__ void __launch_bounds__(128) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
-                                                     uint32_t h, const uint8_t *__restrict__ tex,
+                                                     uint32_t h, TileOrder ord,
+                                                     const uint8_t *__restrict__ tex,
                                                      uint32_t *__restrict__ argb,
                                                      unsigned long long *__restrict__ counts,
                                                      uint32_t *__restrict__ status)
 {
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t px = blockIdx.x * TILE_W + (warp & 1) * 8 + (lane & 7);
-    uint32_t py = blockIdx.y * TILE_H + (warp >> 1) * 4 + (lane >> 3);
+    uint32_t by = centre_out(blockIdx.x / ord.nbx, ord.cby, ord.nby);
+    uint32_t bx = centre_out(blockIdx.x % ord.nbx, ord.cbx, ord.nbx);
+    uint32_t px = bx * TILE_W + (warp & 1) * 8 + (lane & 7);
+    uint32_t py = by * TILE_H + (warp >> 1) * 4 + (lane >> 3);
     Counts c{0, 0, 0};
     bool overflow = false;
     if (px < w && py < h) {
@@ -301,15 +322,54 @@ cudaError_t launch_balls(const vox_cuda_tree *t, const float *c, const float *r,
     return cudaGetLastError();
 }
 
+// Screen position of the centre of the tree's bounding box (inverse of
+// screen2world), clamped to the frame; the frame centre when it lies behind
+// the camera.  Only used to order the tiles.
+TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h)
+{
+    TileOrder o;
+    o.nbx = (w + TILE_W - 1) / TILE_W;
+    o.nby = (h + TILE_H - 1) / TILE_H;
+    double v[3], c[3];
+    for (int i = 0; i < 3; i++) v[i] = 0.5 * ((double)t->bbox[i] + t->bbox[3 + i]) - cam.position[i];
+    double shift = 0.0;
+    if (cam.kind == VOX_CUDA_CAMERA_DOOM) {
+        c[0] = v[0] * cam.cosphi + v[1] * cam.sinphi;
+        c[1] = v[1] * cam.cosphi - v[0] * cam.sinphi;
+        c[2] = v[2];
+        shift = cam.k;
+    } else {
+        // rotate by the conjugate quaternion: v + w t + u x t, t = 2 (u x v), u = -q.xyz
+        double qw = cam.rotation[0], ux = -cam.rotation[1], uy = -cam.rotation[2], uz = -cam.rotation[3];
+        double tx = 2 * (uy * v[2] - uz * v[1]), ty = 2 * (uz * v[0] - ux * v[2]), tz = 2 * (ux * v[1] - uy * v[0]);
+        c[0] = v[0] + qw * tx + (uy * tz - uz * ty);
+        c[1] = v[1] + qw * ty + (uz * tx - ux * tz);
+        c[2] = v[2] + qw * tz + (ux * ty - uy * tx);
+    }
+    double sx = 0.5 * w, sy = 0.5 * h;
+    if (c[1] > 1e-6 && cam.mul != 0.0f) {
+        sx = (c[0] / c[1] + cam.xsub) / cam.mul;
+        sy = (cam.ysub + shift - c[2] / c[1]) / cam.mul;
+    }
+    if (!(sx >= 0)) sx = 0;               // also catches NaN
+    if (!(sy >= 0)) sy = 0;
+    if (sx > w - 1) sx = w - 1;
+    if (sy > h - 1) sy = h - 1;
+    o.cbx = (uint32_t)sx / TILE_W;
+    o.cby = (uint32_t)sy / TILE_H;
+    return o;
+}
+
 template <bool COUNT>
 cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                           const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s)
 {
-    dim3 block(128), grid((w + TILE_W - 1) / TILE_W, (h + TILE_H - 1) / TILE_H);
+    TileOrder ord = tile_order(t, cam, w, h);
+    dim3 block(128), grid(ord.nbx * ord.nby);
     switch (t->cap_class) {
-    case 0: render_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, tex, argb, counts, t->d_status); break;
-    case 1: render_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, tex, argb, counts, t->d_status); break;
-    default: render_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, tex, argb, counts, t->d_status); break;
+    case 0: render_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
+    case 1: render_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
+    default: render_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
     }
     g_launches++;
     return cudaGetLastError();
@@ -416,6 +476,14 @@ EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out
         cudaFree(t->d_pool); cudaFree(t->d_rec_of_id); cudaFree(t->d_status);
         delete t;
         return VOX_CUDA_ECUDA;
+    }
+    if (root) {
+        for (int i = 0; i < 3; i++) {
+            t->bbox[i] = root->bounding_box.min[i];
+            t->bbox[3 + i] = root->bounding_box.max[i];
+        }
+    } else {
+        for (int i = 0; i < 6; i++) t->bbox[i] = 0.0f;
     }
     t->dev.pool = t->d_pool;
     t->dev.rec_of_id = t->d_rec_of_id;
