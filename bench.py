@@ -63,6 +63,8 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the incoherent-query and batched-frame measurements")
     p.add_argument("--frames", type=int, default=NFRAMES,
                    help="orbit frames per step (profiling runs only; the benchmark uses 120)")
     return p.parse_args()
@@ -198,6 +200,101 @@ def cpu_baseline_sample(tree_ptr, states, tex, budget_s=3.0):
     return {"value": frames * W * H / dt / 1e6, "unit": "Mrays/s", "cores": n, "kind": "port",
             "sample": f"{frames} of the {NFRAMES} orbit frames at {W}x{H}, BEST, {dt:.2f} s wall"}
 
+
+
+
+def timed_reps(torch, fn, reps, flush):
+    """Best-of and mean CUDA-event time (ms) of fn() over reps runs, L2 flushed before each."""
+    stream = torch.cuda.current_stream()
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return min(ts), float(np.mean(ts))
+
+
+def measure_incoherent(torch, vg, dt, flush):
+    """16M rays (origins uniform in twice the tree's box, directions uniform on
+    the sphere) and 1M balls (centres in the box, radii U[0.5, 8]) on the
+    256^3 tree, through the device entry points."""
+    from voxvision_gb300 import workloads as wl
+    sp = torch.cuda.current_stream().cuda_stream
+    n = 1 << 24
+    o, d = wl.incoherent_rays(n, -128.0, 384.0, 3)
+    to, td = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    leaf = torch.empty(n, dtype=torch.int32, device="cuda")
+    slot = torch.empty(n, dtype=torch.uint8, device="cuda")
+    pts = torch.empty(n, 3, dtype=torch.float32, device="cuda")
+    nb = 1 << 20
+    c, r = wl.balls(nb, 0.0, 256.0, 0.5, 8.0, 4)
+    tc, tr = torch.from_numpy(c).cuda(), torch.from_numpy(r).cuda()
+    hit = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    rays = lambda: dt.rays_device(to, td, leaf, slot, pts, stream=sp)
+    balls = lambda: dt.balls_device(tc, tr, hit, stream=sp)
+    for _ in range(3):
+        rays(); balls()
+    rb, rm = timed_reps(torch, rays, 5, flush)
+    bb, bm = timed_reps(torch, balls, 5, flush)
+    return {"rays": n, "rays_ms": rm, "rays_mrays_s": n / (rm * 1e-3) / 1e6,
+            "ray_hit_fraction": float((leaf != -1).float().mean().item()),
+            "balls": nb, "balls_ms": bm, "balls_mq_s": nb / (bm * 1e-3) / 1e6,
+            "ball_hit_fraction": float(hit.float().mean().item()),
+            "inputs": "rays: origins U[-128,384)^3 seed 3, dirs uniform on S^2; balls: centres U[0,256)^3, "
+                      "r U[0.5,8] seed 4"}
+
+
+def measure_batched(torch, vg, flush, tex_dev):
+    """Mixed-camera load: 64 frames, resolutions uniform over 320x240..3840x2160,
+    trees uniform over the 64^3..512^3 noise volumes, random orbit poses; one
+    persistent kernel replayed from a CUDA graph (autotuned) against 64 plain
+    per-frame launches."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    sp = torch.cuda.current_stream().cuda_stream
+    trees = []
+    for n, seed, solid in wl.BATCH_TREES:
+        ht = vg.HostTree.from_voxels(wl.voxels_from_mask(wl.noise_volume(n, seed, solid)))
+        trees.append((n, ht, vg.DeviceTree(ht.ptr)))
+    jobs = []
+    for ti, (w, h), az, el in wl.batch_poses(64, len(trees), 14):
+        n, _, dt = trees[ti]
+        cam = HostCamera(0)
+        cam.set_window_size(w, h)
+        cam.set_position(wl.pose_position((n / 2,) * 3, 1.5 * n * 3 ** 0.5, az, el))
+        cam.look_at((n / 2,) * 3)
+        jobs.append((dt, cam.gpu_struct(), w, h, tex_dev, torch.empty(w * h, dtype=torch.int32, device="cuda")))
+    rays = sum(w * h for _, _, w, h, _, _ in jobs)
+
+    def plain():
+        for dt, cam, w, h, tex, out in jobs:
+            dt.render_device(cam, w, h, tex, out, stream=sp)
+
+    for _ in range(3):
+        plain()
+    pb, pm = timed_reps(torch, plain, 5, flush)
+    batch = vg.FrameBatch(jobs)
+    cfg, tune_ms = batch.autotune(stream=sp, reps=2)
+    launch = lambda: batch.launch(stream=sp)
+    for _ in range(3):
+        launch()
+    bb, bm = timed_reps(torch, launch, 5, flush)
+    # identical frames: the batch's output against the plain launches
+    outs = [j[5].clone() for j in jobs]
+    plain()
+    torch.cuda.synchronize()
+    same = all(bool(torch.equal(a, j[5])) for a, j in zip(outs, jobs))
+    batch.close()
+    return {"frames": len(jobs), "rays": rays, "trees": [t[0] for t in trees],
+            "plain_ms": pm, "plain_mrays_s": rays / (pm * 1e-3) / 1e6,
+            "batched_ms": bm, "batched_mrays_s": rays / (bm * 1e-3) / 1e6,
+            "speedup": pm / bm, "autotuned": cfg, "frames_identical": same,
+            "form": "persistent kernel, work queue, CUDA graph replay"}
 
 # ------------------------------------------------------------------ our arm
 
@@ -338,6 +435,9 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(workload_config(info, len(vox)), frames_per_step=nf, rays_per_step=rays_step), "roofline": roofline, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk}
+    if not args.no_extras:
+        line["incoherent"] = measure_incoherent(torch, vg, dt, flush)
+        line["batched"] = measure_batched(torch, vg, flush, d_tex)
     if not args.no_cpu_baseline and world >= 1:
         line["cpu_baseline"] = cpu_baseline_sample(ht.ptr, states, tex)
     print(json.dumps(line), flush=True)

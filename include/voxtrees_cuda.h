@@ -168,6 +168,52 @@ int vox_cuda_ray_counts_device(const vox_cuda_tree *tree, const float *origins, 
 int vox_cuda_ball_counts_device(const vox_cuda_tree *tree, const float *centres,
                                 const float *radii, size_t n, uint64_t *counts, void *stream);
 
+/* ---- Batched frames ------------------------------------------------------
+ * Many frames -- cameras of any resolution over any number of resident
+ * trees -- drawn by one persistent kernel from a shared work queue and
+ * replayed from a CUDA graph.  Each frame is bit-identical to a
+ * vox_cuda_render_device call with the same tree, camera and size; the
+ * batch only removes the per-frame launch and the per-frame tail.
+ * Replaces: a loop of vox_render calls over several contexts
+ * (src/voxrnd/renderer.c:200-319), one frame at a time. */
+typedef struct {
+    const vox_cuda_tree *tree;
+    vox_cuda_camera camera;
+    uint32_t w, h;               /* w a multiple of 16, h of 4            */
+    const uint8_t *texture;      /* device, 32^3 bytes                    */
+    uint32_t *argb;              /* device, w * h pixels                  */
+} vox_cuda_frame_job;
+
+/* tile_w x tile_h pixels per warp tile: 8x4, 16x2, 32x1 (one ray per thread)
+ * or 8x8, 16x4 (two rays per thread); tiles_per_grab: tiles a warp takes
+ * from the queue at once (1..64); blocks_per_sm: resident 128-thread blocks
+ * per SM (1..16). */
+typedef struct {
+    uint32_t tile_w, tile_h;
+    uint32_t tiles_per_grab;
+    uint32_t blocks_per_sm;
+} vox_cuda_batch_config;
+
+typedef struct vox_cuda_batch vox_cuda_batch;
+
+/* Build a batch of njobs (1..1024) frames; config NULL = 8x4 tiles, 1 tile
+ * per grab, 4 blocks per SM.  The trees, textures and frames must outlive the
+ * batch. */
+int vox_cuda_batch_create(const vox_cuda_frame_job *jobs, uint32_t njobs,
+                          const vox_cuda_batch_config *config, vox_cuda_batch **out);
+/* Change one frame's camera; takes effect at the next launch. */
+int vox_cuda_batch_set_camera(vox_cuda_batch *batch, uint32_t job, const vox_cuda_camera *camera);
+/* Replay the graph on `stream` (asynchronous).  Waits for the batch's
+ * previous replay first, so cameras set in between are the ones drawn. */
+int vox_cuda_batch_launch(vox_cuda_batch *batch, void *stream);
+int vox_cuda_batch_get_config(const vox_cuda_batch *batch, vox_cuda_batch_config *config);
+int vox_cuda_batch_set_config(vox_cuda_batch *batch, const vox_cuda_batch_config *config);
+/* Time every candidate configuration (reps timed replays each, 0 = 3) on this
+ * batch, keep the fastest and report it (chosen, best_ms may be NULL). */
+int vox_cuda_batch_autotune(vox_cuda_batch *batch, void *stream, uint32_t reps,
+                            vox_cuda_batch_config *chosen, float *best_ms);
+int vox_cuda_batch_free(vox_cuda_batch *batch);
+
 /* Library version and the number of kernel launches made so far by this
  * process (all entry points); used to report launch counts. */
 const char *vox_cuda_version(void);

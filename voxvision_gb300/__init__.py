@@ -13,10 +13,10 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, CameraStruct,
-                   TreeInfo, VoxCudaError, available, check, lib)
+from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, BatchConfig, CameraStruct,
+                   FrameJob, TreeInfo, VoxCudaError, available, check, lib)
 
-__all__ = ["HostTree", "DeviceTree", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
+__all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
            "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size"]
 
 
@@ -186,3 +186,56 @@ def camera_struct(state: dict) -> CameraStruct:
 
 
 Camera = CameraStruct
+
+
+class FrameBatch:
+    """vox_cuda_batch: many frames in one persistent kernel replayed from a
+    CUDA graph.  jobs: iterable of (DeviceTree, CameraStruct, w, h,
+    texture_device_ptr_or_tensor, argb_device_ptr_or_tensor)."""
+
+    def __init__(self, jobs, config: BatchConfig | None = None):
+        jobs = list(jobs)
+        arr = (FrameJob * len(jobs))()
+        for i, (tree, cam, w, h, tex, argb) in enumerate(jobs):
+            arr[i].tree = tree.h.value
+            arr[i].camera = cam
+            arr[i].w, arr[i].h = w, h
+            arr[i].texture = _dptr(tex).value
+            arr[i].argb = _dptr(argb).value
+        self._keep = jobs
+        h = C.c_void_p()
+        check(lib().vox_cuda_batch_create(arr, len(jobs), C.byref(config) if config else None, C.byref(h)),
+              "vox_cuda_batch_create")
+        self.h = h
+
+    def launch(self, stream=None):
+        check(lib().vox_cuda_batch_launch(self.h, stream), "vox_cuda_batch_launch")
+
+    def set_camera(self, job: int, cam: CameraStruct):
+        check(lib().vox_cuda_batch_set_camera(self.h, job, C.byref(cam)), "vox_cuda_batch_set_camera")
+
+    def config(self) -> dict:
+        c = BatchConfig()
+        check(lib().vox_cuda_batch_get_config(self.h, C.byref(c)), "vox_cuda_batch_get_config")
+        return c.as_dict()
+
+    def set_config(self, cfg: BatchConfig):
+        check(lib().vox_cuda_batch_set_config(self.h, C.byref(cfg)), "vox_cuda_batch_set_config")
+
+    def autotune(self, stream=None, reps: int = 3):
+        c = BatchConfig()
+        ms = C.c_float()
+        check(lib().vox_cuda_batch_autotune(self.h, stream, reps, C.byref(c), C.byref(ms)),
+              "vox_cuda_batch_autotune")
+        return c.as_dict(), float(ms.value)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().vox_cuda_batch_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -41,6 +41,21 @@ class TreeInfo(C.Structure):
                 ("nodes", "inner", "leaves", "dense_leaves", "dots", "depth", "device_bytes")]
 
 
+class FrameJob(C.Structure):
+    """vox_cuda_frame_job (include/voxtrees_cuda.h)."""
+    _fields_ = [("tree", C.c_void_p), ("camera", CameraStruct), ("w", C.c_uint32), ("h", C.c_uint32),
+                ("texture", C.c_void_p), ("argb", C.c_void_p)]
+
+
+class BatchConfig(C.Structure):
+    """vox_cuda_batch_config (include/voxtrees_cuda.h)."""
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("tiles_per_grab", C.c_uint32),
+                ("blocks_per_sm", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 _lib = None
 
 # name -> (restype, argtypes)
@@ -65,6 +80,13 @@ SIGNATURES = {
                                           _vp]),
     "vox_cuda_render_quality_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp,
                                                  _vp, _vp]),
+    "vox_cuda_batch_create": (C.c_int, [C.POINTER(FrameJob), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
+    "vox_cuda_batch_set_camera": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct)]),
+    "vox_cuda_batch_launch": (C.c_int, [_vp, _vp]),
+    "vox_cuda_batch_get_config": (C.c_int, [_vp, C.POINTER(BatchConfig)]),
+    "vox_cuda_batch_set_config": (C.c_int, [_vp, C.POINTER(BatchConfig)]),
+    "vox_cuda_batch_autotune": (C.c_int, [_vp, _vp, _u32, C.POINTER(BatchConfig), C.POINTER(C.c_float)]),
+    "vox_cuda_batch_free": (C.c_int, [_vp]),
     "vox_cuda_render_counts_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp]),
     "vox_cuda_ray_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "vox_cuda_ball_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),

@@ -1,0 +1,384 @@
+/*
+ * batch.cu -- many frames (cameras of any resolution over several resident
+ * trees) rendered by one persistent kernel, replayed from a CUDA graph.
+ *
+ * A per-frame launch ends with a tail: the few warps whose rays walk the tree
+ * longest finish long after the rest of the frame, and the SMs idle while they
+ * do.  Here all the frames' tiles sit in one work queue.  Persistent warps
+ * (a fixed number of blocks per SM) take tiles from a global counter until it
+ * runs out, so the tail of one frame overlaps the body of the others and no
+ * SM waits.  Frames are queued largest first and each frame's tiles outward
+ * from where its tree projects, so long-running tiles start early.
+ *
+ * Every ray is the same search as vox_cuda_render's (traverse.cuh), so each
+ * frame is bit-identical to a plain vox_cuda_render call.
+ *
+ * The graph holds three nodes: copy the job table (cameras may change between
+ * replays), zero the queue counter, run the kernel.  The autotuner times each
+ * (tile shape, tiles per grab, blocks per SM) candidate on the batch itself.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "internal.h"
+
+#define EXPORT extern "C" __attribute__((visibility("default")))
+
+using vox::RayHit;
+
+namespace {
+
+constexpr uint32_t MAX_JOBS = 1024;
+
+struct BatchJobDev {
+    DevTree tree;
+    vox_cuda_camera cam;
+    const uint8_t *tex;
+    uint32_t *argb;
+    uint32_t *status;
+    uint32_t w, h;
+    uint32_t ntx, nty;      // tiles across / down for the batch's tile shape
+    uint32_t ctx, cty;      // tile where the tree's centre projects
+    uint32_t tile_base;     // first queue index of this frame's tiles
+    uint32_t pad;
+};
+
+// Queue index -> frame: the last job whose tile_base is <= tile.
+__device__ __forceinline__ uint32_t find_job(const uint32_t *base, uint32_t njobs, uint32_t tile)
+{
+    uint32_t lo = 0, hi = njobs;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= tile) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <int CAP, int TW, int TH>
+__global__ void __launch_bounds__(128) batch_kernel(const BatchJobDev *__restrict__ jobs, uint32_t njobs,
+                                                    uint32_t total_tiles, uint32_t grab,
+                                                    uint32_t *__restrict__ counter)
+{
+    constexpr int RPT = TW * TH / 32;   // rays per thread per tile
+    __shared__ uint32_t base[MAX_JOBS];
+    for (uint32_t i = threadIdx.x; i < njobs; i += blockDim.x) base[i] = jobs[i].tile_base;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = atomicAdd(counter, grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= total_tiles) break;
+        uint32_t t1 = min(t0 + grab, total_tiles);
+        for (uint32_t tile = t0; tile < t1; tile++) {
+            const BatchJobDev &J = jobs[find_job(base, njobs, tile)];
+            uint32_t local = tile - J.tile_base;
+            uint32_t ty = vox::centre_out(local / J.ntx, J.cty, J.nty);
+            uint32_t tx = vox::centre_out(local % J.ntx, J.ctx, J.ntx);
+            const DevTree t = J.tree;
+            const vox_cuda_camera cam = J.cam;
+            const uint32_t w = J.w, h = J.h;
+#pragma unroll 1
+            for (int r = 0; r < RPT; r++) {
+                uint32_t p = (uint32_t)lane + 32u * (uint32_t)r;
+                uint32_t px = tx * TW + p % TW, py = ty * TH + p / TW;
+                if (px < w && py < h) {
+                    float dx, dy, dz;
+                    vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
+                    RayHit hh;
+                    vox::Counts c{0, 0, 0};
+                    bool overflow = false, hit = false;
+                    if (t.root != VOXP_EMPTY)
+                        hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1],
+                                                         cam.position[2], dx, dy, dz, hh, c, overflow);
+                    J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
+                    if (overflow) atomicOr(J.status, 1u);
+                }
+            }
+        }
+    }
+}
+
+struct Shape {
+    uint32_t tw, th;
+};
+const Shape kShapes[] = {{8, 4}, {16, 2}, {32, 1}, {8, 8}, {16, 4}};
+
+template <int CAP>
+cudaError_t launch_batch_cap(const vox_cuda_batch_config &c, const BatchJobDev *jobs, uint32_t njobs,
+                             uint32_t total, uint32_t *counter, int nsm, cudaStream_t s)
+{
+    dim3 grid(nsm * c.blocks_per_sm), block(128);
+    uint32_t g = c.tiles_per_grab;
+    if (c.tile_w == 8 && c.tile_h == 4) batch_kernel<CAP, 8, 4><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
+    else if (c.tile_w == 16 && c.tile_h == 2) batch_kernel<CAP, 16, 2><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
+    else if (c.tile_w == 32 && c.tile_h == 1) batch_kernel<CAP, 32, 1><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
+    else if (c.tile_w == 8 && c.tile_h == 8) batch_kernel<CAP, 8, 8><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
+    else batch_kernel<CAP, 16, 4><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
+    count_launch();
+    return cudaGetLastError();
+}
+
+bool valid_config(const vox_cuda_batch_config &c)
+{
+    bool shape = false;
+    for (const Shape &s : kShapes) shape |= (s.tw == c.tile_w && s.th == c.tile_h);
+    return shape && c.tiles_per_grab >= 1 && c.tiles_per_grab <= 64 && c.blocks_per_sm >= 1 &&
+           c.blocks_per_sm <= 16;
+}
+
+}  // namespace
+
+struct vox_cuda_batch {
+    int device = 0;
+    int nsm = 0;
+    int cap_class = 0;
+    std::vector<vox_cuda_frame_job> jobs;     // caller's jobs, in caller order
+    std::vector<uint32_t> order;              // queue position -> caller index
+    std::vector<BatchJobDev> table;           // host copy, in queue order
+    BatchJobDev *h_stage = nullptr;           // pinned copy the graph reads
+    BatchJobDev *d_table = nullptr;
+    uint32_t *d_counter = nullptr;            // work queue head (scratch)
+    uint32_t total_tiles = 0;
+    vox_cuda_batch_config cfg{8, 4, 1, 4};
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr;
+    bool launched = false;
+};
+
+namespace {
+
+void fill_table(vox_cuda_batch *b)
+{
+    uint32_t base = 0;
+    b->table.resize(b->jobs.size());
+    for (size_t q = 0; q < b->order.size(); q++) {
+        const vox_cuda_frame_job &j = b->jobs[b->order[q]];
+        BatchJobDev &d = b->table[q];
+        std::memset(&d, 0, sizeof d);
+        d.tree = j.tree->dev;
+        d.cam = j.camera;
+        d.tex = j.texture;
+        d.argb = j.argb;
+        d.status = j.tree->d_status;
+        d.w = j.w;
+        d.h = j.h;
+        vox::TileOrder o = tile_order(j.tree, j.camera, j.w, j.h, b->cfg.tile_w, b->cfg.tile_h);
+        d.ntx = o.nbx; d.nty = o.nby; d.ctx = o.cbx; d.cty = o.cby;
+        d.tile_base = base;
+        base += o.nbx * o.nby;
+    }
+    b->total_tiles = base;
+}
+
+cudaError_t launch_kernel(vox_cuda_batch *b, cudaStream_t s)
+{
+    uint32_t n = (uint32_t)b->jobs.size();
+    switch (b->cap_class) {
+    case 0: return launch_batch_cap<CAP0>(b->cfg, b->d_table, n, b->total_tiles, b->d_counter, b->nsm, s);
+    case 1: return launch_batch_cap<CAP1>(b->cfg, b->d_table, n, b->total_tiles, b->d_counter, b->nsm, s);
+    default: return launch_batch_cap<CAP2>(b->cfg, b->d_table, n, b->total_tiles, b->d_counter, b->nsm, s);
+    }
+}
+
+void drop_graph(vox_cuda_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// Capture: copy the job table, zero the queue head, run the kernel.
+int build_graph(vox_cuda_batch *b)
+{
+    drop_graph(b);
+    fill_table(b);
+    std::memcpy(b->h_stage, b->table.data(), b->table.size() * sizeof(BatchJobDev));
+    cudaStream_t s = b->cap_stream;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return VOX_CUDA_ECUDA;
+    cudaError_t e = cudaMemcpyAsync(b->d_table, b->h_stage, b->table.size() * sizeof(BatchJobDev),
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = launch_kernel(b, s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return VOX_CUDA_ECUDA;
+    }
+    b->graph = g;
+    if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+        drop_graph(b);
+        return VOX_CUDA_ECUDA;
+    }
+    return VOX_CUDA_OK;
+}
+
+void release(vox_cuda_batch *b)
+{
+    drop_graph(b);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    if (b->h_stage) cudaFreeHost(b->h_stage);
+    if (b->d_table) cudaFree(b->d_table);
+    if (b->d_counter) cudaFree(b->d_counter);
+}
+
+}  // namespace
+
+EXPORT int vox_cuda_batch_create(const vox_cuda_frame_job *jobs, uint32_t njobs,
+                                 const vox_cuda_batch_config *config, vox_cuda_batch **out)
+{
+    if (!out || !jobs || njobs == 0 || njobs > MAX_JOBS) return VOX_CUDA_EINVAL;
+    *out = nullptr;
+    for (uint32_t i = 0; i < njobs; i++) {
+        const vox_cuda_frame_job &j = jobs[i];
+        if (!j.tree || !j.texture || !j.argb) return VOX_CUDA_EINVAL;
+        if (j.w == 0 || j.h == 0 || (j.w & 0xF) || (j.h & 0x3)) return VOX_CUDA_EGEOMETRY;
+        if (j.camera.kind != VOX_CUDA_CAMERA_SIMPLE && j.camera.kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+    }
+    if (config && !valid_config(*config)) return VOX_CUDA_EINVAL;
+    vox_cuda_batch *b = new (std::nothrow) vox_cuda_batch();
+    if (!b) return VOX_CUDA_ENOMEM;
+    if (cudaGetDevice(&b->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess) {
+        delete b;
+        return VOX_CUDA_ENODEV;
+    }
+    b->jobs.assign(jobs, jobs + njobs);
+    for (uint32_t i = 0; i < njobs; i++) b->cap_class = std::max(b->cap_class, jobs[i].tree->cap_class);
+    // largest frames first
+    b->order.resize(njobs);
+    std::iota(b->order.begin(), b->order.end(), 0u);
+    std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t x, uint32_t y) {
+        return (uint64_t)jobs[x].w * jobs[x].h > (uint64_t)jobs[y].w * jobs[y].h;
+    });
+    if (config) b->cfg = *config;
+    size_t tb = njobs * sizeof(BatchJobDev);
+    if (cudaMallocHost(&b->h_stage, tb) != cudaSuccess || cudaMalloc(&b->d_table, tb) != cudaSuccess ||
+        cudaMalloc(&b->d_counter, sizeof(uint32_t)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess) {
+        release(b);
+        delete b;
+        return VOX_CUDA_ENOMEM;
+    }
+    int rc = build_graph(b);
+    if (rc) {
+        release(b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_batch_set_camera(vox_cuda_batch *b, uint32_t job, const vox_cuda_camera *camera)
+{
+    if (!b || !camera || job >= b->jobs.size()) return VOX_CUDA_EINVAL;
+    if (camera->kind != VOX_CUDA_CAMERA_SIMPLE && camera->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+    b->jobs[job].camera = *camera;
+    for (size_t q = 0; q < b->order.size(); q++) {
+        if (b->order[q] != job) continue;
+        BatchJobDev &d = b->table[q];
+        d.cam = *camera;
+        const vox_cuda_frame_job &j = b->jobs[job];
+        vox::TileOrder o = tile_order(j.tree, *camera, j.w, j.h, b->cfg.tile_w, b->cfg.tile_h);
+        d.ctx = o.cbx;
+        d.cty = o.cby;
+    }
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_batch_launch(vox_cuda_batch *b, void *stream)
+{
+    if (!b || !b->exec) return VOX_CUDA_EINVAL;
+    // The graph reads h_stage when it runs: wait for the previous replay before
+    // refreshing it with the current cameras.
+    if (b->launched && cudaEventSynchronize(b->done) != cudaSuccess) return VOX_CUDA_ECUDA;
+    std::memcpy(b->h_stage, b->table.data(), b->table.size() * sizeof(BatchJobDev));
+    cudaStream_t s = as_stream(stream);
+    if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return VOX_CUDA_ECUDA;
+    count_launch();
+    if (cudaEventRecord(b->done, s) != cudaSuccess) return VOX_CUDA_ECUDA;
+    b->launched = true;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_batch_get_config(const vox_cuda_batch *b, vox_cuda_batch_config *config)
+{
+    if (!b || !config) return VOX_CUDA_EINVAL;
+    *config = b->cfg;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_batch_set_config(vox_cuda_batch *b, const vox_cuda_batch_config *config)
+{
+    if (!b || !config || !valid_config(*config)) return VOX_CUDA_EINVAL;
+    if (b->launched && cudaEventSynchronize(b->done) != cudaSuccess) return VOX_CUDA_ECUDA;
+    b->cfg = *config;
+    return build_graph(b);
+}
+
+EXPORT int vox_cuda_batch_autotune(vox_cuda_batch *b, void *stream, uint32_t reps,
+                                   vox_cuda_batch_config *chosen, float *best_ms)
+{
+    if (!b) return VOX_CUDA_EINVAL;
+    if (reps == 0) reps = 3;
+    cudaStream_t s = as_stream(stream);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return VOX_CUDA_ECUDA;
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return VOX_CUDA_ECUDA; }
+    const uint32_t grabs[] = {1, 2, 4};
+    const uint32_t bpsm[] = {4, 8};
+    vox_cuda_batch_config best = b->cfg;
+    float best_t = 1e30f;
+    int rc = VOX_CUDA_OK;
+    for (const Shape &sh : kShapes) {
+        for (uint32_t g : grabs) {
+            for (uint32_t k : bpsm) {
+                vox_cuda_batch_config c{sh.tw, sh.th, g, k};
+                if ((rc = vox_cuda_batch_set_config(b, &c)) != VOX_CUDA_OK) goto out;
+                if ((rc = vox_cuda_batch_launch(b, stream)) != VOX_CUDA_OK) goto out;   // warm-up
+                float tmin = 1e30f;
+                for (uint32_t r = 0; r < reps; r++) {
+                    cudaEventRecord(e0, s);
+                    if ((rc = vox_cuda_batch_launch(b, stream)) != VOX_CUDA_OK) goto out;
+                    cudaEventRecord(e1, s);
+                    if (cudaEventSynchronize(e1) != cudaSuccess) { rc = VOX_CUDA_ECUDA; goto out; }
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    tmin = std::min(tmin, ms);
+                }
+                if (tmin < best_t) {
+                    best_t = tmin;
+                    best = c;
+                }
+            }
+        }
+    }
+    rc = vox_cuda_batch_set_config(b, &best);
+    if (chosen) *chosen = best;
+    if (best_ms) *best_ms = best_t;
+out:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+EXPORT int vox_cuda_batch_free(vox_cuda_batch *b)
+{
+    if (!b) return VOX_CUDA_EINVAL;
+    if (b->launched) cudaEventSynchronize(b->done);
+    release(b);
+    delete b;
+    return VOX_CUDA_OK;
+}

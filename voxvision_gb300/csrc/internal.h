@@ -1,0 +1,78 @@
+/*
+ * internal.h -- definitions shared by the translation units of
+ * libvoxtrees_cuda (not part of the C ABI).
+ */
+#ifndef VOX_INTERNAL_H
+#define VOX_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "flatten.h"
+#include "pool_layout.h"
+#include "traverse.cuh"
+#include "../../include/voxtrees_cuda.h"
+
+using vox::DevTree;
+
+struct vox_cuda_tree {
+    int device;
+    float bbox[6];           // root bounding box (for scheduling only)
+    uint4 *d_pool;
+    uint32_t *d_rec_of_id;
+    uint32_t *d_status;      // bit 0: a traversal stack overflowed
+    DevTree dev;
+    int cap_class;           // 0: 28 stack entries, 1: 64, 2: 256
+    FlatTree flat;           // host copy: pre-order table and maps
+    size_t pool_bytes;
+};
+
+
+// Ray stacks hold at most 3 pending children per inner level on the path.
+constexpr int CAP0 = 28, CAP1 = 64, CAP2 = 256;
+
+inline int cap_class_for_depth(uint64_t depth)
+{
+    uint64_t need = 3 * depth + 1;
+    if (need <= (uint64_t)CAP0) return 0;
+    if (need <= (uint64_t)CAP1) return 1;
+    if (need <= (uint64_t)CAP2) return 2;
+    return -1;
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int status_of(cudaError_t e) { return e == cudaSuccess ? VOX_CUDA_OK : VOX_CUDA_ECUDA; }
+
+/* Adds one to the process-wide kernel launch count (vox_cuda_launch_count). */
+void count_launch();
+
+namespace vox {
+
+// k-th index of 0..n-1 taken outward from c: c, c+1, c-1, c+2, ... then the
+// rest of the longer side.
+__device__ __forceinline__ uint32_t centre_out(uint32_t k, uint32_t c, uint32_t n)
+{
+    uint32_t m = min(c, n - 1 - c);
+    if (k <= 2 * m) return (k & 1) ? c + (k + 1) / 2 : c - k / 2;
+    uint32_t j = k - (2 * m + 1);
+    return (c < n - 1 - c) ? c + m + 1 + j : c - m - 1 - j;
+}
+
+// Block tiles are issued rows-first outward from the tile where the tree's
+// centre projects: the rays that walk the tree longest start first, so the
+// frame does not wait on late starters.  Every tile is drawn exactly once.
+struct TileOrder {
+    uint32_t nbx, nby, cbx, cby;
+};
+
+}  // namespace vox
+
+constexpr int TILE_W = 16, TILE_H = 8;   // render block tile; warps are 8x4
+
+/* Order in which the render kernel issues its block tiles for this camera. */
+vox::TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
+                          uint32_t tile_w = TILE_W, uint32_t tile_h = TILE_H);
+
+#endif

@@ -22,6 +22,7 @@
 #include <new>
 
 #include "flatten.h"
+#include "internal.h"
 #include "pool_layout.h"
 #include "traverse.cuh"
 #include "../../include/voxtrees_cuda.h"
@@ -29,38 +30,14 @@
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
 using vox::Counts;
+using vox::TileOrder;
+using vox::centre_out;
 using vox::DevTree;
 using vox::RayHit;
-
-struct vox_cuda_tree {
-    int device;
-    float bbox[6];           // root bounding box (for scheduling only)
-    uint4 *d_pool;
-    uint32_t *d_rec_of_id;
-    uint32_t *d_status;      // bit 0: a traversal stack overflowed
-    DevTree dev;
-    int cap_class;           // 0: 28 stack entries, 1: 64, 2: 256
-    FlatTree flat;           // host copy: pre-order table and maps
-    size_t pool_bytes;
-};
 
 namespace {
 
 std::atomic<uint64_t> g_launches{0};
-
-// Ray stacks hold at most 3 pending children per inner level on the path.
-constexpr int CAP0 = 28, CAP1 = 64, CAP2 = 256;
-
-int cap_class_for_depth(uint64_t depth)
-{
-    uint64_t need = 3 * depth + 1;
-    if (need <= (uint64_t)CAP0) return 0;
-    if (need <= (uint64_t)CAP1) return 1;
-    if (need <= (uint64_t)CAP2) return 2;
-    return -1;
-}
-
-inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 __device__ __forceinline__ void add_counts(unsigned long long *counts, const Counts &c)
 {
@@ -131,25 +108,6 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
     }
     if (COUNT) add_counts(counts, c);
 }
-
-constexpr int TILE_W = 16, TILE_H = 8;   // block tile; warps are 8x4
-
-// k-th index of 0..n-1 taken outward from c: c, c+1, c-1, c+2, ... then the
-// rest of the longer side.
-__device__ __forceinline__ uint32_t centre_out(uint32_t k, uint32_t c, uint32_t n)
-{
-    uint32_t m = min(c, n - 1 - c);
-    if (k <= 2 * m) return (k & 1) ? c + (k + 1) / 2 : c - k / 2;
-    uint32_t j = k - (2 * m + 1);
-    return (c < n - 1 - c) ? c + m + 1 + j : c - m - 1 - j;
-}
-
-// Block tiles are issued rows-first outward from the tile where the tree's
-// centre projects: the rays that walk the tree longest start first, so the
-// frame does not wait on late starters.  Every tile is drawn exactly once.
-struct TileOrder {
-    uint32_t nbx, nby, cbx, cby;
-};
 
 template <int CAP, bool COUNT>
 __global__ void __launch_bounds__(128) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
@@ -303,7 +261,7 @@ cudaError_t launch_rays(const vox_cuda_tree *t, const float *o, const float *d, 
     case 1: ray_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
     default: ray_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
     }
-    g_launches++;
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -318,46 +276,8 @@ cudaError_t launch_balls(const vox_cuda_tree *t, const float *c, const float *r,
     case 1: ball_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
     default: ball_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
     }
-    g_launches++;
+    count_launch();
     return cudaGetLastError();
-}
-
-// Screen position of the centre of the tree's bounding box (inverse of
-// screen2world), clamped to the frame; the frame centre when it lies behind
-// the camera.  Only used to order the tiles.
-TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h)
-{
-    TileOrder o;
-    o.nbx = (w + TILE_W - 1) / TILE_W;
-    o.nby = (h + TILE_H - 1) / TILE_H;
-    double v[3], c[3];
-    for (int i = 0; i < 3; i++) v[i] = 0.5 * ((double)t->bbox[i] + t->bbox[3 + i]) - cam.position[i];
-    double shift = 0.0;
-    if (cam.kind == VOX_CUDA_CAMERA_DOOM) {
-        c[0] = v[0] * cam.cosphi + v[1] * cam.sinphi;
-        c[1] = v[1] * cam.cosphi - v[0] * cam.sinphi;
-        c[2] = v[2];
-        shift = cam.k;
-    } else {
-        // rotate by the conjugate quaternion: v + w t + u x t, t = 2 (u x v), u = -q.xyz
-        double qw = cam.rotation[0], ux = -cam.rotation[1], uy = -cam.rotation[2], uz = -cam.rotation[3];
-        double tx = 2 * (uy * v[2] - uz * v[1]), ty = 2 * (uz * v[0] - ux * v[2]), tz = 2 * (ux * v[1] - uy * v[0]);
-        c[0] = v[0] + qw * tx + (uy * tz - uz * ty);
-        c[1] = v[1] + qw * ty + (uz * tx - ux * tz);
-        c[2] = v[2] + qw * tz + (ux * ty - uy * tx);
-    }
-    double sx = 0.5 * w, sy = 0.5 * h;
-    if (c[1] > 1e-6 && cam.mul != 0.0f) {
-        sx = (c[0] / c[1] + cam.xsub) / cam.mul;
-        sy = (cam.ysub + shift - c[2] / c[1]) / cam.mul;
-    }
-    if (!(sx >= 0)) sx = 0;               // also catches NaN
-    if (!(sy >= 0)) sy = 0;
-    if (sx > w - 1) sx = w - 1;
-    if (sy > h - 1) sy = h - 1;
-    o.cbx = (uint32_t)sx / TILE_W;
-    o.cby = (uint32_t)sy / TILE_H;
-    return o;
 }
 
 template <bool COUNT>
@@ -371,7 +291,7 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
     case 1: render_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
     default: render_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
     }
-    g_launches++;
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -385,11 +305,10 @@ cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera 
     case 1: render_squares_kernel<CAP1><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
     default: render_squares_kernel<CAP2><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
     }
-    g_launches++;
+    count_launch();
     return cudaGetLastError();
 }
 
-int status_of(cudaError_t e) { return e == cudaSuccess ? VOX_CUDA_OK : VOX_CUDA_ECUDA; }
 
 // Reads and clears the tree's overflow flag after a synchronous call.
 int check_tree_status(const vox_cuda_tree *t, cudaStream_t s)
@@ -417,6 +336,48 @@ struct Scratch {
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
+
+void count_launch() { g_launches++; }
+
+// Screen position of the centre of the tree's bounding box (inverse of
+// screen2world), clamped to the frame; the frame centre when it lies behind
+// the camera.  Only used to order the tiles.
+TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
+                     uint32_t tile_w, uint32_t tile_h)
+{
+    TileOrder o;
+    o.nbx = (w + tile_w - 1) / tile_w;
+    o.nby = (h + tile_h - 1) / tile_h;
+    double v[3], c[3];
+    for (int i = 0; i < 3; i++) v[i] = 0.5 * ((double)t->bbox[i] + t->bbox[3 + i]) - cam.position[i];
+    double shift = 0.0;
+    if (cam.kind == VOX_CUDA_CAMERA_DOOM) {
+        c[0] = v[0] * cam.cosphi + v[1] * cam.sinphi;
+        c[1] = v[1] * cam.cosphi - v[0] * cam.sinphi;
+        c[2] = v[2];
+        shift = cam.k;
+    } else {
+        // rotate by the conjugate quaternion: v + w t + u x t, t = 2 (u x v), u = -q.xyz
+        double qw = cam.rotation[0], ux = -cam.rotation[1], uy = -cam.rotation[2], uz = -cam.rotation[3];
+        double tx = 2 * (uy * v[2] - uz * v[1]), ty = 2 * (uz * v[0] - ux * v[2]), tz = 2 * (ux * v[1] - uy * v[0]);
+        c[0] = v[0] + qw * tx + (uy * tz - uz * ty);
+        c[1] = v[1] + qw * ty + (uz * tx - ux * tz);
+        c[2] = v[2] + qw * tz + (ux * ty - uy * tx);
+    }
+    double sx = 0.5 * w, sy = 0.5 * h;
+    if (c[1] > 1e-6 && cam.mul != 0.0f) {
+        sx = (c[0] / c[1] + cam.xsub) / cam.mul;
+        sy = (cam.ysub + shift - c[2] / c[1]) / cam.mul;
+    }
+    if (!(sx >= 0)) sx = 0;               // also catches NaN
+    if (!(sy >= 0)) sy = 0;
+    if (sx > w - 1) sx = w - 1;
+    if (sy > h - 1) sy = h - 1;
+    o.cbx = (uint32_t)sx / tile_w;
+    o.cby = (uint32_t)sy / tile_h;
+    return o;
+}
+
 
 // ======================================================================== API
 

@@ -131,3 +131,29 @@ def balls(n: int, lo: float, hi: float, rmin: float, rmax: float, seed: int):
     centres = (lo + (hi - lo) * u[: 3 * n]).reshape(n, 3).astype(np.float32)
     radii = (rmin + (rmax - rmin) * u[3 * n:]).astype(np.float32)
     return np.ascontiguousarray(centres), np.ascontiguousarray(radii)
+
+
+RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+BATCH_TREES = [(64, 10, 0.05), (128, 11, 0.10), (256, 12, 0.15), (512, 13, 0.20)]
+
+
+def batch_poses(n: int = 64, ntrees: int = 4, seed: int = 14):
+    """n frame requests of the mixed-camera load: (tree index, (w, h),
+    azimuth, elevation) with resolution and tree uniform, azimuth U[0, 2pi),
+    elevation U[5, 45] degrees."""
+    u = uniform01(seed, 4 * n).reshape(n, 4)
+    out = []
+    for i in range(n):
+        ti = min(int(u[i, 0] * ntrees), ntrees - 1)
+        ri = min(int(u[i, 1] * len(RESOLUTIONS)), len(RESOLUTIONS) - 1)
+        az = 2.0 * math.pi * u[i, 2]
+        el = 5.0 + 40.0 * u[i, 3]
+        out.append((ti, RESOLUTIONS[ri], az, el))
+    return out
+
+
+def pose_position(centre, radius: float, az: float, el_deg: float) -> np.ndarray:
+    el = math.radians(el_deg)
+    c = np.asarray(centre, dtype=np.float64)
+    return (c + radius * np.array([math.cos(el) * math.cos(az), math.cos(el) * math.sin(az),
+                                   math.sin(el)])).astype(np.float32)
