@@ -49,6 +49,7 @@ extern "C" {
 #define VOX_CUDA_EBUDGET    -8   /* admission budget exceeded                      */
 #define VOX_CUDA_ETIMEOUT   -9   /* a bounded wait gave up                         */
 #define VOX_CUDA_ENODEV    -10   /* no usable CUDA device                          */
+#define VOX_CUDA_ECAPACITY -11   /* request larger than a fixed-capacity entry point */
 
 #define VOX_CUDA_MISS       0xFFFFFFFFu
 #define VOX_CUDA_SLOT_DENSE 0xFFu
@@ -213,6 +214,21 @@ int vox_cuda_batch_set_config(vox_cuda_batch *batch, const vox_cuda_batch_config
 int vox_cuda_batch_autotune(vox_cuda_batch *batch, void *stream, uint32_t reps,
                             vox_cuda_batch_config *chosen, float *best_ms);
 int vox_cuda_batch_free(vox_cuda_batch *batch);
+
+/* Draw njobs frames (1..VOX_CUDA_NOALLOC_MAX_JOBS) like a batch, in one
+ * persistent-kernel launch on `stream`, without allocating any memory.  No
+ * counterpart in the reference: it is for callers that cannot allocate when
+ * they render -- loops that must not stall on cudaMalloc, hosts that own all
+ * GPU memory through their own budget, code running with the device nearly
+ * full.  Its scratch (job table and work-queue head) is a fixed 16 KiB array
+ * in the library's device image, kept by every GPU that loads the library
+ * until exit.  Frames are bit-identical to vox_cuda_render_device's.
+ * More than VOX_CUDA_NOALLOC_MAX_JOBS jobs: VOX_CUDA_ECAPACITY.  All calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * ordered (same stream, or synchronised).  The first call on a device looks
+ * up the array's address; make it before starting any stream capture. */
+#define VOX_CUDA_NOALLOC_MAX_JOBS 64
+int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njobs, void *stream);
 
 /* Library version and the number of kernel launches made so far by this
  * process (all entry points); used to report launch counts. */

@@ -19,7 +19,7 @@ CAMERA_DOOM = 1
 
 ERRORS = {
     0: "ok", -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EDEPTH", -5: "ESTACK",
-    -6: "ETOOBIG", -7: "EGEOMETRY", -8: "EBUDGET", -9: "ETIMEOUT", -10: "ENODEV",
+    -6: "ETOOBIG", -7: "EGEOMETRY", -8: "EBUDGET", -9: "ETIMEOUT", -10: "ENODEV", -11: "ECAPACITY",
 }
 
 
@@ -87,6 +87,7 @@ SIGNATURES = {
     "vox_cuda_batch_set_config": (C.c_int, [_vp, C.POINTER(BatchConfig)]),
     "vox_cuda_batch_autotune": (C.c_int, [_vp, _vp, _u32, C.POINTER(BatchConfig), C.POINTER(C.c_float)]),
     "vox_cuda_batch_free": (C.c_int, [_vp]),
+    "vox_cuda_render_frames_noalloc": (C.c_int, [C.POINTER(FrameJob), _u32, _vp]),
     "vox_cuda_render_counts_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp]),
     "vox_cuda_ray_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "vox_cuda_ball_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -381,4 +382,132 @@ EXPORT int vox_cuda_batch_free(vox_cuda_batch *b)
     release(b);
     delete b;
     return VOX_CUDA_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * Frames without any allocation.
+ *
+ * Some callers cannot allocate GPU memory at the moment they want a frame:
+ * a render loop that must never stall on cudaMalloc (it synchronises the
+ * device), a host application whose memory is handed out by its own budget
+ * and that forbids libraries from allocating behind its back, or code that
+ * runs when the device is nearly full and an allocation could fail.  For them
+ * vox_cuda_render_frames_noalloc draws a batch of frames with the persistent
+ * kernel above while allocating nothing, neither on the device nor on the
+ * host: the kernel's scratch -- the job table and the work-queue head -- lives
+ * in a fixed array in the library's device image, and the caller supplies
+ * the trees, textures and frames as for vox_cuda_batch_create.
+ *
+ * Limits and sharing.  The array holds at most VOX_CUDA_NOALLOC_MAX_JOBS job
+ * entries plus the queue head (16 KiB; every GPU that loads the library keeps
+ * it until the process exits).  All calls on a device use the same array and
+ * it keeps the previous call's contents, so each call rewrites the job table
+ * and zeroes the queue head on its stream before the kernel runs; two calls
+ * whose work overlaps on the GPU (different streams, or different host
+ * threads without ordering) race on the array and give wrong frames.
+ *
+ * Set-up.  Host code cannot use the array's name as a device address.  The
+ * first call on each device looks its address up with cudaGetSymbolAddress
+ * (with that device current) and caches it; make that first call before any
+ * stream capture is started on the device.
+ * ------------------------------------------------------------------------- */
+
+namespace {
+
+constexpr size_t NOALLOC_HEAD_BYTES = 256;
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD_BYTES + VOX_CUDA_NOALLOC_MAX_JOBS * sizeof(BatchJobDev);
+static_assert(NOALLOC_BYTES <= 16384, "no-allocation scratch must stay within 16 KiB");
+
+// [0, 4): work-queue head; [256, ...): job table.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES];
+std::atomic<int> g_noalloc_ready[NOALLOC_MAX_DEVICES];
+
+// Device address of the scratch array on `dev`, looked up once per device.
+int noalloc_scratch(int dev, unsigned char **out)
+{
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return VOX_CUDA_ENODEV;
+    if (g_noalloc_ready[dev].load(std::memory_order_acquire) == 0) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return VOX_CUDA_ECUDA;
+        g_noalloc_addr[dev] = p;
+        g_noalloc_ready[dev].store(1, std::memory_order_release);
+    }
+    *out = static_cast<unsigned char *>(g_noalloc_addr[dev]);
+    return VOX_CUDA_OK;
+}
+
+template <int CAP>
+void launch_noalloc(const BatchJobDev *table, uint32_t njobs, uint32_t total, uint32_t *head, int nsm,
+                    cudaStream_t s)
+{
+    batch_kernel<CAP, 8, 4><<<nsm * 8, 128, 0, s>>>(table, njobs, total, 2, head);
+}
+
+}  // namespace
+
+EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njobs, void *stream)
+{
+    if (!jobs || njobs == 0) return VOX_CUDA_EINVAL;
+    if (njobs > VOX_CUDA_NOALLOC_MAX_JOBS) return VOX_CUDA_ECAPACITY;
+    int cap = 0;
+    for (uint32_t i = 0; i < njobs; i++) {
+        const vox_cuda_frame_job &j = jobs[i];
+        if (!j.tree || !j.texture || !j.argb) return VOX_CUDA_EINVAL;
+        if (j.w == 0 || j.h == 0 || (j.w & 0xF) || (j.h & 0x3)) return VOX_CUDA_EGEOMETRY;
+        if (j.camera.kind != VOX_CUDA_CAMERA_SIMPLE && j.camera.kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+        cap = std::max(cap, j.tree->cap_class);
+    }
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return VOX_CUDA_ENODEV;
+    unsigned char *scratch = nullptr;
+    int rc = noalloc_scratch(dev, &scratch);
+    if (rc) return rc;
+
+    // Largest frames first (insertion sort on a fixed array: no allocation).
+    uint32_t order[VOX_CUDA_NOALLOC_MAX_JOBS];
+    for (uint32_t i = 0; i < njobs; i++) {
+        uint64_t px = (uint64_t)jobs[i].w * jobs[i].h;
+        uint32_t k = i;
+        while (k > 0 && (uint64_t)jobs[order[k - 1]].w * jobs[order[k - 1]].h < px) {
+            order[k] = order[k - 1];
+            k--;
+        }
+        order[k] = i;
+    }
+    BatchJobDev table[VOX_CUDA_NOALLOC_MAX_JOBS];
+    uint32_t base = 0;
+    for (uint32_t q = 0; q < njobs; q++) {
+        const vox_cuda_frame_job &j = jobs[order[q]];
+        BatchJobDev &d = table[q];
+        std::memset(&d, 0, sizeof d);
+        d.tree = j.tree->dev;
+        d.cam = j.camera;
+        d.tex = j.texture;
+        d.argb = j.argb;
+        d.status = j.tree->d_status;
+        d.w = j.w;
+        d.h = j.h;
+        vox::TileOrder o = tile_order(j.tree, j.camera, j.w, j.h, 8, 4);
+        d.ntx = o.nbx; d.nty = o.nby; d.ctx = o.cbx; d.cty = o.cby;
+        d.tile_base = base;
+        base += o.nbx * o.nby;
+    }
+    cudaStream_t s = as_stream(stream);
+    uint32_t *head = reinterpret_cast<uint32_t *>(scratch);
+    BatchJobDev *dtable = reinterpret_cast<BatchJobDev *>(scratch + NOALLOC_HEAD_BYTES);
+    if (cudaMemcpyAsync(dtable, table, njobs * sizeof(BatchJobDev), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(head, 0, sizeof(uint32_t), s) != cudaSuccess)
+        return VOX_CUDA_ECUDA;
+    switch (cap) {
+    case 0: launch_noalloc<CAP0>(dtable, njobs, base, head, nsm, s); break;
+    case 1: launch_noalloc<CAP1>(dtable, njobs, base, head, nsm, s); break;
+    default: launch_noalloc<CAP2>(dtable, njobs, base, head, nsm, s); break;
+    }
+    count_launch();
+    return status_of(cudaGetLastError());
 }

@@ -395,6 +395,7 @@ EXPORT const char *vox_cuda_strerror(int code)
     case VOX_CUDA_EBUDGET: return "admission budget exceeded";
     case VOX_CUDA_ETIMEOUT: return "bounded wait timed out";
     case VOX_CUDA_ENODEV: return "no CUDA device";
+    case VOX_CUDA_ECAPACITY: return "request exceeds the entry point's fixed capacity";
     default: return "unknown error";
     }
 }
