@@ -89,6 +89,20 @@ const uint32_t *vox_context_pixels(const struct vox_rnd_ctx *ctx);
 /* VOX_CUDA_OK or the error of the last vox_render / vox_redraw. */
 int vox_context_status(const struct vox_rnd_ctx *ctx);
 
+/* Collision detector (src/voxrnd/cd.h:25-60): keeps an attached camera out
+ * of the context's scene.  Allocated with malloc; release with free(). */
+struct vox_cd;
+/* cd.h:25 */
+struct vox_cd *vox_make_cd(void);
+/* cd.h:32: camera treated as a ball of `radius` */
+void vox_cd_attach_camera(struct vox_cd *cd, struct vox_camera *camera, float radius);
+/* cd.h:39 */
+void vox_cd_attach_context(struct vox_cd *cd, struct vox_rnd_ctx *ctx);
+/* cd.h:47: undo the camera's last move if it entered the scene (GPU ball query) */
+void vox_cd_collide(struct vox_cd *cd);
+/* cd.h:60: no effect, as in the reference */
+void vox_cd_gravity(struct vox_cd *cd, const vox_dot gravity);
+
 #ifdef __cplusplus
 }
 #endif

@@ -316,3 +316,33 @@ def test_errors_and_empty_tree():
     assert e.value.code == -7
     img = dt.render(cam, 64, 32, np.zeros(32768, np.uint8))
     assert (img == 0).all()
+
+
+def test_collision_detector_keeps_camera_out_of_the_scene(tree256):
+    """cd.c:34-55: a move into the scene is undone, a move through free space
+    is kept; the decision is the reference ball query's."""
+    import ctypes as C
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    ht, dt = tree256
+    L = vg().lib()
+    ctx = L.vox_make_context_headless(64, 32)
+    cam = HostCamera(0)
+    L.vox_context_set_camera(ctx, cam.obj)
+    L.vox_context_set_scene(ctx, ht.ptr)
+    cd = L.vox_make_cd()
+    start = np.array([-40.0, -40.0, -40.0], np.float32)
+    cam.set_position(start)
+    L.vox_cd_attach_camera(cd, cam.obj, C.c_float(3.0))
+    L.vox_cd_attach_context(cd, ctx)
+    vox = wl.voxels_from_mask(wl.noise_volume(256, 2, 0.08))
+    inside = vox[len(vox) // 2] + 0.5                      # centre of a solid voxel
+    for target in (inside, np.array([-60.0, -50.0, -45.0], np.float32), inside + 0.25):
+        before = cam.position().copy()
+        cam.set_position(target)
+        L.vox_cd_collide(cd)
+        hit, _ = orc.ball_batch(ht.ptr, np.asarray([target], np.float32), np.asarray([3.0], np.float32))
+        expect = before if hit[0] else np.asarray(target, np.float32)
+        assert np.array_equal(cam.position(), expect)
+    C.CDLL(None).free(C.c_void_p(cd))
+    L.vox_destroy_context(ctx)

@@ -116,6 +116,11 @@ SIGNATURES = {
     "vox_redraw": (None, [_vp]),
     "vox_context_pixels": (_vp, [_vp]),
     "vox_context_status": (C.c_int, [_vp]),
+    "vox_make_cd": (_vp, []),
+    "vox_cd_attach_camera": (None, [_vp, _vp, _f]),
+    "vox_cd_attach_context": (None, [_vp, _vp]),
+    "vox_cd_collide": (None, [_vp]),
+    "vox_cd_gravity": (None, [_vp, _vp]),
 }
 
 

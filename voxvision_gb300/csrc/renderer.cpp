@@ -170,3 +170,50 @@ EXPORT void vox_redraw(struct vox_rnd_ctx *ctx)
 EXPORT const uint32_t *vox_context_pixels(const struct vox_rnd_ctx *ctx) { return ctx->pixels; }
 
 EXPORT int vox_context_status(const struct vox_rnd_ctx *ctx) { return ctx->status; }
+
+/* ---- collision detector (src/voxrnd/cd.c) ---- */
+
+struct vox_cd {                 /* cd.c:6-11 */
+    struct vox_camera *camera;
+    struct vox_rnd_ctx *ctx;
+    vox_dot last_position;
+    float camera_radius;
+};
+
+EXPORT struct vox_cd *vox_make_cd(void)
+{
+    struct vox_cd *cd = static_cast<struct vox_cd *>(std::calloc(1, sizeof(struct vox_cd)));
+    return cd;
+}
+
+EXPORT void vox_cd_attach_camera(struct vox_cd *cd, struct vox_camera *camera, float radius)
+{
+    cd->camera = camera;
+    cd->camera_radius = radius;
+    camera->iface->get_position(camera, cd->last_position);
+}
+
+EXPORT void vox_cd_attach_context(struct vox_cd *cd, struct vox_rnd_ctx *ctx) { cd->ctx = ctx; }
+
+/* cd.c:29-32: a stub in the reference as well. */
+EXPORT void vox_cd_gravity(struct vox_cd *cd, const vox_dot gravity) {}
+
+/* cd.c:34-55: if the camera moved into the scene (a ball of the camera's
+ * radius meets a voxel), put it back where it was; otherwise remember the
+ * new position.  The ball query runs on the GPU against the context's tree. */
+EXPORT void vox_cd_collide(struct vox_cd *cd)
+{
+    struct vox_camera *camera = cd->camera;
+    struct vox_rnd_ctx *ctx = cd->ctx;
+    if (!camera || !ctx) return;
+    vox_dot position;
+    camera->iface->get_position(camera, position);
+    if (std::memcmp(position, cd->last_position, sizeof(vox_dot)) == 0) return;
+    if (!ctx->tree && vox_cuda_tree_upload(ctx->scene, &ctx->tree) != VOX_CUDA_OK) return;
+    uint8_t hit = 0;
+    if (vox_cuda_ball_batch(ctx->tree, position, &cd->camera_radius, 1, &hit, ctx->stream) != VOX_CUDA_OK) return;
+    if (hit)
+        camera->iface->set_property_dot(camera, "position", cd->last_position);
+    else
+        std::memcpy(cd->last_position, position, sizeof(vox_dot));
+}
