@@ -249,7 +249,115 @@ def measure_incoherent(torch, vg, dt, flush):
                       "r U[0.5,8] seed 4"}
 
 
-def measure_batched(torch, vg, flush, tex_dev):
+def build_batch_trees(vg):
+    from voxvision_gb300 import workloads as wl
+    trees = []
+    for n, seed, solid in wl.BATCH_TREES:
+        ht = vg.HostTree.from_voxels(wl.voxels_from_mask(wl.noise_volume(n, seed, solid)))
+        trees.append((n, ht, vg.DeviceTree(ht.ptr)))
+    return trees
+
+
+def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 20000), duration=0.4, seed=15):
+    """Served load: 256 clients with Poisson arrivals at the aggregate rate;
+    70% frames (resolution uniform over 320x240..3840x2160, tree uniform,
+    random orbit pose), 30% batches of 1k-64k ball queries; 4 resident trees
+    under a 40 GB budget.  Latency = submission to result in host memory."""
+    import threading
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 64 << 30, 4096, 256, 4, 8))
+    ids = [srv.add_tree(t[2]) for t in trees]
+    rng = np.random.default_rng(seed)
+    ball_pool = []
+    for i in range(16):
+        k = int(rng.integers(1000, 64001))
+        side = trees[i % len(trees)][0]
+        ball_pool.append((i % len(trees), wl.balls(k, 0.0, float(side), 0.5, 8.0, 100 + i)))
+
+    def make_requests(n):
+        reqs = []
+        for i in range(n):
+            ti = int(rng.integers(len(trees)))
+            if rng.random() < 0.7:
+                w, h = wl.RESOLUTIONS[int(rng.integers(len(wl.RESOLUTIONS)))]
+                side = trees[ti][0]
+                cam = HostCamera(0)
+                cam.set_window_size(w, h)
+                cam.set_position(wl.pose_position((side / 2,) * 3, 1.5 * side * 3 ** 0.5,
+                                                  rng.uniform(0, 2 * np.pi), rng.uniform(5, 45)))
+                cam.look_at((side / 2,) * 3)
+                reqs.append(("frame", ti, cam.gpu_struct(), w, h))
+            else:
+                bi = int(rng.integers(len(ball_pool)))
+                reqs.append(("balls",) + (ball_pool[bi][0],) + ball_pool[bi][1])
+        return reqs
+
+    out = {}
+    for rate in rates:
+        n = max(200, int(rate * duration))
+        reqs = make_requests(n)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        tickets = [None] * n
+        times = [None] * n
+        ready = threading.Semaphore(0)
+
+        def collect():
+            for i in range(n):
+                ready.acquire()
+                rc = srv.wait(tickets[i], 120000)
+                try:
+                    _, t = srv.result(tickets[i], copy=False)
+                    srv.release(tickets[i])
+                except vg.VoxCudaError as e:
+                    rc, t = e.code, (0, 0, 0)
+                times[i] = (rc,) + t
+
+        th = threading.Thread(target=collect)
+        th.start()
+        t0 = time.perf_counter()
+        for i, q in enumerate(reqs):
+            while time.perf_counter() - t0 < arrivals[i]:
+                pass
+            if q[0] == "frame":
+                tickets[i] = srv.submit_frame(ids[q[1]], q[2], q[3], q[4])
+            else:
+                tickets[i] = srv.submit_balls(ids[q[1]], q[2], q[3])
+            ready.release()
+        th.join()
+        ok = np.array([t[0] == 0 for t in times])
+        lat = np.array([(t[3] - t[1]) * 1e-6 for t in times])
+        is_frame = np.array([q[0] == "frame" for q in reqs]) & ok
+        is_ball = np.array([q[0] == "balls" for q in reqs]) & ok
+        span = (max(t[3] for t in times if t[0] == 0) - min(t[1] for t in times if t[0] == 0)) * 1e-9
+        rays = sum(q[3] * q[4] for q, t in zip(reqs, times) if q[0] == "frame" and t[0] == 0)
+        out[str(rate)] = {"requests": n, "errors": int(sum(1 for t in times if t[0] != 0)),
+                          "frame_p50_ms": float(np.percentile(lat[is_frame], 50)),
+                          "frame_p99_ms": float(np.percentile(lat[is_frame], 99)),
+                          "ball_p50_ms": float(np.percentile(lat[is_ball], 50)) if is_ball.any() else None,
+                          "ball_p99_ms": float(np.percentile(lat[is_ball], 99)) if is_ball.any() else None,
+                          "error_codes": sorted({int(t[0]) for t in times if t[0] != 0}),
+                          "mrays_s": rays / span / 1e6, "offered_hz": rate,
+                          "achieved_hz": n / span}
+    stats = srv.stats()
+    srv.close()
+    # the plain path: the same kind of frames, one synchronous call at a time
+    reqs = [q for q in make_requests(300) if q[0] == "frame"][:150]
+    lat = []
+    t_all = time.perf_counter()
+    for q in reqs:
+        t1 = time.perf_counter()
+        trees[q[1]][2].render(q[2], q[3], q[4], tex)
+        lat.append((time.perf_counter() - t1) * 1e3)
+    span = time.perf_counter() - t_all
+    plain = {"frame_p50_ms": float(np.percentile(lat, 50)), "frame_p99_ms": float(np.percentile(lat, 99)),
+             "mrays_s": sum(q[3] * q[4] for q in reqs) / span / 1e6, "frames": len(reqs),
+             "call": "vox_cuda_render, one frame at a time"}
+    return {"rates": out, "plain": plain, "budget_gb": 40, "clients": 256, "peak_bytes": stats["peak_bytes"],
+            "launches": stats["launches"]}
+
+
+def measure_batched(torch, vg, flush, tex_dev, trees=None):
     """Mixed-camera load: 64 frames, resolutions uniform over 320x240..3840x2160,
     trees uniform over the 64^3..512^3 noise volumes, random orbit poses; one
     persistent kernel replayed from a CUDA graph (autotuned) against 64 plain
@@ -257,10 +365,8 @@ def measure_batched(torch, vg, flush, tex_dev):
     from voxvision_gb300 import workloads as wl
     from voxvision_gb300.cameras import HostCamera
     sp = torch.cuda.current_stream().cuda_stream
-    trees = []
-    for n, seed, solid in wl.BATCH_TREES:
-        ht = vg.HostTree.from_voxels(wl.voxels_from_mask(wl.noise_volume(n, seed, solid)))
-        trees.append((n, ht, vg.DeviceTree(ht.ptr)))
+    if trees is None:
+        trees = build_batch_trees(vg)
     jobs = []
     for ti, (w, h), az, el in wl.batch_poses(64, len(trees), 14):
         n, _, dt = trees[ti]
@@ -437,7 +543,9 @@ def run_ours(args):
             "gpu_launches": int(launches), "clocks": clk}
     if not args.no_extras:
         line["incoherent"] = measure_incoherent(torch, vg, dt, flush)
-        line["batched"] = measure_batched(torch, vg, flush, d_tex)
+        btrees = build_batch_trees(vg)
+        line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
+        line["served"] = measure_served(vg, btrees, tex)
     if not args.no_cpu_baseline and world >= 1:
         line["cpu_baseline"] = cpu_baseline_sample(ht.ptr, states, tex)
     print(json.dumps(line), flush=True)

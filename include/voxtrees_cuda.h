@@ -230,6 +230,57 @@ int vox_cuda_batch_free(vox_cuda_batch *batch);
 #define VOX_CUDA_NOALLOC_MAX_JOBS 64
 int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njobs, void *stream);
 
+/* ---- Request server --------------------------------------------------------
+ * Frame and ball-collision requests from any number of client threads over
+ * resident trees, admitted by a device-memory budget and batched
+ * continuously: everything admitted since the previous launch goes out in
+ * the next one, on the next of several streams, so requests that arrive
+ * while others run overlap with them on the device.  Each result equals
+ * the plain entry point's for the same request alone.
+ * Replaces: applications calling vox_render / vox_tree_ball_collidep from
+ * many threads (renderer.h:208 is callable from any thread). */
+typedef struct {
+    uint64_t budget_bytes;       /* device bytes for resident trees + request buffers */
+    uint64_t host_budget_bytes;  /* pinned host bytes for results and staged inputs   */
+    uint32_t max_inflight;   /* requests admitted at once                         */
+    uint32_t max_batch;      /* requests per launch (1..1024)                     */
+    uint32_t streams;        /* launch streams (1..32)                            */
+    uint32_t max_launches;   /* launches in flight at once                        */
+} vox_cuda_server_config;
+
+typedef struct {
+    uint64_t submitted, completed, rejected, launches;
+    uint64_t bytes_in_use, peak_bytes;
+    uint64_t pending, inflight;
+} vox_cuda_server_stats;
+
+typedef struct vox_cuda_server vox_cuda_server;
+
+/* config NULL = 40 GiB device budget, 16 GiB pinned host budget, 1024 in
+ * flight, 256 per launch, 4 streams, 8 launches in flight.  texture: host 32^3 bytes used for every frame. */
+int vox_cuda_server_create(const vox_cuda_server_config *config, const uint8_t *texture,
+                           vox_cuda_server **out);
+/* Make a tree available to requests (charged to the budget while the server
+ * lives; the tree must outlive the server). */
+int vox_cuda_server_add_tree(vox_cuda_server *srv, const vox_cuda_tree *tree, uint32_t *tree_id);
+/* Queue a BEST frame / a ball batch (inputs are copied); the ticket names the
+ * request.  VOX_CUDA_EBUDGET if it could never fit the budget. */
+int vox_cuda_server_submit_frame(vox_cuda_server *srv, uint32_t tree_id, const vox_cuda_camera *camera,
+                                 uint32_t w, uint32_t h, uint64_t *ticket);
+int vox_cuda_server_submit_balls(vox_cuda_server *srv, uint32_t tree_id, const float *centres,
+                                 const float *radii, uint32_t n, uint64_t *ticket);
+/* Wait up to timeout_ms for a request: its status, or VOX_CUDA_ETIMEOUT. */
+int vox_cuda_server_wait(vox_cuda_server *srv, uint64_t ticket, uint32_t timeout_ms);
+/* A finished request's result (w*h ARGB pixels, or n hit bytes) in server
+ * memory, valid until vox_cuda_server_release; times_ns (may be NULL) gets
+ * submission, launch and completion times (steady clock, ns). */
+int vox_cuda_server_result(vox_cuda_server *srv, uint64_t ticket, const void **data, size_t *bytes,
+                           uint64_t *times_ns);
+int vox_cuda_server_release(vox_cuda_server *srv, uint64_t ticket);
+int vox_cuda_server_get_stats(vox_cuda_server *srv, vox_cuda_server_stats *stats);
+/* Finish all queued requests, then stop. */
+int vox_cuda_server_destroy(vox_cuda_server *srv);
+
 /* Library version and the number of kernel launches made so far by this
  * process (all entry points); used to report launch counts. */
 const char *vox_cuda_version(void);

@@ -1,0 +1,135 @@
+"""The request server: requests from several threads, admitted by a memory
+budget and batched continuously; every result equals the same request run
+alone through the plain entry points (frames pixel-exact, ball hits exact)."""
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def setup():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from voxvision_gb300.build import build
+    build()
+    import voxvision_gb300 as vg
+    from voxvision_gb300 import workloads as wl
+    vg.set_voxel_size((1, 1, 1))
+    hosts = [vg.HostTree.from_voxels(wl.voxels_from_mask(wl.blobs_volume(64, 20, 1, 0.20))),
+             vg.HostTree.from_voxels(wl.voxels_from_mask(wl.noise_volume(128, 8, 0.10)))]
+    trees = [vg.DeviceTree(h.ptr) for h in hosts]
+    tex = wl.texture32(7)
+    return vg, wl, hosts, trees, tex
+
+
+def _requests(wl, n, seed):
+    from voxvision_gb300.cameras import HostCamera
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        ti = int(rng.integers(2))
+        side = (64, 128)[ti]
+        if rng.random() < 0.7:
+            w, h = [(64, 32), (160, 120), (320, 240), (640, 480)][int(rng.integers(4))]
+            cam = HostCamera(int(rng.integers(2)))
+            cam.set_window_size(w, h)
+            cam.set_position(wl.pose_position((side / 2,) * 3, 1.5 * side * 3 ** 0.5,
+                                              rng.uniform(0, 2 * np.pi), rng.uniform(5, 45)))
+            cam.look_at((side / 2,) * 3)
+            out.append(("frame", ti, cam.gpu_struct(), w, h))
+        else:
+            k = int(rng.integers(1000, 20000))
+            c, r = wl.balls(k, 0.0, float(side), 0.5, 8.0, seed * 1000 + i)
+            out.append(("balls", ti, c, r))
+    return out
+
+
+def _alone(trees, tex, req):
+    if req[0] == "frame":
+        _, ti, cam, w, h = req
+        return trees[ti].render(cam, w, h, tex).ravel().view(np.uint8)
+    _, ti, c, r = req
+    return trees[ti].balls(c, r)
+
+
+def _run_mixed(vg, trees, tex, reqs, config, nthreads=4):
+    srv = vg.Server(tex, config)
+    ids = [srv.add_tree(t) for t in trees]
+    tickets = [None] * len(reqs)
+
+    def client(k):
+        for i in range(k, len(reqs), nthreads):
+            q = reqs[i]
+            if q[0] == "frame":
+                tickets[i] = srv.submit_frame(ids[q[1]], q[2], q[3], q[4])
+            else:
+                tickets[i] = srv.submit_balls(ids[q[1]], q[2], q[3])
+
+    th = [threading.Thread(target=client, args=(k,)) for k in range(nthreads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    results = []
+    for t in tickets:
+        assert srv.wait(t, 60000) == 0
+        arr, times = srv.result(t)
+        assert times[0] <= times[1] <= times[2]
+        results.append(arr)
+        srv.release(t)
+    stats = srv.stats()
+    srv.close()
+    return results, stats
+
+
+def test_mixed_requests_equal_requests_alone(setup):
+    vg, wl, hosts, trees, tex = setup
+    reqs = _requests(wl, 48, 1)
+    cfg = vg.ServerConfig(1 << 34, 1 << 32, 64, 16, 4, 8)
+    results, stats = _run_mixed(vg, trees, tex, reqs, cfg)
+    for q, got in zip(reqs, results):
+        assert np.array_equal(got, _alone(trees, tex, q)), q[0]
+    assert stats["completed"] == stats["submitted"] == len(reqs)
+    assert stats["launches"] >= 1
+
+
+def test_tight_budget_queues_but_stays_exact(setup):
+    """A budget that holds the trees plus about two 640x480 frames forces
+    admission to wait for memory; results are unchanged."""
+    vg, wl, hosts, trees, tex = setup
+    tree_bytes = sum(t.info()["device_bytes"] for t in trees)
+    reqs = _requests(wl, 24, 2)
+    cfg = vg.ServerConfig(tree_bytes + 2 * 640 * 480 * 4 + 4 * 20000 * 17, 1 << 30, 8, 4, 2, 2)
+    results, stats = _run_mixed(vg, trees, tex, reqs, cfg, nthreads=3)
+    for q, got in zip(reqs, results):
+        assert np.array_equal(got, _alone(trees, tex, q)), q[0]
+    assert stats["peak_bytes"] <= cfg.budget_bytes
+
+
+def test_budget_refusal_and_bounded_wait(setup):
+    vg, wl, hosts, trees, tex = setup
+    tree_bytes = sum(t.info()["device_bytes"] for t in trees)
+    srv = vg.Server(tex, vg.ServerConfig(tree_bytes + 320 * 240 * 4, 1 << 30, 4, 4, 1, 1))
+    ids = [srv.add_tree(t) for t in trees]
+    from voxvision_gb300.cameras import HostCamera
+    cam = HostCamera(0)
+    cam.set_window_size(640, 480)
+    cam.set_position((200, 0, 50))
+    cam.look_at((32, 32, 32))
+    with pytest.raises(vg.VoxCudaError) as e:         # can never fit
+        srv.submit_frame(ids[0], cam.gpu_struct(), 640, 480)
+    assert e.value.code == -8
+    cam.set_window_size(320, 240)
+    t1 = srv.submit_frame(ids[0], cam.gpu_struct(), 320, 240)
+    t2 = srv.submit_frame(ids[0], cam.gpu_struct(), 320, 240)   # waits for t1's memory
+    r2 = srv.wait(t2, 0)
+    assert r2 in (0, -9)                                # done already, or a bounded wait gave up
+    assert srv.wait(t1, 60000) == 0 and srv.wait(t2, 60000) == 0
+    a1, _ = srv.result(t1)
+    a2, _ = srv.result(t2)
+    assert np.array_equal(a1, a2)
+    srv.close()

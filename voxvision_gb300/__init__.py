@@ -14,9 +14,9 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, BatchConfig, CameraStruct,
-                   FrameJob, TreeInfo, VoxCudaError, available, check, lib)
+                   FrameJob, ServerConfig, ServerStats, TreeInfo, VoxCudaError, available, check, lib)
 
-__all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
+__all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Server", "ServerConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
            "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size"]
 
 
@@ -232,6 +232,73 @@ class FrameBatch:
     def close(self):
         if getattr(self, "h", None) and self.h.value:
             lib().vox_cuda_batch_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """vox_cuda_server: frame and ball requests from many threads, admitted by
+    a device-memory budget and batched continuously onto the GPU."""
+
+    def __init__(self, texture: np.ndarray, config: ServerConfig | None = None):
+        self._tex = np.ascontiguousarray(texture, dtype=np.uint8)
+        h = C.c_void_p()
+        check(lib().vox_cuda_server_create(C.byref(config) if config else None, _p(self._tex), C.byref(h)),
+              "vox_cuda_server_create")
+        self.h = h
+        self._trees = []
+
+    def add_tree(self, tree: "DeviceTree") -> int:
+        tid = C.c_uint32()
+        check(lib().vox_cuda_server_add_tree(self.h, tree.h, C.byref(tid)), "vox_cuda_server_add_tree")
+        self._trees.append(tree)
+        return int(tid.value)
+
+    def submit_frame(self, tree_id: int, cam: CameraStruct, w: int, h: int) -> int:
+        t = C.c_uint64()
+        check(lib().vox_cuda_server_submit_frame(self.h, tree_id, C.byref(cam), w, h, C.byref(t)),
+              "vox_cuda_server_submit_frame")
+        return int(t.value)
+
+    def submit_balls(self, tree_id: int, centres: np.ndarray, radii: np.ndarray) -> int:
+        c = np.ascontiguousarray(centres, dtype=np.float32)
+        r = np.ascontiguousarray(radii, dtype=np.float32)
+        t = C.c_uint64()
+        check(lib().vox_cuda_server_submit_balls(self.h, tree_id, _p(c), _p(r), r.shape[0], C.byref(t)),
+              "vox_cuda_server_submit_balls")
+        return int(t.value)
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> int:
+        return int(lib().vox_cuda_server_wait(self.h, ticket, timeout_ms))
+
+    def result(self, ticket: int, copy: bool = True):
+        """(array of the result, (t_submit, t_launch, t_done) ns)."""
+        data = C.c_void_p()
+        nbytes = C.c_size_t()
+        times = (C.c_uint64 * 3)()
+        check(lib().vox_cuda_server_result(self.h, ticket, C.byref(data), C.byref(nbytes), times),
+              "vox_cuda_server_result")
+        arr = None
+        if copy:
+            arr = np.ctypeslib.as_array((C.c_uint8 * nbytes.value).from_address(data.value)).copy()
+        return arr, tuple(int(x) for x in times)
+
+    def release(self, ticket: int):
+        check(lib().vox_cuda_server_release(self.h, ticket), "vox_cuda_server_release")
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(lib().vox_cuda_server_get_stats(self.h, C.byref(s)), "vox_cuda_server_get_stats")
+        return {k: int(getattr(s, k)) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib().vox_cuda_server_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

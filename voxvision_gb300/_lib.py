@@ -56,6 +56,18 @@ class BatchConfig(C.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class ServerConfig(C.Structure):
+    """vox_cuda_server_config (include/voxtrees_cuda.h)."""
+    _fields_ = [("budget_bytes", C.c_uint64), ("host_budget_bytes", C.c_uint64), ("max_inflight", C.c_uint32),
+                ("max_batch", C.c_uint32),
+                ("streams", C.c_uint32), ("max_launches", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "rejected", "launches", "bytes_in_use",
+                                          "peak_bytes", "pending", "inflight")]
+
+
 _lib = None
 
 # name -> (restype, argtypes)
@@ -88,6 +100,16 @@ SIGNATURES = {
     "vox_cuda_batch_autotune": (C.c_int, [_vp, _vp, _u32, C.POINTER(BatchConfig), C.POINTER(C.c_float)]),
     "vox_cuda_batch_free": (C.c_int, [_vp]),
     "vox_cuda_render_frames_noalloc": (C.c_int, [C.POINTER(FrameJob), _u32, _vp]),
+    "vox_cuda_server_create": (C.c_int, [C.POINTER(ServerConfig), _vp, C.POINTER(_vp)]),
+    "vox_cuda_server_add_tree": (C.c_int, [_vp, _vp, C.POINTER(_u32)]),
+    "vox_cuda_server_submit_frame": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct), _u32, _u32,
+                                               C.POINTER(C.c_uint64)]),
+    "vox_cuda_server_submit_balls": (C.c_int, [_vp, _u32, _vp, _vp, _u32, C.POINTER(C.c_uint64)]),
+    "vox_cuda_server_wait": (C.c_int, [_vp, C.c_uint64, _u32]),
+    "vox_cuda_server_result": (C.c_int, [_vp, C.c_uint64, C.POINTER(_vp), C.POINTER(_sz), C.POINTER(C.c_uint64)]),
+    "vox_cuda_server_release": (C.c_int, [_vp, C.c_uint64]),
+    "vox_cuda_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
+    "vox_cuda_server_destroy": (C.c_int, [_vp]),
     "vox_cuda_render_counts_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp]),
     "vox_cuda_ray_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "vox_cuda_ball_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),

@@ -511,3 +511,48 @@ EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32
     count_launch();
     return status_of(cudaGetLastError());
 }
+
+/* ---------------------------------------------------------------------------
+ * Frame jobs for the request server (server.cpp): the batch kernel over a job
+ * table the server allocated for one launch.
+ * ------------------------------------------------------------------------- */
+
+size_t frame_job_entry_bytes() { return sizeof(BatchJobDev); }
+
+int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
+                       uint32_t *d_counter, int nsm, cudaStream_t s)
+{
+    if (njobs == 0 || njobs > MAX_JOBS) return VOX_CUDA_EINVAL;
+    BatchJobDev *table = static_cast<BatchJobDev *>(h_table);
+    uint32_t base = 0;
+    int cap = 0;
+    for (uint32_t q = 0; q < njobs; q++) {
+        const vox_cuda_frame_job &j = jobs[q];
+        BatchJobDev &d = table[q];
+        std::memset(&d, 0, sizeof d);
+        d.tree = j.tree->dev;
+        d.cam = j.camera;
+        d.tex = j.texture;
+        d.argb = j.argb;
+        d.status = j.tree->d_status;
+        d.w = j.w;
+        d.h = j.h;
+        vox::TileOrder o = tile_order(j.tree, j.camera, j.w, j.h, 8, 4);
+        d.ntx = o.nbx; d.nty = o.nby; d.ctx = o.cbx; d.cty = o.cby;
+        d.tile_base = base;
+        base += o.nbx * o.nby;
+        cap = std::max(cap, j.tree->cap_class);
+    }
+    if (cudaMemcpyAsync(d_table, table, njobs * sizeof(BatchJobDev), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s) != cudaSuccess)
+        return VOX_CUDA_ECUDA;
+    vox_cuda_batch_config c{8, 4, 2, 4};
+    const BatchJobDev *dt = static_cast<const BatchJobDev *>(d_table);
+    cudaError_t e;
+    switch (cap) {
+    case 0: e = launch_batch_cap<CAP0>(c, dt, njobs, base, d_counter, nsm, s); break;
+    case 1: e = launch_batch_cap<CAP1>(c, dt, njobs, base, d_counter, nsm, s); break;
+    default: e = launch_batch_cap<CAP2>(c, dt, njobs, base, d_counter, nsm, s); break;
+    }
+    return status_of(e);
+}

@@ -75,4 +75,11 @@ constexpr int TILE_W = 16, TILE_H = 8;   // render block tile; warps are 8x4
 vox::TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                           uint32_t tile_w = TILE_W, uint32_t tile_h = TILE_H);
 
+/* The batched frame kernel over a job table the caller allocated for one
+ * launch (batch.cu): fills h_table (pinned, frame_job_entry_bytes() per job),
+ * copies it to d_table, zeroes *d_counter and launches, all on s. */
+size_t frame_job_entry_bytes();
+int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
+                       uint32_t *d_counter, int nsm, cudaStream_t s);
+
 #endif

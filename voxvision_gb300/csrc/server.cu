@@ -1,0 +1,570 @@
+/*
+ * server.cu -- a request server over device-resident trees: frame and
+ * ball-collision requests from any number of client threads, admitted by a
+ * device-memory budget and batched continuously onto the GPU.
+ *
+ * Continuous batching.  A worker thread repeats: retire finished launches
+ * (returning their memory to the budget), admit waiting requests in arrival
+ * order while the budget and the in-flight slots allow, and put everything
+ * admitted since the previous launch into one launch on the next of several
+ * streams -- all frames into one persistent work-queue kernel (the batched
+ * kernel of batch.cu), each ball request into the ball kernel, then the
+ * copies of the results to pinned host memory.  Requests that arrive while
+ * earlier launches are still on the GPU therefore go out in the next launch
+ * and overlap with them on the device instead of waiting for them.
+ *
+ * Every result is the one the plain entry points give for the same request
+ * alone (vox_cuda_render_device, vox_cuda_ball_batch): same kernels, same
+ * trees, no state shared between requests.
+ *
+ * Waiting is bounded: vox_cuda_server_wait gives up after its timeout with
+ * VOX_CUDA_ETIMEOUT; a request that can never fit the budget is refused at
+ * submission with VOX_CUDA_EBUDGET.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "internal.h"
+
+#define EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+uint64_t now_ns()
+{
+    return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Pinned host buffers by power-of-two size class, reused across requests.
+size_t pinned_class(size_t bytes)
+{
+    size_t cls = 4096;
+    while (cls < bytes) cls <<= 1;
+    return cls;
+}
+
+class PinnedPool {
+  public:
+    ~PinnedPool()
+    {
+        for (auto &kv : free_)
+            for (void *p : kv.second) cudaFreeHost(p);
+    }
+    void *get(size_t bytes, size_t *cls_out)
+    {
+        size_t cls = pinned_class(bytes);
+        *cls_out = cls;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto &v = free_[cls];
+            if (!v.empty()) {
+                void *p = v.back();
+                v.pop_back();
+                return p;
+            }
+        }
+        void *p = nullptr;
+        if (cudaMallocHost(&p, cls) != cudaSuccess) return nullptr;
+        return p;
+    }
+    void put(void *p, size_t cls)
+    {
+        if (!p) return;
+        std::lock_guard<std::mutex> lk(mu_);
+        free_[cls].push_back(p);
+    }
+
+  private:
+    std::mutex mu_;
+    std::map<size_t, std::vector<void *>> free_;
+};
+
+enum Kind { FRAME = 0, BALLS = 1 };
+
+struct Request {
+    uint64_t ticket = 0;
+    Kind kind = FRAME;
+    uint32_t tree = 0;
+    vox_cuda_camera cam{};
+    uint32_t w = 0, h = 0, n = 0;
+    std::vector<float> centres, radii;
+    uint64_t dev_bytes = 0;         // charged to the device budget while admitted
+    uint64_t host_bytes = 0;        // charged to the pinned-host budget while admitted
+    void *d_buf = nullptr;          // frame, or centres | radii | hits
+    void *h_res = nullptr;          // pinned result
+    size_t h_cls = 0, res_bytes = 0;
+    void *h_in = nullptr;           // pinned ball inputs
+    size_t h_in_cls = 0;
+    uint64_t t_submit = 0, t_launch = 0, t_done = 0;
+    int status = VOX_CUDA_OK;
+    bool done = false;
+};
+
+struct Launch {
+    vox_cuda_server *srv = nullptr;
+    std::vector<Request *> reqs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;     // recorded after the result copies
+    void *h_table = nullptr;
+    size_t h_table_cls = 0;
+    void *d_table = nullptr;        // job table + queue head
+    std::atomic<bool> finished{false};   // set by the stream callback
+    std::atomic<uint64_t> t_cb{0};       // completion time seen by the callback
+    bool has_callback = false;      // then only `finished` may retire the launch
+    // buffers to give back once retired (taken off the requests under the lock)
+    std::vector<void *> dev_free;
+    std::vector<std::pair<void *, size_t>> host_free;
+};
+
+}  // namespace
+
+struct vox_cuda_server {
+    vox_cuda_server_config cfg{};
+    int device = 0, nsm = 0;
+    std::vector<const vox_cuda_tree *> trees;
+    uint8_t *d_tex = nullptr;
+    std::vector<cudaStream_t> streams;
+    size_t next_stream = 0;
+    PinnedPool pinned;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request *> pending;
+    std::vector<Request *> admitted;
+    std::vector<Launch *> inflight;
+    std::unordered_map<uint64_t, Request *> reqs;
+    uint64_t next_ticket = 1;
+    uint64_t used = 0, peak = 0, tree_bytes = 0, host_used = 0;
+    uint64_t submitted = 0, completed = 0, rejected = 0, launches = 0;
+    uint32_t inflight_reqs = 0;
+    uint32_t building = 0;          // launches being built outside the lock
+    bool stop = false;
+    std::thread worker;
+};
+
+namespace {
+
+// Runs on a driver thread once the launch's work and copies are done.  It
+// takes no lock and makes no CUDA call: the worker may hold the server lock
+// inside a CUDA call that waits for this stream, so blocking here could
+// deadlock.  A missed wake-up costs at most the worker's poll interval.
+void CUDART_CB on_launch_done(void *arg)
+{
+    Launch *L = static_cast<Launch *>(arg);
+    vox_cuda_server *s = L->srv;
+    L->t_cb.store(now_ns(), std::memory_order_relaxed);
+    L->finished.store(true, std::memory_order_release);
+    s->cv_work.notify_one();
+}
+
+// A launch whose callback is queued is retired only after the callback ran
+// (it still touches the launch); otherwise its event is polled.
+bool launch_finished(Launch *L)
+{
+    if (L->has_callback) {
+        if (!L->finished.load(std::memory_order_acquire)) return false;
+        uint64_t t = L->t_cb.load(std::memory_order_relaxed);
+        for (Request *r : L->reqs) if (!r->t_done) r->t_done = t;
+        return true;
+    }
+    if (L->done && cudaEventQuery(L->done) == cudaSuccess) {
+        uint64_t t = now_ns();
+        for (Request *r : L->reqs) if (!r->t_done) r->t_done = t;
+        return true;
+    }
+    return false;
+}
+
+// Under the lock: finished launches leave the in-flight list, their requests
+// are published and their memory is returned to the budgets; the buffers
+// themselves are handed back later by release_launch, outside the lock.
+void retire(vox_cuda_server *s, std::vector<Launch *> &out)
+{
+    bool any = false;
+    for (size_t i = 0; i < s->inflight.size();) {
+        Launch *L = s->inflight[i];
+        if (!launch_finished(L)) { i++; continue; }
+        for (Request *r : L->reqs) {
+            if (r->d_buf) L->dev_free.push_back(r->d_buf);
+            r->d_buf = nullptr;
+            if (r->h_in) L->host_free.push_back({r->h_in, r->h_in_cls});
+            r->h_in = nullptr;
+            s->used -= r->dev_bytes;
+            s->host_used -= r->host_bytes;
+            s->inflight_reqs--;
+            r->done = true;
+            s->completed++;
+        }
+        out.push_back(L);
+        s->inflight[i] = s->inflight.back();
+        s->inflight.pop_back();
+        any = true;
+    }
+    if (any) s->cv_done.notify_all();
+}
+
+// Outside the lock: give a retired launch's buffers back (stream-ordered).
+void release_launch(vox_cuda_server *s, Launch *L)
+{
+    for (void *p : L->dev_free) cudaFreeAsync(p, L->stream);
+    for (auto &hp : L->host_free) s->pinned.put(hp.first, hp.second);
+    if (L->d_table) cudaFreeAsync(L->d_table, L->stream);
+    s->pinned.put(L->h_table, L->h_table_cls);
+    if (L->done) cudaEventDestroy(L->done);
+    delete L;
+}
+
+// Outside the lock: everything admitted since the last launch, as one launch
+// on stream st.  The requests are not yet published, so no client touches
+// them meanwhile.
+Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cudaStream_t st)
+{
+    Launch *L = new Launch();
+    L->srv = s;
+    L->stream = st;
+    uint64_t t = now_ns();
+    std::vector<vox_cuda_frame_job> jobs;
+    std::vector<Request *> frames;
+    for (Request *r : batch) {
+        r->t_launch = t;
+        L->reqs.push_back(r);
+        size_t out_bytes = r->kind == FRAME ? (size_t)r->w * r->h * 4 : (size_t)r->n;
+        r->res_bytes = out_bytes;
+        r->h_res = s->pinned.get(out_bytes, &r->h_cls);
+        if (!r->h_res) { r->status = VOX_CUDA_ENOMEM; continue; }
+        if (r->kind == FRAME) {
+            if (cudaMallocAsync(&r->d_buf, out_bytes, st) != cudaSuccess) { r->status = VOX_CUDA_ENOMEM; continue; }
+            vox_cuda_frame_job j;
+            j.tree = s->trees[r->tree];
+            j.camera = r->cam;
+            j.w = r->w;
+            j.h = r->h;
+            j.texture = s->d_tex;
+            j.argb = static_cast<uint32_t *>(r->d_buf);
+            jobs.push_back(j);
+            frames.push_back(r);
+        } else {
+            size_t n = r->n, in_bytes = n * 16;
+            r->h_in = s->pinned.get(in_bytes, &r->h_in_cls);
+            if (!r->h_in || cudaMallocAsync(&r->d_buf, in_bytes + n + 256, st) != cudaSuccess) {
+                r->status = VOX_CUDA_ENOMEM;
+                continue;
+            }
+            std::memcpy(r->h_in, r->centres.data(), n * 12);
+            std::memcpy(static_cast<char *>(r->h_in) + n * 12, r->radii.data(), n * 4);
+            char *d = static_cast<char *>(r->d_buf);
+            if (cudaMemcpyAsync(d, r->h_in, in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+                r->status = VOX_CUDA_ECUDA;
+                continue;
+            }
+            int rc = vox_cuda_ball_batch_device(s->trees[r->tree], reinterpret_cast<float *>(d),
+                                                reinterpret_cast<float *>(d + n * 12), n,
+                                                reinterpret_cast<uint8_t *>(d + in_bytes), st);
+            if (rc) { r->status = rc; continue; }
+            if (cudaMemcpyAsync(r->h_res, d + in_bytes, n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                r->status = VOX_CUDA_ECUDA;
+        }
+    }
+    if (!jobs.empty()) {
+        size_t tb = (jobs.size() * frame_job_entry_bytes() + 255) & ~(size_t)255;
+        L->h_table = s->pinned.get(tb, &L->h_table_cls);
+        int rc = VOX_CUDA_ENOMEM;
+        if (L->h_table && cudaMallocAsync(&L->d_table, tb + 256, st) == cudaSuccess) {
+            uint32_t *counter = reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_table) + tb);
+            rc = enqueue_frame_jobs(jobs.data(), (uint32_t)jobs.size(), L->h_table, L->d_table, counter,
+                                    s->nsm, st);
+        }
+        for (Request *r : frames) {
+            if (rc) { r->status = rc; continue; }
+            if (cudaMemcpyAsync(r->h_res, r->d_buf, r->res_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                r->status = VOX_CUDA_ECUDA;
+        }
+    }
+    // completion is seen through the event; the callback only wakes the worker
+    if (cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventRecord(L->done, st) != cudaSuccess) {
+        if (L->done) cudaEventDestroy(L->done);
+        L->done = nullptr;
+    }
+    L->has_callback = cudaLaunchHostFunc(st, on_launch_done, L) == cudaSuccess;
+    if (!L->has_callback && !L->done) {
+        // neither a callback nor an event: wait for the stream outside any callback path
+        cudaStreamSynchronize(st);
+        uint64_t t2 = now_ns();
+        for (Request *r : L->reqs) { r->t_done = t2; if (!r->status) r->status = VOX_CUDA_ECUDA; }
+        L->finished.store(true);
+        L->has_callback = true;
+    }
+    return L;
+}
+
+void admit(vox_cuda_server *s)
+{
+    while (!s->pending.empty()) {
+        Request *r = s->pending.front();
+        if (s->inflight_reqs >= s->cfg.max_inflight) break;
+        if (s->used + r->dev_bytes > s->cfg.budget_bytes) break;   // arrival order: no overtaking
+        if (s->host_used + r->host_bytes > s->cfg.host_budget_bytes) break;
+        s->pending.pop_front();
+        s->used += r->dev_bytes;
+        s->host_used += r->host_bytes;
+        s->peak = std::max(s->peak, s->used);
+        s->inflight_reqs++;
+        s->admitted.push_back(r);
+        if (s->admitted.size() >= s->cfg.max_batch) break;
+    }
+}
+
+void worker_loop(vox_cuda_server *s)
+{
+    cudaSetDevice(s->device);
+    std::vector<Launch *> retired;
+    std::vector<Request *> batch;
+    for (;;) {
+        cudaStream_t st = nullptr;
+        bool quit = false;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait_for(lk, std::chrono::microseconds(s->inflight.empty() ? 2000 : 100), [s] {
+                if (s->stop) return true;
+                for (Launch *L : s->inflight) if (launch_finished(L)) return true;
+                return !s->pending.empty() && s->inflight_reqs < s->cfg.max_inflight;
+            });
+            retire(s, retired);
+            quit = s->stop && s->pending.empty() && s->admitted.empty() && s->inflight.empty();
+            admit(s);
+            if (!s->admitted.empty() && s->inflight.size() + s->building < s->cfg.max_launches) {
+                batch.swap(s->admitted);
+                st = s->streams[s->next_stream++ % s->streams.size()];
+                s->building++;
+            }
+        }
+        for (Launch *L : retired) release_launch(s, L);
+        retired.clear();
+        if (!batch.empty()) {
+            Launch *L = build_launch(s, batch, st);
+            batch.clear();
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->building--;
+            s->inflight.push_back(L);
+            s->launches++;
+        }
+        if (quit) break;
+    }
+}
+
+uint64_t request_bytes(Kind k, uint64_t a, uint64_t b)
+{
+    return k == FRAME ? a * b * 4 : a * 17 + 512;
+}
+
+// pinned host bytes a request holds while admitted: its result, and for ball
+// requests the staged inputs
+uint64_t request_host_bytes(Kind k, uint64_t a, uint64_t b)
+{
+    return k == FRAME ? pinned_class(a * b * 4) : pinned_class(a) + pinned_class(a * 16);
+}
+
+}  // namespace
+
+EXPORT int vox_cuda_server_create(const vox_cuda_server_config *config, const uint8_t *texture,
+                                  vox_cuda_server **out)
+{
+    if (!out || !texture) return VOX_CUDA_EINVAL;
+    *out = nullptr;
+    vox_cuda_server_config cfg = {40ull << 30, 16ull << 30, 1024, 256, 4, 8};
+    if (config) cfg = *config;
+    if (cfg.budget_bytes == 0 || cfg.host_budget_bytes == 0 || cfg.max_inflight == 0 || cfg.max_batch == 0 ||
+        cfg.max_batch > 1024 || cfg.streams == 0 || cfg.streams > 32 || cfg.max_launches == 0)
+        return VOX_CUDA_EINVAL;
+    vox_cuda_server *s = new (std::nothrow) vox_cuda_server();
+    if (!s) return VOX_CUDA_ENOMEM;
+    s->cfg = cfg;
+    if (cudaGetDevice(&s->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess) {
+        delete s;
+        return VOX_CUDA_ENODEV;
+    }
+    if (cudaMalloc(&s->d_tex, 32768) != cudaSuccess) { delete s; return VOX_CUDA_ENOMEM; }
+    if (cudaMemcpy(s->d_tex, texture, 32768, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(s->d_tex);
+        delete s;
+        return VOX_CUDA_ECUDA;
+    }
+    for (uint32_t i = 0; i < cfg.streams; i++) {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
+            cudaFree(s->d_tex);
+            delete s;
+            return VOX_CUDA_ECUDA;
+        }
+        s->streams.push_back(st);
+    }
+    s->worker = std::thread(worker_loop, s);
+    *out = s;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_server_add_tree(vox_cuda_server *s, const vox_cuda_tree *tree, uint32_t *tree_id)
+{
+    if (!s || !tree || !tree_id) return VOX_CUDA_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    vox_cuda_tree_info info;
+    vox_cuda_tree_get_info(tree, &info);
+    if (s->used + info.device_bytes > s->cfg.budget_bytes) return VOX_CUDA_EBUDGET;
+    s->used += info.device_bytes;          // resident trees count against the budget
+    s->tree_bytes += info.device_bytes;
+    s->peak = std::max(s->peak, s->used);
+    *tree_id = (uint32_t)s->trees.size();
+    s->trees.push_back(tree);
+    return VOX_CUDA_OK;
+}
+
+static int submit(vox_cuda_server *s, Request *r, uint64_t *ticket)
+{
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (r->tree >= s->trees.size()) { delete r; return VOX_CUDA_EINVAL; }
+    if (s->tree_bytes + r->dev_bytes > s->cfg.budget_bytes || r->host_bytes > s->cfg.host_budget_bytes) {
+        s->rejected++;
+        delete r;
+        return VOX_CUDA_EBUDGET;
+    }
+    r->ticket = s->next_ticket++;
+    r->t_submit = now_ns();
+    s->reqs[r->ticket] = r;
+    s->pending.push_back(r);
+    s->submitted++;
+    *ticket = r->ticket;
+    s->cv_work.notify_one();
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_server_submit_frame(vox_cuda_server *s, uint32_t tree_id, const vox_cuda_camera *camera,
+                                        uint32_t w, uint32_t h, uint64_t *ticket)
+{
+    if (!s || !camera || !ticket) return VOX_CUDA_EINVAL;
+    if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
+    if (camera->kind != VOX_CUDA_CAMERA_SIMPLE && camera->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+    Request *r = new (std::nothrow) Request();
+    if (!r) return VOX_CUDA_ENOMEM;
+    r->kind = FRAME;
+    r->tree = tree_id;
+    r->cam = *camera;
+    r->w = w;
+    r->h = h;
+    r->dev_bytes = request_bytes(FRAME, w, h);
+    r->host_bytes = request_host_bytes(FRAME, w, h);
+    return submit(s, r, ticket);
+}
+
+EXPORT int vox_cuda_server_submit_balls(vox_cuda_server *s, uint32_t tree_id, const float *centres,
+                                        const float *radii, uint32_t n, uint64_t *ticket)
+{
+    if (!s || !ticket || n == 0 || !centres || !radii) return VOX_CUDA_EINVAL;
+    Request *r = new (std::nothrow) Request();
+    if (!r) return VOX_CUDA_ENOMEM;
+    r->kind = BALLS;
+    r->tree = tree_id;
+    r->n = n;
+    r->centres.assign(centres, centres + 3 * (size_t)n);
+    r->radii.assign(radii, radii + n);
+    r->dev_bytes = request_bytes(BALLS, n, 0);
+    r->host_bytes = request_host_bytes(BALLS, n, 0);
+    return submit(s, r, ticket);
+}
+
+EXPORT int vox_cuda_server_wait(vox_cuda_server *s, uint64_t ticket, uint32_t timeout_ms)
+{
+    if (!s) return VOX_CUDA_EINVAL;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return VOX_CUDA_EINVAL;
+    Request *r = it->second;
+    if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [r] { return r->done; }))
+        return VOX_CUDA_ETIMEOUT;
+    return r->status;
+}
+
+EXPORT int vox_cuda_server_result(vox_cuda_server *s, uint64_t ticket, const void **data, size_t *bytes,
+                                  uint64_t *times_ns)
+{
+    if (!s) return VOX_CUDA_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return VOX_CUDA_EINVAL;
+    Request *r = it->second;
+    if (!r->done) return VOX_CUDA_ETIMEOUT;
+    if (data) *data = r->h_res;
+    if (bytes) *bytes = r->res_bytes;
+    if (times_ns) {
+        times_ns[0] = r->t_submit;
+        times_ns[1] = r->t_launch;
+        times_ns[2] = r->t_done;
+    }
+    return r->status;
+}
+
+EXPORT int vox_cuda_server_release(vox_cuda_server *s, uint64_t ticket)
+{
+    if (!s) return VOX_CUDA_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return VOX_CUDA_EINVAL;
+    Request *r = it->second;
+    if (!r->done) return VOX_CUDA_EINVAL;
+    s->pinned.put(r->h_res, r->h_cls);
+    s->reqs.erase(it);
+    delete r;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_server_get_stats(vox_cuda_server *s, vox_cuda_server_stats *st)
+{
+    if (!s || !st) return VOX_CUDA_EINVAL;
+    std::lock_guard<std::mutex> lk(s->mu);
+    st->submitted = s->submitted;
+    st->completed = s->completed;
+    st->rejected = s->rejected;
+    st->launches = s->launches;
+    st->bytes_in_use = s->used;
+    st->peak_bytes = s->peak;
+    st->pending = s->pending.size();
+    st->inflight = s->inflight_reqs;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_server_destroy(vox_cuda_server *s)
+{
+    if (!s) return VOX_CUDA_EINVAL;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_one();
+    if (s->worker.joinable()) s->worker.join();
+    for (cudaStream_t st : s->streams) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (auto &kv : s->reqs) {
+        s->pinned.put(kv.second->h_res, kv.second->h_cls);
+        delete kv.second;
+    }
+    cudaFree(s->d_tex);
+    delete s;
+    return VOX_CUDA_OK;
+}

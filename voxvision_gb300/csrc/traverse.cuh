@@ -28,6 +28,7 @@ struct DevTree {
     uint32_t root;               // record offset of the root, VOXP_EMPTY if none
     uint32_t n_nodes;
     float vx, vy, vz;            // vox_voxel at upload time
+    uint32_t max_steps;          // nodes + voxels: no search takes more loop steps
 };
 
 struct Counts {
@@ -144,8 +145,12 @@ __device__ __forceinline__ bool trace_ray(const DevTree &t, uint32_t start,
     uint32_t vi = 0, vn = 0, vrec = 0, vid = 0;
     float best = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
     int win = -1;
+    uint32_t steps = 0;
 
     for (;;) {
+        // Each node and each voxel is tested at most once per search, so more
+        // steps than the tree holds means a damaged pool: stop with an error.
+        if (++steps > t.max_steps) { overflow = true; return false; }
         uint4 u0 = ld16(pool + (scan ? cur + vi : cur));
         uint4 u1 = make_uint4(0u, 0u, 0u, 0u), u2 = make_uint4(0u, 0u, 0u, 0u);
         if (!scan) {
@@ -301,7 +306,9 @@ __device__ __forceinline__ bool trace_ball(const DevTree &t, float cx, float cy,
     uint32_t cur = t.root;
     const uint4 *pool = t.pool;
     float rr = __fmul_rn(r, r);
+    uint32_t steps = 0;
     for (;;) {
+        if (++steps > t.max_steps) { overflow = true; return false; }   // damaged pool
         uint4 a = ld16(pool + cur);
         uint4 b = ld16(pool + cur + 1);
         if (COUNT) cnt.nodes++;

@@ -454,6 +454,8 @@ EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out
     t->dev.vx = t->flat.voxel[0];
     t->dev.vy = t->flat.voxel[1];
     t->dev.vz = t->flat.voxel[2];
+    uint64_t steps = (uint64_t)nodes + t->flat.n_dots + 2;
+    t->dev.max_steps = steps > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)steps;
     // The flattened image is on the device now; keep only the maps.
     std::vector<uint4_host>().swap(t->flat.units);
     *out = t;
