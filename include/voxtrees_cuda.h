@@ -134,6 +134,32 @@ int vox_cuda_render_device(const vox_cuda_tree *tree, const vox_cuda_camera *cam
                            uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
                            void *stream);
 
+/* Settings of the BEST-quality frame kernel behind vox_cuda_render*,
+ * process-wide (no counterpart in the reference, whose renderer has no
+ * kernel).  cull = 1: trace only the rectangle of vox_cuda_frame_rect for the
+ * tree's bounding box and clear the rest of the frame; 0: trace every pixel.
+ * overlap = 1: launch with programmatic dependent launch, so that a frame's
+ * traversal starts while the previous kernel of the stream finishes; the
+ * kernel still reads the texture and writes the frame only after that
+ * kernel has completed, so stream order holds for all caller memory; 0: an
+ * ordinary launch.  Every setting draws the same frame.  Defaults: 1, 1.
+ * Values other than 0 and 1: VOX_CUDA_EINVAL. */
+typedef struct {
+    uint32_t cull;
+    uint32_t overlap;
+} vox_cuda_render_config;
+int vox_cuda_render_set_config(const vox_cuda_render_config *config);
+int vox_cuda_render_get_config(vox_cuda_render_config *config);
+
+/* The rectangle [rect[0], rect[2]) x [rect[1], rect[3]) of a w x h frame
+ * outside which no pixel's ray can enter the box bbox (min x, y, z, max x,
+ * y, z), rounded out to multiples of 8 x 4 pixels; all zero when no pixel
+ * can.  The BEST frame kernel traces only this rectangle of the tree's
+ * bounding box and clears the rest.  Host-only arithmetic, no GPU needed.
+ * No counterpart in the reference, which traces every pixel. */
+int vox_cuda_frame_rect(const float *bbox, const vox_cuda_camera *camera, uint32_t w, uint32_t h,
+                        uint32_t *rect);
+
 /* Quality values of vox_context_set_quality (src/voxrnd/renderer.h). */
 #define VOX_CUDA_QUALITY_BEST                0x0
 #define VOX_CUDA_QUALITY_FAST                0x1

@@ -1,0 +1,172 @@
+"""GPU parity of the BEST frame kernel under every setting (culled to the
+tree's screen rectangle or not, overlapped with the previous kernel of the
+stream or not): each frame equals the oracle's pixel for pixel, every pixel
+of the output is written (the ones outside the rectangle are cleared), stream
+order holds for the texture and the frame when consecutive kernels overlap,
+and the setting API validates its input."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+CONFIGS = [(1, 1), (1, 0), (0, 1), (0, 0)]
+GARBAGE = 0x5EADBEEF
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from voxvision_gb300.build import build
+    build()
+    import voxvision_gb300 as vg
+    saved = vg.render_config()
+    yield
+    vg.set_render_config(saved["cull"], saved["overlap"])
+
+
+def vg():
+    import voxvision_gb300
+    return voxvision_gb300
+
+
+@pytest.fixture(scope="module")
+def tree256():
+    from voxvision_gb300 import workloads as wl
+    vg().set_voxel_size((1, 1, 1))
+    orc.set_voxel((1, 1, 1))
+    ht = vg().HostTree.from_voxels(wl.voxels_from_mask(wl.noise_volume(256, 2, 0.08)))
+    return ht, vg().DeviceTree(ht.ptr)
+
+
+@pytest.fixture(scope="module")
+def tree64():
+    from voxvision_gb300 import workloads as wl
+    vg().set_voxel_size((1, 1, 1))
+    orc.set_voxel((1, 1, 1))
+    ht = vg().HostTree.from_voxels(wl.voxels_from_mask(wl.blobs_volume(64, 20, 1, 0.20)))
+    return ht, vg().DeviceTree(ht.ptr)
+
+
+def render_device(dt, cam, w, h, tex):
+    """Through vox_cuda_render_device into a buffer full of garbage."""
+    d_tex = torch.from_numpy(tex).cuda()
+    out = torch.full((w * h,), GARBAGE, dtype=torch.int64).to(torch.int32).cuda()
+    dt.render_device(cam, w, h, d_tex, out, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(np.uint32).reshape(h, w)
+
+
+@pytest.mark.parametrize("frame", [0, 44, 90])
+def test_orbit_frames_equal_oracle_under_every_setting(tree256, frame):
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import orbit_camera
+    ht, dt = tree256
+    tex = wl.texture32(7)
+    cam = orbit_camera(frame, 120, 1920, 1080, (128, 128, 128), 1.5 * 256 * 3 ** 0.5)
+    ref, _ = orc.render_best(ht.ptr, cam.state(), 1920, 1080, tex)
+    for cfg in CONFIGS:
+        vg().set_render_config(*cfg)
+        img = render_device(dt, cam.gpu_struct(), 1920, 1080, tex)
+        assert np.array_equal(img, ref), f"setting {cfg}: {(img != ref).sum()} pixels differ"
+
+
+def _cameras():
+    """Simple and doom cameras near, far, off-centre, inside the tree's box
+    and looking away from it; fields of view 0.3..2."""
+    from voxvision_gb300 import workloads as wl
+    rng = np.random.default_rng(5)
+    centre = np.array([32.0, 32.0, 32.0])
+    out = []
+    for kind in (0, 1):
+        for dist in (1.05, 1.5, 3.0, 30.0):
+            for _ in range(2):
+                pos = wl.pose_position(centre, dist * 55.4, rng.uniform(0, 6.28), rng.uniform(-50, 50))
+                out.append((kind, pos, centre + rng.normal(0, 20, 3), float(rng.choice([0.3, 1.0, 2.0]))))
+        out.append((kind, centre + 2.5, centre + 30.0, 1.0))
+        out.append((kind, centre + [0, 200.0, 5.0], centre + [0, 400.0, 5.0], 1.0))
+    return out
+
+
+@pytest.mark.parametrize("cfg", [(1, 1), (0, 0)])
+def test_many_cameras_equal_oracle(tree64, cfg):
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    ht, dt = tree64
+    tex = wl.texture32(7)
+    vg().set_render_config(*cfg)
+    for kind, pos, target, fov in _cameras():
+        for w, h in ((128, 96), (336, 200)):
+            cam = HostCamera(kind)
+            cam.set_fov(fov)
+            cam.set_window_size(w, h)
+            cam.set_position(pos)
+            cam.look_at(np.asarray(target, np.float32))
+            ref, _ = orc.render_best(ht.ptr, cam.state(), w, h, tex)
+            img = render_device(dt, cam.gpu_struct(), w, h, tex)
+            assert np.array_equal(img, ref), f"{kind} {pos} {w}x{h}: {(img != ref).sum()} pixels differ"
+            host = dt.render(cam.gpu_struct(), w, h, tex)
+            assert np.array_equal(host, ref)
+
+
+def test_smallest_frame_and_empty_tree(tree64):
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    ht, dt = tree64
+    tex = wl.texture32(7)
+    vg().set_render_config(1, 1)
+    cam = HostCamera(0)
+    cam.set_window_size(16, 4)
+    cam.set_position((32.0, -60.0, 32.0))
+    cam.look_at(np.array([32.0, 32.0, 32.0], np.float32))
+    ref, _ = orc.render_best(ht.ptr, cam.state(), 16, 4, tex)
+    assert np.array_equal(render_device(dt, cam.gpu_struct(), 16, 4, tex), ref)
+    empty = vg().DeviceTree(None)
+    cam.set_window_size(64, 32)
+    assert (render_device(empty, cam.gpu_struct(), 64, 32, tex) == 0).all()
+
+
+def test_stream_order_holds_when_frames_overlap(tree64):
+    """Frames rendered back to back into one buffer, the texture rewritten by
+    a torch kernel and the frame copied out between them, all on one stream:
+    each copy shows the frame of the camera and texture before it."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    ht, dt = tree64
+    vg().set_render_config(1, 1)
+    texs = [wl.texture32(7), wl.texture32(8)]
+    stream = torch.cuda.current_stream()
+    d_tex = torch.from_numpy(texs[0]).cuda()
+    d_texs = [torch.from_numpy(t).cuda() for t in texs]
+    w, h = 336, 200
+    out = torch.full((w * h,), GARBAGE, dtype=torch.int64).to(torch.int32).cuda()
+    cams, copies = [], []
+    rng = np.random.default_rng(9)
+    for i in range(12):
+        cam = HostCamera(i % 2)
+        cam.set_window_size(w, h)
+        cam.set_position(wl.pose_position((32, 32, 32), rng.uniform(60, 200), rng.uniform(0, 6.28),
+                                          rng.uniform(-40, 40)))
+        cam.look_at(np.asarray((32, 32, 32) + rng.normal(0, 10, 3), np.float32))
+        d_tex.copy_(d_texs[i % 2])
+        dt.render_device(cam.gpu_struct(), w, h, d_tex, out, stream=stream.cuda_stream)
+        copies.append(out.clone())
+        cams.append(cam)
+    torch.cuda.synchronize()
+    for i, (cam, cp) in enumerate(zip(cams, copies)):
+        ref, _ = orc.render_best(ht.ptr, cam.state(), w, h, texs[i % 2])
+        img = cp.cpu().numpy().view(np.uint32).reshape(h, w)
+        assert np.array_equal(img, ref), f"frame {i}: {(img != ref).sum()} pixels differ"
+
+
+def test_setting_api_validates():
+    with pytest.raises(vg().VoxCudaError):
+        vg().set_render_config(2, 1)
+    with pytest.raises(vg().VoxCudaError):
+        vg().set_render_config(1, 2)
+    vg().set_render_config(0, 1)
+    assert vg().render_config() == {"cull": 0, "overlap": 1}

@@ -14,10 +14,12 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, BatchConfig, CameraStruct,
-                   FrameJob, ServerConfig, ServerStats, TreeInfo, VoxCudaError, available, check, lib)
+                   FrameJob, RenderConfig, ServerConfig, ServerStats, TreeInfo, VoxCudaError, available, check,
+                   lib)
 
 __all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Server", "ServerConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
-           "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size"]
+           "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size",
+           "frame_rect", "render_config", "set_render_config"]
 
 
 def _p(a: np.ndarray):
@@ -186,6 +188,29 @@ def camera_struct(state: dict) -> CameraStruct:
 
 
 Camera = CameraStruct
+
+
+def frame_rect(bbox, cam: CameraStruct, w: int, h: int):
+    """vox_cuda_frame_rect: (x0, y0, x1, y1) of the w x h frame outside which
+    no ray of `cam` can enter the box bbox = (min xyz, max xyz)."""
+    b = np.ascontiguousarray(bbox, dtype=np.float32)
+    r = np.zeros(4, np.uint32)
+    check(lib().vox_cuda_frame_rect(_p(b), C.byref(cam), w, h, _p(r)), "vox_cuda_frame_rect")
+    return tuple(int(x) for x in r)
+
+
+def render_config() -> dict:
+    """The process-wide BEST frame kernel settings (vox_cuda_render_get_config)."""
+    c = RenderConfig()
+    check(lib().vox_cuda_render_get_config(C.byref(c)), "vox_cuda_render_get_config")
+    return {"cull": c.cull, "overlap": c.overlap}
+
+
+def set_render_config(cull: int = 1, overlap: int = 1):
+    """vox_cuda_render_set_config: cull to the tree's screen rectangle,
+    overlap consecutive frames' kernels (both 0 or 1)."""
+    c = RenderConfig(cull, overlap)
+    check(lib().vox_cuda_render_set_config(C.byref(c)), "vox_cuda_render_set_config")
 
 
 class FrameBatch:

@@ -63,6 +63,11 @@ class ServerConfig(C.Structure):
                 ("streams", C.c_uint32), ("max_launches", C.c_uint32)]
 
 
+class RenderConfig(C.Structure):
+    """vox_cuda_render_config (include/voxtrees_cuda.h)."""
+    _fields_ = [("cull", C.c_uint32), ("overlap", C.c_uint32)]
+
+
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "rejected", "launches", "bytes_in_use",
                                           "peak_bytes", "pending", "inflight")]
@@ -92,6 +97,9 @@ SIGNATURES = {
                                           _vp]),
     "vox_cuda_render_quality_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp,
                                                  _vp, _vp]),
+    "vox_cuda_frame_rect": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp]),
+    "vox_cuda_render_set_config": (C.c_int, [C.POINTER(RenderConfig)]),
+    "vox_cuda_render_get_config": (C.c_int, [C.POINTER(RenderConfig)]),
     "vox_cuda_batch_create": (C.c_int, [C.POINTER(FrameJob), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
     "vox_cuda_batch_set_camera": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct)]),
     "vox_cuda_batch_launch": (C.c_int, [_vp, _vp]),

@@ -67,6 +67,16 @@ struct TileOrder {
     uint32_t nbx, nby, cbx, cby;
 };
 
+// Work of one BEST frame: the screen rectangle that the tree's bounding box
+// can project into (pixels outside it cannot reach the tree and are misses),
+// cut in 16x8-pixel block tiles issued outward from the tile where the tree's
+// centre projects, and the number of blocks that clear the rest.
+struct FramePlan {
+    uint32_t x0, y0, x1, y1;     // traced rectangle, multiples of 8 x 4
+    uint32_t ntx, nty, ctx, cty; // tiles across / down, tile where the centre projects
+    uint32_t ntiles, nclear;     // tracing blocks, clearing blocks
+};
+
 }  // namespace vox
 
 constexpr int TILE_W = 16, TILE_H = 8;   // render block tile; warps are 8x4
@@ -74,6 +84,12 @@ constexpr int TILE_W = 16, TILE_H = 8;   // render block tile; warps are 8x4
 /* Order in which the render kernel issues its block tiles for this camera. */
 vox::TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                           uint32_t tile_w = TILE_W, uint32_t tile_h = TILE_H);
+
+/* The plan of a BEST frame; cull = false traces the whole frame.
+ * Conservative: every pixel whose ray can enter the tree's bounding box lies
+ * inside the rectangle. */
+void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h, bool cull,
+                vox::FramePlan &p);
 
 /* The batched frame kernel over a job table the caller allocated for one
  * launch (batch.cu): fills h_table (pinned, frame_job_entry_bytes() per job),

@@ -112,171 +112,213 @@ struct RayHit {
     uint32_t rec;     // record offset of the leaf
 };
 
-/* vox_ray_tree_intersection (search.c:8-153) from the node whose record is
- * at `start`.
+/* vox_ray_tree_intersection (search.c:8-153) as a resumable search.
  *
- * Every loop iteration makes one 16..48-byte load (a node record, or one
- * voxel of the leaf being scanned) and one box test, so the lanes of a warp
- * stay in step whatever mix of nodes and voxels they are on.  The box test
- * of a node is search.c:22-23; of a voxel, the leaf loop's test at :55.
- * When an inner node's box is entered, its plane crossings (:105-148) are
- * computed at once: the children behind the crossings are pushed in visiting
- * order and the search continues in the entry octant (:86-97).  Computing
- * the crossings before the entry octant has been searched changes nothing:
- * they depend only on the node and the ray, and they are used only if that
- * octant finds nothing.  The first hit ends the search, as the first
- * non-NULL return ends the recursion.
+ * RaySearch holds everything one search carries between loop iterations
+ * except its stack of pending tasks, which the caller keeps beside it (a
+ * separate local array, so the search state itself stays in registers), and
+ * ray_step() runs one iteration.  Every iteration makes one 16..48-byte load
+ * (a node record, or one voxel of the leaf being scanned) and one box test,
+ * so the lanes of a warp stay in step whatever mix of nodes and voxels they
+ * are on, and a lane whose search ended can start another between any two
+ * iterations (the refill render kernel does).  The box test of a node is
+ * search.c:22-23; of a voxel, the leaf loop's test at :55.  When an inner
+ * node's box is entered, its plane crossings (:105-148) are computed at once:
+ * the children behind the crossings are pushed in visiting order and the
+ * search continues in the entry octant (:86-97).  Computing the crossings
+ * before the entry octant has been searched changes nothing: they depend only
+ * on the node and the ray, and they are used only if that octant finds
+ * nothing.  The first hit ends the search, as the first non-NULL return ends
+ * the recursion.
  *
- * Returns true on a hit.  `overflow` is set (and the search ends as a miss)
- * if the stack would exceed CAP entries, which the upload-time depth check
- * rules out (3 entries per inner level suffice). */
+ * The stack holds pending tasks {record offset, ray origin}; it never needs
+ * more than 3 entries per inner level, which the upload-time depth check
+ * guarantees for CAP.  A search that would overflow it, or that takes more
+ * iterations than the tree has nodes and voxels (a damaged pool), ends with
+ * STEP_ERROR. */
+enum : int { STEP_MORE = 0, STEP_HIT = 1, STEP_MISS = 2, STEP_ERROR = 3 };
+
+struct RaySearch {
+    int sp;                    // entries on the caller's stack
+    uint32_t cur;              // node mode: record offset; voxel mode: first voxel
+    float ox, oy, oz;          // origin of the next box test
+    float dx, dy, dz;
+    bool scan;                 // scanning the voxels of a leaf
+    uint32_t vi, vn, vrec, vid;
+    float best, bx, by, bz;
+    int win;
+    uint32_t steps;
+};
+
+__device__ __forceinline__ void ray_begin(RaySearch &s, uint32_t start, float ox, float oy, float oz,
+                                          float dx, float dy, float dz)
+{
+    s.sp = 0;
+    s.cur = start;
+    s.ox = ox; s.oy = oy; s.oz = oz;
+    s.dx = dx; s.dy = dy; s.dz = dz;
+    s.scan = false;
+    s.vi = 0; s.vn = 0; s.vrec = 0; s.vid = 0;
+    s.best = 0.0f; s.bx = 0.0f; s.by = 0.0f; s.bz = 0.0f;
+    s.win = -1;
+    s.steps = 0;
+}
+
+template <int CAP, bool COUNT>
+__device__ __forceinline__ int ray_step(const DevTree &t, RaySearch &s, uint4 (&stack)[CAP], RayHit &hit,
+                                        Counts &cnt)
+{
+    // Each node and each voxel is tested at most once per search, so more
+    // steps than the tree holds means a damaged pool: stop with an error.
+    if (++s.steps > t.max_steps) return STEP_ERROR;
+    const uint4 *pool = t.pool;
+    const float dx = s.dx, dy = s.dy, dz = s.dz;
+    uint4 u0 = ld16(pool + (s.scan ? s.cur + s.vi : s.cur));
+    uint4 u1 = make_uint4(0u, 0u, 0u, 0u), u2 = make_uint4(0u, 0u, 0u, 0u);
+    if (!s.scan) {
+        u1 = ld16(pool + s.cur + 1);
+        u2 = ld16(pool + s.cur + 2);
+    }
+    float lx = ubf(u0.x), ly = ubf(u0.y), lz = ubf(u0.z), hx, hy, hz;
+    if (s.scan) {   // voxel box [dot, dot + vox_voxel] (search.c:53-54)
+        hx = __fadd_rn(lx, t.vx); hy = __fadd_rn(ly, t.vy); hz = __fadd_rn(lz, t.vz);
+        if (COUNT) cnt.voxels++;
+    } else {
+        hx = ubf(u0.w); hy = ubf(u1.x); hz = ubf(u1.y);
+        if (COUNT) cnt.nodes++;
+    }
+    float ex, ey, ez;
+    bool in = hit_box(lx, ly, lz, hx, hy, hz, s.ox, s.oy, s.oz, dx, dy, dz, ex, ey, ez);
+    bool resume = false;
+
+    if (s.scan) {
+        // leaf loop body, search.c:55-78: nearest voxel by L1 distance from
+        // the leaf's entry point, first one at distance 0 wins at once
+        bool stop = false;
+        if (in) {
+            float dist = l1(s.ox, s.oy, s.oz, ex, ey, ez);
+            if (dist == 0.0f) {
+                s.bx = ex; s.by = ey; s.bz = ez; s.win = (int)s.vi; stop = true;
+            } else if (dist < s.best) {
+                s.best = dist; s.bx = ex; s.by = ey; s.bz = ez; s.win = (int)s.vi;
+            }
+        }
+        s.vi++;
+        if (stop || s.vi == s.vn) {
+            if (s.win >= 0) {
+                hit.x = s.bx; hit.y = s.by; hit.z = s.bz;
+                hit.leaf = s.vid; hit.slot = (uint32_t)s.win; hit.rec = s.vrec;
+                return STEP_HIT;
+            }
+            s.scan = false;
+            resume = true;
+        }
+    } else if (!in) {
+        resume = true;
+    } else {
+        uint32_t meta = u1.z, link = u1.w, kind = meta & 3u;
+        if (kind == VOXP_KIND_DENSE) {                      // search.c:31-37
+            hit.x = ex; hit.y = ey; hit.z = ez;
+            hit.leaf = link; hit.slot = 0xFFu; hit.rec = s.cur;
+            return STEP_HIT;
+        }
+        if (kind == VOXP_KIND_LEAF) {                       // search.c:39-50
+            s.vn = meta >> 2;
+            if (s.vn == 0) {
+                resume = true;
+            } else {
+                s.scan = true; s.vrec = s.cur; s.vid = u2.x; s.cur = link; s.vi = 0;
+                s.best = __int_as_float(0x7f800000); s.win = -1;
+                s.ox = ex; s.oy = ey; s.oz = ez;
+            }
+        } else {                                            // inner node
+            if (COUNT) cnt.inner++;
+            float cx = ubf(u2.x), cy = ubf(u2.y), cz = ubf(u2.z);
+            // geom.c:53-65 get_corrected_subspace_idx
+            uint32_t sub = ((cx == ex) ? (dx < 0.0f) : (cx > ex))
+                         | (((cy == ey) ? (dy < 0.0f) : (cy > ey)) << 1)
+                         | (((cz == ez) ? (dz < 0.0f) : (cz > ez)) << 2);
+            uint32_t mask = (meta >> 8) & 0xFFu;
+            // search.c:105-113: the crossings with the three dividing
+            // planes that lie in the box, kept in axis order
+            float qx0, qy0, qz0, qx1, qy1, qz1, qx2, qy2, qz2;
+            bool v0 = hit_plane(0, ex, ey, ez, dx, dy, dz, cx, lx, ly, lz, hx, hy, hz, qx0, qy0, qz0);
+            bool v1 = hit_plane(1, ex, ey, ez, dx, dy, dz, cy, lx, ly, lz, hx, hy, hz, qx1, qy1, qz1);
+            bool v2 = hit_plane(2, ex, ey, ez, dx, dy, dz, cz, lx, ly, lz, hx, hy, hz, qx2, qy2, qz2);
+            int pc = (int)v0 + (int)v1 + (int)v2;
+            // compacted slots a, b, c = first, second, third valid crossing
+            float ax = v0 ? qx0 : (v1 ? qx1 : qx2);
+            float ay = v0 ? qy0 : (v1 ? qy1 : qy2);
+            float az = v0 ? qz0 : (v1 ? qz1 : qz2);
+            int ai = v0 ? 0 : (v1 ? 1 : 2);
+            bool ab1 = v0 && v1;
+            float bxp = ab1 ? qx1 : qx2, byp = ab1 ? qy1 : qy2, bzp = ab1 ? qz1 : qz2;
+            int bi = ab1 ? 1 : 2;
+            float cxp = qx2, cyp = qy2, czp = qz2;
+            int ci = 2;
+            float ma = l1(ex, ey, ez, ax, ay, az);
+            float mb = l1(ex, ey, ez, bxp, byp, bzp);
+            float mc = l1(ex, ey, ez, cxp, cyp, czp);
+            // search.c:115-134: selection sort with immediate swaps on '<'
+            if (pc > 1 && mb < ma) {
+                float t0 = ax; ax = bxp; bxp = t0; t0 = ay; ay = byp; byp = t0; t0 = az; az = bzp; bzp = t0;
+                t0 = ma; ma = mb; mb = t0; int ti = ai; ai = bi; bi = ti;
+            }
+            if (pc > 2 && mc < ma) {
+                float t0 = ax; ax = cxp; cxp = t0; t0 = ay; ay = cyp; cyp = t0; t0 = az; az = czp; czp = t0;
+                t0 = ma; ma = mc; mc = t0; int ti = ai; ai = ci; ci = ti;
+            }
+            if (pc > 2 && mc < mb) {
+                float t0 = bxp; bxp = cxp; cxp = t0; t0 = byp; byp = cyp; cyp = t0; t0 = bzp; bzp = czp; czp = t0;
+                t0 = mb; mb = mc; mc = t0; int ti = bi; bi = ci; ci = ti;
+            }
+            // search.c:137: each crossing flips one octant bit; NULL
+            // children are skipped (they return NULL at once)
+            uint32_t s1 = sub ^ (1u << ai), s2 = s1 ^ (1u << bi), s3 = s2 ^ (1u << ci);
+            bool w1 = pc > 0 && ((mask >> s1) & 1u);
+            bool w2 = pc > 1 && ((mask >> s2) & 1u);
+            bool w3 = pc > 2 && ((mask >> s3) & 1u);
+            int npush = (int)w1 + (int)w2 + (int)w3;
+            if (s.sp + npush > CAP) return STEP_ERROR;
+            if (w3) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s3) - 1u)),
+                                                 __float_as_uint(cxp), __float_as_uint(cyp), __float_as_uint(czp));
+            if (w2) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s2) - 1u)),
+                                                 __float_as_uint(bxp), __float_as_uint(byp), __float_as_uint(bzp));
+            if (w1) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s1) - 1u)),
+                                                 __float_as_uint(ax), __float_as_uint(ay), __float_as_uint(az));
+            if ((mask >> sub) & 1u) {                       // search.c:92-93
+                s.cur = link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << sub) - 1u));
+                s.ox = ex; s.oy = ey; s.oz = ez;
+            } else {
+                resume = true;
+            }
+        }
+    }
+    if (resume) {
+        if (s.sp == 0) return STEP_MISS;
+        uint4 e = stack[--s.sp];
+        s.cur = e.x;
+        s.ox = ubf(e.y); s.oy = ubf(e.z); s.oz = ubf(e.w);
+    }
+    return STEP_MORE;
+}
+
+/* The whole search from the node whose record is at `start`.  Returns true
+ * on a hit; `overflow` is set (and the search ends as a miss) on STEP_ERROR. */
 template <int CAP, bool COUNT>
 __device__ __forceinline__ bool trace_ray(const DevTree &t, uint32_t start,
                                           float ox0, float oy0, float oz0,
                                           float dx, float dy, float dz,
                                           RayHit &hit, Counts &cnt, bool &overflow)
 {
+    RaySearch s;
     uint4 stack[CAP];
-    int sp = 0;
-    const uint4 *pool = t.pool;
-    uint32_t cur = start;                 // node mode: record offset; voxel mode: first voxel
-    float ox = ox0, oy = oy0, oz = oz0;   // origin of the next box test
-    bool scan = false;                    // scanning the voxels of a leaf
-    uint32_t vi = 0, vn = 0, vrec = 0, vid = 0;
-    float best = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
-    int win = -1;
-    uint32_t steps = 0;
-
+    ray_begin(s, start, ox0, oy0, oz0, dx, dy, dz);
     for (;;) {
-        // Each node and each voxel is tested at most once per search, so more
-        // steps than the tree holds means a damaged pool: stop with an error.
-        if (++steps > t.max_steps) { overflow = true; return false; }
-        uint4 u0 = ld16(pool + (scan ? cur + vi : cur));
-        uint4 u1 = make_uint4(0u, 0u, 0u, 0u), u2 = make_uint4(0u, 0u, 0u, 0u);
-        if (!scan) {
-            u1 = ld16(pool + cur + 1);
-            u2 = ld16(pool + cur + 2);
-        }
-        float lx = ubf(u0.x), ly = ubf(u0.y), lz = ubf(u0.z), hx, hy, hz;
-        if (scan) {   // voxel box [dot, dot + vox_voxel] (search.c:53-54)
-            hx = __fadd_rn(lx, t.vx); hy = __fadd_rn(ly, t.vy); hz = __fadd_rn(lz, t.vz);
-            if (COUNT) cnt.voxels++;
-        } else {
-            hx = ubf(u0.w); hy = ubf(u1.x); hz = ubf(u1.y);
-            if (COUNT) cnt.nodes++;
-        }
-        float ex, ey, ez;
-        bool in = hit_box(lx, ly, lz, hx, hy, hz, ox, oy, oz, dx, dy, dz, ex, ey, ez);
-        bool resume = false;
-
-        if (scan) {
-            // leaf loop body, search.c:55-78: nearest voxel by L1 distance from
-            // the leaf's entry point, first one at distance 0 wins at once
-            bool stop = false;
-            if (in) {
-                float dist = l1(ox, oy, oz, ex, ey, ez);
-                if (dist == 0.0f) {
-                    bx = ex; by = ey; bz = ez; win = (int)vi; stop = true;
-                } else if (dist < best) {
-                    best = dist; bx = ex; by = ey; bz = ez; win = (int)vi;
-                }
-            }
-            vi++;
-            if (stop || vi == vn) {
-                if (win >= 0) {
-                    hit.x = bx; hit.y = by; hit.z = bz;
-                    hit.leaf = vid; hit.slot = (uint32_t)win; hit.rec = vrec;
-                    return true;
-                }
-                scan = false;
-                resume = true;
-            }
-        } else if (!in) {
-            resume = true;
-        } else {
-            uint32_t meta = u1.z, link = u1.w, kind = meta & 3u;
-            if (kind == VOXP_KIND_DENSE) {                      // search.c:31-37
-                hit.x = ex; hit.y = ey; hit.z = ez;
-                hit.leaf = link; hit.slot = 0xFFu; hit.rec = cur;
-                return true;
-            }
-            if (kind == VOXP_KIND_LEAF) {                       // search.c:39-50
-                vn = meta >> 2;
-                if (vn == 0) {
-                    resume = true;
-                } else {
-                    scan = true; vrec = cur; vid = u2.x; cur = link; vi = 0;
-                    best = __int_as_float(0x7f800000); win = -1;
-                    ox = ex; oy = ey; oz = ez;
-                }
-            } else {                                            // inner node
-                if (COUNT) cnt.inner++;
-                float cx = ubf(u2.x), cy = ubf(u2.y), cz = ubf(u2.z);
-                // geom.c:53-65 get_corrected_subspace_idx
-                uint32_t sub = ((cx == ex) ? (dx < 0.0f) : (cx > ex))
-                             | (((cy == ey) ? (dy < 0.0f) : (cy > ey)) << 1)
-                             | (((cz == ez) ? (dz < 0.0f) : (cz > ez)) << 2);
-                uint32_t mask = (meta >> 8) & 0xFFu;
-                // search.c:105-113: the crossings with the three dividing
-                // planes that lie in the box, kept in axis order
-                float qx0, qy0, qz0, qx1, qy1, qz1, qx2, qy2, qz2;
-                bool v0 = hit_plane(0, ex, ey, ez, dx, dy, dz, cx, lx, ly, lz, hx, hy, hz, qx0, qy0, qz0);
-                bool v1 = hit_plane(1, ex, ey, ez, dx, dy, dz, cy, lx, ly, lz, hx, hy, hz, qx1, qy1, qz1);
-                bool v2 = hit_plane(2, ex, ey, ez, dx, dy, dz, cz, lx, ly, lz, hx, hy, hz, qx2, qy2, qz2);
-                int pc = (int)v0 + (int)v1 + (int)v2;
-                // compacted slots a, b, c = first, second, third valid crossing
-                float ax = v0 ? qx0 : (v1 ? qx1 : qx2);
-                float ay = v0 ? qy0 : (v1 ? qy1 : qy2);
-                float az = v0 ? qz0 : (v1 ? qz1 : qz2);
-                int ai = v0 ? 0 : (v1 ? 1 : 2);
-                bool ab1 = v0 && v1;
-                float bxp = ab1 ? qx1 : qx2, byp = ab1 ? qy1 : qy2, bzp = ab1 ? qz1 : qz2;
-                int bi = ab1 ? 1 : 2;
-                float cxp = qx2, cyp = qy2, czp = qz2;
-                int ci = 2;
-                float ma = l1(ex, ey, ez, ax, ay, az);
-                float mb = l1(ex, ey, ez, bxp, byp, bzp);
-                float mc = l1(ex, ey, ez, cxp, cyp, czp);
-                // search.c:115-134: selection sort with immediate swaps on '<'
-                if (pc > 1 && mb < ma) {
-                    float t0 = ax; ax = bxp; bxp = t0; t0 = ay; ay = byp; byp = t0; t0 = az; az = bzp; bzp = t0;
-                    t0 = ma; ma = mb; mb = t0; int ti = ai; ai = bi; bi = ti;
-                }
-                if (pc > 2 && mc < ma) {
-                    float t0 = ax; ax = cxp; cxp = t0; t0 = ay; ay = cyp; cyp = t0; t0 = az; az = czp; czp = t0;
-                    t0 = ma; ma = mc; mc = t0; int ti = ai; ai = ci; ci = ti;
-                }
-                if (pc > 2 && mc < mb) {
-                    float t0 = bxp; bxp = cxp; cxp = t0; t0 = byp; byp = cyp; cyp = t0; t0 = bzp; bzp = czp; czp = t0;
-                    t0 = mb; mb = mc; mc = t0; int ti = bi; bi = ci; ci = ti;
-                }
-                // search.c:137: each crossing flips one octant bit; NULL
-                // children are skipped (they return NULL at once)
-                uint32_t s1 = sub ^ (1u << ai), s2 = s1 ^ (1u << bi), s3 = s2 ^ (1u << ci);
-                bool w1 = pc > 0 && ((mask >> s1) & 1u);
-                bool w2 = pc > 1 && ((mask >> s2) & 1u);
-                bool w3 = pc > 2 && ((mask >> s3) & 1u);
-                int npush = (int)w1 + (int)w2 + (int)w3;
-                if (sp + npush > CAP) { overflow = true; return false; }
-                if (w3) stack[sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s3) - 1u)),
-                                                 __float_as_uint(cxp), __float_as_uint(cyp), __float_as_uint(czp));
-                if (w2) stack[sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s2) - 1u)),
-                                                 __float_as_uint(bxp), __float_as_uint(byp), __float_as_uint(bzp));
-                if (w1) stack[sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s1) - 1u)),
-                                                 __float_as_uint(ax), __float_as_uint(ay), __float_as_uint(az));
-                if ((mask >> sub) & 1u) {                       // search.c:92-93
-                    cur = link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << sub) - 1u));
-                    ox = ex; oy = ey; oz = ez;
-                } else {
-                    resume = true;
-                }
-            }
-        }
-        if (resume) {
-            if (sp == 0) return false;
-            uint4 e = stack[--sp];
-            cur = e.x;
-            ox = ubf(e.y); oy = ubf(e.z); oz = ubf(e.w);
+        int r = ray_step<CAP, COUNT>(t, s, stack, hit, cnt);
+        if (r != STEP_MORE) {
+            if (r == STEP_ERROR) overflow = true;
+            return r == STEP_HIT;
         }
     }
 }

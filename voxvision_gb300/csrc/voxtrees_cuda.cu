@@ -15,7 +15,9 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -34,6 +36,7 @@ using vox::TileOrder;
 using vox::centre_out;
 using vox::DevTree;
 using vox::RayHit;
+using vox::FramePlan;
 
 namespace {
 
@@ -109,29 +112,76 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
     if (COUNT) add_counts(counts, c);
 }
 
+// vox_render BEST (renderer.c:200-319, branch :308): camera ray, search and
+// colour fused, one thread per pixel.  A warp covers an 8x4 pixel tile, a
+// block 16x8, so the rays of a warp are neighbours and walk the same nodes.
+//
+// Only the blocks of the screen rectangle that the tree's bounding box can
+// project into are traced (FramePlan, planned on the host); they are issued
+// outward from where the tree's centre projects, so the rays that walk the
+// tree longest start first.  The blocks after them clear the rest of the
+// frame: those pixels are misses.
+//
+// Overlap with the previous kernel of the stream (PDL): the kernel is
+// launched with programmatic stream serialisation and lets its own successor
+// start as soon as all its blocks are running (launch_dependents).  Before
+// griddepcontrol.wait it reads only the tree's pool (written once, at upload,
+// before the upload returns) and its parameters; the texture, the frame, the
+// status word and the counters are touched only after the wait, which
+// returns once the previous kernel has completed and its memory is visible.
+// So the traversal of this frame runs in the tail of the previous one while
+// every read and write of stream-ordered memory keeps the stream's order.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <int CAP, bool COUNT>
-__global__ void __launch_bounds__(128) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
-                                                     uint32_t h, TileOrder ord,
-                                                     const uint8_t *__restrict__ tex,
+__global__ void __launch_bounds__(128) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
+                                                     FramePlan p, const uint8_t *__restrict__ tex,
                                                      uint32_t *__restrict__ argb,
                                                      unsigned long long *__restrict__ counts,
                                                      uint32_t *__restrict__ status)
 {
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t by = centre_out(blockIdx.x / ord.nbx, ord.cby, ord.nby);
-    uint32_t bx = centre_out(blockIdx.x % ord.nbx, ord.cbx, ord.nbx);
-    uint32_t px = bx * TILE_W + (warp & 1) * 8 + (lane & 7);
-    uint32_t py = by * TILE_H + (warp >> 1) * 4 + (lane >> 3);
+    pdl_launch_dependents();
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (blockIdx.x >= p.ntiles) {
+        // clearing blocks: rows dealt to their warps; a warp's lanes store 16
+        // bytes each when the frame is 16-byte aligned (row starts and x0, x1
+        // then are: w is a multiple of 16, x0 and x1 of 8)
+        pdl_wait();
+        if (COUNT) return;
+        const bool vec = (reinterpret_cast<uintptr_t>(argb) & 15u) == 0;
+        const uint32_t nw = (gridDim.x - p.ntiles) * 4u;
+        for (uint32_t y = (blockIdx.x - p.ntiles) * 4u + warp; y < h; y += nw) {
+            uint32_t *row = argb + (size_t)y * w;
+            uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
+            if (y >= p.y0 && y < p.y1) { b0 = p.x0; a1 = p.x1; b1 = w; }
+            if (vec) {
+                uint4 *r4 = reinterpret_cast<uint4 *>(row);
+                for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+                for (uint32_t i = a1 / 4 + lane; i < b1 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                for (uint32_t i = a0 + lane; i < b0; i += 32) row[i] = 0u;
+                for (uint32_t i = a1 + lane; i < b1; i += 32) row[i] = 0u;
+            }
+        }
+        return;
+    }
+    uint32_t by = centre_out(blockIdx.x / p.ntx, p.cty, p.nty);
+    uint32_t bx = centre_out(blockIdx.x % p.ntx, p.ctx, p.ntx);
+    uint32_t px = p.x0 + bx * TILE_W + (warp & 1) * 8 + (lane & 7);
+    uint32_t py = p.y0 + by * TILE_H + (warp >> 1) * 4 + (lane >> 3);
     Counts c{0, 0, 0};
-    bool overflow = false;
-    if (px < w && py < h) {
+    bool overflow = false, hit = false, mine = px < p.x1 && py < p.y1;
+    RayHit hh;
+    if (mine) {
         float dx, dy, dz;
         vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
-        RayHit hh;
-        bool hit = false;
         if (t.root != VOXP_EMPTY)
-            hit = vox::trace_ray<CAP, COUNT>(t, t.root, cam.position[0], cam.position[1],
-                                             cam.position[2], dx, dy, dz, hh, c, overflow);
+            hit = vox::trace_ray<CAP, COUNT>(t, t.root, cam.position[0], cam.position[1], cam.position[2],
+                                             dx, dy, dz, hh, c, overflow);
+    }
+    pdl_wait();
+    if (mine) {
         if (!COUNT) argb[(size_t)py * w + px] = hit ? vox::texel_color(tex, t, hh.x, hh.y, hh.z) : 0u;
         if (overflow) atomicOr(status, 1u);
     }
@@ -280,18 +330,36 @@ cudaError_t launch_balls(const vox_cuda_tree *t, const float *c, const float *r,
     return cudaGetLastError();
 }
 
+// Process-wide settings of the BEST frame kernel (vox_cuda_render_set_config).
+std::atomic<uint32_t> g_render_cull{1}, g_render_overlap{1};
+
 template <bool COUNT>
 cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                           const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s)
 {
-    TileOrder ord = tile_order(t, cam, w, h);
-    dim3 block(128), grid(ord.nbx * ord.nby);
+    // the counting kernel counts the reference's work: every pixel traced
+    FramePlan p;
+    plan_frame(t, cam, w, h, !COUNT && g_render_cull.load(), p);
+    void (*kern)(DevTree, vox_cuda_camera, uint32_t, uint32_t, FramePlan, const uint8_t *, uint32_t *,
+                 unsigned long long *, uint32_t *);
     switch (t->cap_class) {
-    case 0: render_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
-    case 1: render_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
-    default: render_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, cam, w, h, ord, tex, argb, counts, t->d_status); break;
+    case 0: kern = render_kernel<CAP0, COUNT>; break;
+    case 1: kern = render_kernel<CAP1, COUNT>; break;
+    default: kern = render_kernel<CAP2, COUNT>; break;
     }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(p.ntiles + p.nclear);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = g_render_overlap.load() ? 1 : 0;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, t->dev, cam, w, h, p, tex, argb, counts, t->d_status);
     count_launch();
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
@@ -379,6 +447,156 @@ TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_
 }
 
 
+// Linear map of screen2world: direction = M * (mul*sx - xsub, 1, ysub' - mul*sy)
+// with ysub' = ysub for the simple camera (quaternion rotation, every term of
+// which is linear in the vector) and ysub + k for the doom camera (rotation
+// by phi about z).  Returns false for a camera whose state is not finite.
+static bool camera_map(const vox_cuda_camera &cam, double M[3][3], double &ysub)
+{
+    const float f[] = {cam.position[0], cam.position[1], cam.position[2], cam.rotation[0], cam.rotation[1],
+                       cam.rotation[2], cam.rotation[3], cam.mul, cam.xsub, cam.ysub, cam.sinphi,
+                       cam.cosphi, cam.k};
+    for (float x : f)
+        if (!std::isfinite(x)) return false;
+    ysub = cam.ysub;
+    if (cam.kind == VOX_CUDA_CAMERA_DOOM) {
+        double c = cam.cosphi, sn = cam.sinphi;
+        double D[3][3] = {{c, -sn, 0}, {sn, c, 0}, {0, 0, 1}};
+        std::memcpy(M, D, sizeof D);
+        ysub += cam.k;
+        return true;
+    }
+    double qw = cam.rotation[0], qi = cam.rotation[1], qj = cam.rotation[2], qk = cam.rotation[3];
+    for (int j = 0; j < 3; j++) {
+        double v[3] = {0, 0, 0};
+        v[j] = 1;
+        double t0 = 2 * (qj * v[2] - qk * v[1]), t1 = 2 * (qk * v[0] - qi * v[2]), t2 = 2 * (qi * v[1] - qj * v[0]);
+        M[0][j] = v[0] + qw * t0 + (qj * t2 - qk * t1);
+        M[1][j] = v[1] + qw * t1 + (qk * t0 - qi * t2);
+        M[2][j] = v[2] + qw * t2 + (qi * t1 - qj * t0);
+    }
+    return true;
+}
+
+// The rectangle of a frame that can see the box bbox (min xyz, max xyz).
+// The eight corners of the box, widened by a margin far above the rounding
+// of the float search, are projected through the inverse of the camera map;
+// the pixels whose rays can enter the box lie in the convex hull of the
+// projections (the rays of a frame are an affine family of directions from
+// one point), so the rectangle around them, widened by two pixels plus the
+// rounding of the float ray directions, holds every pixel that can hit.  A
+// box wholly behind the camera plane gives no pixel (every ray points
+// forward); one with a corner at or behind the plane (the camera in or next
+// to the box), a degenerate or non-finite camera give the whole frame.  The rectangle is
+// rounded out to multiples of 8 x 4 pixels; [0,0)x[0,0) when no pixel can
+// see the box.  centre_px receives where the box's centre projects (the
+// frame centre when it lies behind the camera).
+static void frame_rect(const float bbox[6], const vox_cuda_camera &cam, uint32_t w, uint32_t h,
+                       uint32_t rect[4], double centre_px[2])
+{
+    uint32_t x0 = 0, y0 = 0, x1 = w, y1 = h;
+    centre_px[0] = 0.5 * w;
+    centre_px[1] = 0.5 * h;
+    bool empty = false;
+    double M[3][3], ysub = 0;
+    if (camera_map(cam, M, ysub) && cam.mul != 0.0f && std::isfinite(bbox[0] + bbox[1] + bbox[2] +
+                                                                    bbox[3] + bbox[4] + bbox[5])) {
+        double det = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                     M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                     M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+        double nm = 0;
+        for (auto &r : M)
+            for (double x : r) nm += x * x;
+        if (std::fabs(det) > 1e-9 * nm * std::sqrt(nm)) {
+            double Mi[3][3];
+            Mi[0][0] = (M[1][1] * M[2][2] - M[1][2] * M[2][1]) / det;
+            Mi[0][1] = (M[0][2] * M[2][1] - M[0][1] * M[2][2]) / det;
+            Mi[0][2] = (M[0][1] * M[1][2] - M[0][2] * M[1][1]) / det;
+            Mi[1][0] = (M[1][2] * M[2][0] - M[1][0] * M[2][2]) / det;
+            Mi[1][1] = (M[0][0] * M[2][2] - M[0][2] * M[2][0]) / det;
+            Mi[1][2] = (M[0][2] * M[1][0] - M[0][0] * M[1][2]) / det;
+            Mi[2][0] = (M[1][0] * M[2][1] - M[1][1] * M[2][0]) / det;
+            Mi[2][1] = (M[0][1] * M[2][0] - M[0][0] * M[2][1]) / det;
+            Mi[2][2] = (M[0][0] * M[1][1] - M[0][1] * M[1][0]) / det;
+            double nmi = 0;
+            for (auto &r : Mi)
+                for (double x : r) nmi += x * x;
+            const double o[3] = {cam.position[0], cam.position[1], cam.position[2]};
+            double big = 1.0;
+            for (int i = 0; i < 3; i++)
+                big = std::max({big, std::fabs(o[i]), std::fabs((double)bbox[i]), std::fabs((double)bbox[3 + i])});
+            const double mw = 1e-4 * big;                        // world margin
+            const double mul = cam.mul, xsub = cam.xsub;
+            const double vmax = 1 + std::fabs(xsub) + std::fabs(ysub) + std::fabs(mul) * ((double)w + h);
+            const double mpx = 2 + 1e-5 * vmax * std::sqrt(nm * nmi) / std::fabs(mul);   // pixel margin
+            double sxmin = INFINITY, sxmax = -INFINITY, symin = INFINITY, symax = -INFINITY;
+            bool bounded = true;
+            int behind = 0;
+            for (int c = 0; c < 8; c++) {
+                double P[3], a[3];
+                for (int i = 0; i < 3; i++)
+                    P[i] = ((c >> i) & 1) ? (double)bbox[3 + i] + mw : (double)bbox[i] - mw;
+                for (int i = 0; i < 3; i++)
+                    a[i] = Mi[i][0] * (P[0] - o[0]) + Mi[i][1] * (P[1] - o[1]) + Mi[i][2] * (P[2] - o[2]);
+                double na = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+                if (a[1] < -1e-6 * na) behind++;
+                if (!(a[1] > 1e-6 * na)) { bounded = false; continue; }
+                double sx = (a[0] / a[1] + xsub) / mul, sy = (ysub - a[2] / a[1]) / mul;
+                sxmin = std::min(sxmin, sx); sxmax = std::max(sxmax, sx);
+                symin = std::min(symin, sy); symax = std::max(symax, sy);
+            }
+            if (behind == 8) {
+                empty = true;          // the whole box lies behind the camera plane
+            } else if (bounded && std::isfinite(sxmin + sxmax + symin + symax)) {
+                double xa = std::floor(sxmin - mpx), xb = std::ceil(sxmax + mpx);
+                double ya = std::floor(symin - mpx), yb = std::ceil(symax + mpx);
+                if (xb < 0 || yb < 0 || xa > w - 1.0 || ya > h - 1.0) {
+                    empty = true;
+                } else {
+                    xa = std::max(xa, 0.0); ya = std::max(ya, 0.0);
+                    xb = std::min(xb, w - 1.0); yb = std::min(yb, h - 1.0);
+                    x0 = (uint32_t)xa & ~7u; y0 = (uint32_t)ya & ~3u;
+                    x1 = std::min(w, ((uint32_t)xb & ~7u) + 8u);
+                    y1 = std::min(h, ((uint32_t)yb & ~3u) + 4u);
+                }
+            }
+            double C[3], a[3];
+            for (int i = 0; i < 3; i++) C[i] = 0.5 * ((double)bbox[i] + bbox[3 + i]) - o[i];
+            for (int i = 0; i < 3; i++) a[i] = Mi[i][0] * C[0] + Mi[i][1] * C[1] + Mi[i][2] * C[2];
+            if (a[1] > 1e-9) {
+                centre_px[0] = (a[0] / a[1] + xsub) / mul;
+                centre_px[1] = (ysub - a[2] / a[1]) / mul;
+            }
+        }
+    }
+    if (empty) x0 = x1 = y0 = y1 = 0;
+    rect[0] = x0; rect[1] = y0; rect[2] = x1; rect[3] = y1;
+}
+
+void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h, bool cull,
+                FramePlan &p)
+{
+    uint32_t r[4] = {0, 0, w, h};
+    double c[2] = {0.5 * w, 0.5 * h};
+    if (t->dev.root == VOXP_EMPTY) {
+        if (cull) r[2] = r[3] = 0;
+    } else {
+        frame_rect(t->bbox, cam, w, h, r, c);
+        if (!cull) { r[0] = r[1] = 0; r[2] = w; r[3] = h; }
+    }
+    p.x0 = r[0]; p.y0 = r[1]; p.x1 = r[2]; p.y1 = r[3];
+    p.ntx = (p.x1 - p.x0 + TILE_W - 1) / TILE_W;
+    p.nty = (p.y1 - p.y0 + TILE_H - 1) / TILE_H;
+    p.ntiles = p.ntx * p.nty;
+    double tx = (c[0] - p.x0) / TILE_W, ty = (c[1] - p.y0) / TILE_H;
+    p.ctx = (p.ntx && tx >= 0) ? (uint32_t)std::min(tx, p.ntx - 1.0) : 0;   // NaN -> 0
+    p.cty = (p.nty && ty >= 0) ? (uint32_t)std::min(ty, p.nty - 1.0) : 0;
+    // clearing blocks: one warp per row up to 64 blocks, none when nothing is left
+    uint64_t outside = (uint64_t)w * h - (uint64_t)(p.x1 - p.x0) * (p.y1 - p.y0);
+    p.nclear = outside ? std::min<uint32_t>(64u, (h + 3) / 4) : 0;
+    if (p.ntiles + p.nclear == 0) p.nclear = 1;
+}
+
 // ======================================================================== API
 
 EXPORT const char *vox_cuda_strerror(int code)
@@ -434,6 +652,10 @@ EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out
         e = cudaMemcpy(t->d_pool, t->flat.units.data(), t->pool_bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nodes)
         e = cudaMemcpy(t->d_rec_of_id, t->flat.rec_of_id.data(), nodes * 4, cudaMemcpyHostToDevice);
+    // A copy from pageable memory may still be in flight when cudaMemcpy
+    // returns; the pool must be complete before any kernel on any stream
+    // reads it (the frame kernel reads it ahead of its stream dependency).
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
     if (e != cudaSuccess) {
         cudaFree(t->d_pool); cudaFree(t->d_rec_of_id); cudaFree(t->d_status);
         delete t;
@@ -649,6 +871,33 @@ EXPORT int vox_cuda_ball_counts_device(const vox_cuda_tree *t, const float *c, c
     if (!t || !counts || (n && (!c || !r))) return VOX_CUDA_EINVAL;
     return status_of(launch_balls<true>(t, c, r, n, nullptr,
                                         reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
+}
+
+EXPORT int vox_cuda_frame_rect(const float *bbox, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                               uint32_t *rect)
+{
+    if (!bbox || !cam || !rect) return VOX_CUDA_EINVAL;
+    if (cam->kind != VOX_CUDA_CAMERA_SIMPLE && cam->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+    if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
+    double c[2];
+    frame_rect(bbox, *cam, w, h, rect, c);
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_render_set_config(const vox_cuda_render_config *cfg)
+{
+    if (!cfg || cfg->cull > 1 || cfg->overlap > 1) return VOX_CUDA_EINVAL;
+    g_render_cull.store(cfg->cull);
+    g_render_overlap.store(cfg->overlap);
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_render_get_config(vox_cuda_render_config *cfg)
+{
+    if (!cfg) return VOX_CUDA_EINVAL;
+    cfg->cull = g_render_cull.load();
+    cfg->overlap = g_render_overlap.load();
+    return VOX_CUDA_OK;
 }
 
 static bool valid_quality(unsigned int q)
