@@ -164,6 +164,65 @@ __device__ __forceinline__ void ray_begin(RaySearch &s, uint32_t start, float ox
     s.steps = 0;
 }
 
+/* search.c:105-148: the crossings of the ray (from the entry point e of an
+ * inner node) with the node's three dividing planes that lie in its box,
+ * sorted by L1 distance from e with the reference's selection sort
+ * (:115-134, immediate swaps on '<'); each crossing flips one octant bit of
+ * the entry octant `sub` (:137).  Pushes the crossing children so that they
+ * pop in visiting order (NULL children are skipped: they return NULL at
+ * once).  Returns false when the stack would overflow. */
+template <int CAP>
+__device__ __forceinline__ bool push_crossings(RaySearch &s, uint4 (&stack)[CAP], float ex, float ey, float ez,
+                                               float lx, float ly, float lz, float hx, float hy, float hz,
+                                               float cx, float cy, float cz, uint32_t sub, uint32_t mask,
+                                               uint32_t link)
+{
+    const float dx = s.dx, dy = s.dy, dz = s.dz;
+    float qx0, qy0, qz0, qx1, qy1, qz1, qx2, qy2, qz2;
+    bool v0 = hit_plane(0, ex, ey, ez, dx, dy, dz, cx, lx, ly, lz, hx, hy, hz, qx0, qy0, qz0);
+    bool v1 = hit_plane(1, ex, ey, ez, dx, dy, dz, cy, lx, ly, lz, hx, hy, hz, qx1, qy1, qz1);
+    bool v2 = hit_plane(2, ex, ey, ez, dx, dy, dz, cz, lx, ly, lz, hx, hy, hz, qx2, qy2, qz2);
+    int pc = (int)v0 + (int)v1 + (int)v2;
+    // compacted slots a, b, c = first, second, third valid crossing
+    float ax = v0 ? qx0 : (v1 ? qx1 : qx2);
+    float ay = v0 ? qy0 : (v1 ? qy1 : qy2);
+    float az = v0 ? qz0 : (v1 ? qz1 : qz2);
+    int ai = v0 ? 0 : (v1 ? 1 : 2);
+    bool ab1 = v0 && v1;
+    float bxp = ab1 ? qx1 : qx2, byp = ab1 ? qy1 : qy2, bzp = ab1 ? qz1 : qz2;
+    int bi = ab1 ? 1 : 2;
+    float cxp = qx2, cyp = qy2, czp = qz2;
+    int ci = 2;
+    float ma = l1(ex, ey, ez, ax, ay, az);
+    float mb = l1(ex, ey, ez, bxp, byp, bzp);
+    float mc = l1(ex, ey, ez, cxp, cyp, czp);
+    if (pc > 1 && mb < ma) {
+        float t0 = ax; ax = bxp; bxp = t0; t0 = ay; ay = byp; byp = t0; t0 = az; az = bzp; bzp = t0;
+        t0 = ma; ma = mb; mb = t0; int ti = ai; ai = bi; bi = ti;
+    }
+    if (pc > 2 && mc < ma) {
+        float t0 = ax; ax = cxp; cxp = t0; t0 = ay; ay = cyp; cyp = t0; t0 = az; az = czp; czp = t0;
+        t0 = ma; ma = mc; mc = t0; int ti = ai; ai = ci; ci = ti;
+    }
+    if (pc > 2 && mc < mb) {
+        float t0 = bxp; bxp = cxp; cxp = t0; t0 = byp; byp = cyp; cyp = t0; t0 = bzp; bzp = czp; czp = t0;
+        t0 = mb; mb = mc; mc = t0; int ti = bi; bi = ci; ci = ti;
+    }
+    uint32_t s1 = sub ^ (1u << ai), s2 = s1 ^ (1u << bi), s3 = s2 ^ (1u << ci);
+    bool w1 = pc > 0 && ((mask >> s1) & 1u);
+    bool w2 = pc > 1 && ((mask >> s2) & 1u);
+    bool w3 = pc > 2 && ((mask >> s3) & 1u);
+    int npush = (int)w1 + (int)w2 + (int)w3;
+    if (s.sp + npush > CAP) return false;
+    if (w3) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s3) - 1u)),
+                                       __float_as_uint(cxp), __float_as_uint(cyp), __float_as_uint(czp));
+    if (w2) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s2) - 1u)),
+                                       __float_as_uint(bxp), __float_as_uint(byp), __float_as_uint(bzp));
+    if (w1) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s1) - 1u)),
+                                       __float_as_uint(ax), __float_as_uint(ay), __float_as_uint(az));
+    return true;
+}
+
 template <int CAP, bool COUNT>
 __device__ __forceinline__ int ray_step(const DevTree &t, RaySearch &s, uint4 (&stack)[CAP], RayHit &hit,
                                         Counts &cnt)
@@ -239,53 +298,8 @@ __device__ __forceinline__ int ray_step(const DevTree &t, RaySearch &s, uint4 (&
                          | (((cy == ey) ? (dy < 0.0f) : (cy > ey)) << 1)
                          | (((cz == ez) ? (dz < 0.0f) : (cz > ez)) << 2);
             uint32_t mask = (meta >> 8) & 0xFFu;
-            // search.c:105-113: the crossings with the three dividing
-            // planes that lie in the box, kept in axis order
-            float qx0, qy0, qz0, qx1, qy1, qz1, qx2, qy2, qz2;
-            bool v0 = hit_plane(0, ex, ey, ez, dx, dy, dz, cx, lx, ly, lz, hx, hy, hz, qx0, qy0, qz0);
-            bool v1 = hit_plane(1, ex, ey, ez, dx, dy, dz, cy, lx, ly, lz, hx, hy, hz, qx1, qy1, qz1);
-            bool v2 = hit_plane(2, ex, ey, ez, dx, dy, dz, cz, lx, ly, lz, hx, hy, hz, qx2, qy2, qz2);
-            int pc = (int)v0 + (int)v1 + (int)v2;
-            // compacted slots a, b, c = first, second, third valid crossing
-            float ax = v0 ? qx0 : (v1 ? qx1 : qx2);
-            float ay = v0 ? qy0 : (v1 ? qy1 : qy2);
-            float az = v0 ? qz0 : (v1 ? qz1 : qz2);
-            int ai = v0 ? 0 : (v1 ? 1 : 2);
-            bool ab1 = v0 && v1;
-            float bxp = ab1 ? qx1 : qx2, byp = ab1 ? qy1 : qy2, bzp = ab1 ? qz1 : qz2;
-            int bi = ab1 ? 1 : 2;
-            float cxp = qx2, cyp = qy2, czp = qz2;
-            int ci = 2;
-            float ma = l1(ex, ey, ez, ax, ay, az);
-            float mb = l1(ex, ey, ez, bxp, byp, bzp);
-            float mc = l1(ex, ey, ez, cxp, cyp, czp);
-            // search.c:115-134: selection sort with immediate swaps on '<'
-            if (pc > 1 && mb < ma) {
-                float t0 = ax; ax = bxp; bxp = t0; t0 = ay; ay = byp; byp = t0; t0 = az; az = bzp; bzp = t0;
-                t0 = ma; ma = mb; mb = t0; int ti = ai; ai = bi; bi = ti;
-            }
-            if (pc > 2 && mc < ma) {
-                float t0 = ax; ax = cxp; cxp = t0; t0 = ay; ay = cyp; cyp = t0; t0 = az; az = czp; czp = t0;
-                t0 = ma; ma = mc; mc = t0; int ti = ai; ai = ci; ci = ti;
-            }
-            if (pc > 2 && mc < mb) {
-                float t0 = bxp; bxp = cxp; cxp = t0; t0 = byp; byp = cyp; cyp = t0; t0 = bzp; bzp = czp; czp = t0;
-                t0 = mb; mb = mc; mc = t0; int ti = bi; bi = ci; ci = ti;
-            }
-            // search.c:137: each crossing flips one octant bit; NULL
-            // children are skipped (they return NULL at once)
-            uint32_t s1 = sub ^ (1u << ai), s2 = s1 ^ (1u << bi), s3 = s2 ^ (1u << ci);
-            bool w1 = pc > 0 && ((mask >> s1) & 1u);
-            bool w2 = pc > 1 && ((mask >> s2) & 1u);
-            bool w3 = pc > 2 && ((mask >> s3) & 1u);
-            int npush = (int)w1 + (int)w2 + (int)w3;
-            if (s.sp + npush > CAP) return STEP_ERROR;
-            if (w3) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s3) - 1u)),
-                                                 __float_as_uint(cxp), __float_as_uint(cyp), __float_as_uint(czp));
-            if (w2) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s2) - 1u)),
-                                                 __float_as_uint(bxp), __float_as_uint(byp), __float_as_uint(bzp));
-            if (w1) stack[s.sp++] = make_uint4(link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << s1) - 1u)),
-                                                 __float_as_uint(ax), __float_as_uint(ay), __float_as_uint(az));
+            if (!push_crossings<CAP>(s, stack, ex, ey, ez, lx, ly, lz, hx, hy, hz, cx, cy, cz, sub, mask, link))
+                return STEP_ERROR;
             if ((mask >> sub) & 1u) {                       // search.c:92-93
                 s.cur = link + VOXP_REC_UNITS * (uint32_t)__popc(mask & ((1u << sub) - 1u));
                 s.ox = ex; s.oy = ey; s.oz = ez;
