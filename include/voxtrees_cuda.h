@@ -124,7 +124,10 @@ int vox_cuda_ball_batch_device(const vox_cuda_tree *tree, const float *centres,
  * lookup fused in one kernel, written to a linear w x h ARGB8888 frame
  * (pixel (x, y) at argb[y * w + x]; misses are 0).  texture: the 32^3 u8
  * colour texture (index x*1024 + y*32 + z).  w must be a multiple of 16 and
- * h of 4 (renderer.c:97-100).
+ * h of 4 (renderer.c:97-100).  vox_cuda_render: a page-locked frame
+ * (cudaHostAlloc, cudaHostRegister) is drawn in place by the kernel, whose
+ * stores cross the host link while the frame is traced; a pageable one is
+ * drawn on the device and copied out.
  * Replaces vox_render + vox_redraw with quality VOX_QUALITY_BEST
  * (src/voxrnd/renderer.c:200-327). */
 int vox_cuda_render(const vox_cuda_tree *tree, const vox_cuda_camera *camera,

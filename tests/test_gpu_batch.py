@@ -116,3 +116,46 @@ def test_batch_rejects_bad_jobs(scene):
     assert e.value.code == -7
     with pytest.raises(vg.VoxCudaError):
         vg.FrameBatch(jobs, vg.BatchConfig(12, 4, 1, 4))
+
+
+def test_culled_rectangles_follow_camera_changes(scene):
+    """Cameras inside a tree's box (whole frame traced), looking away from it
+    (nothing traced, whole frame cleared), far away and off-centre: every
+    frame equals the plain call's with the output full of garbage before each
+    replay, also after set_camera changes how many tiles each frame has."""
+    vg, hosts, devs, jobs, meta, tex = scene
+    from voxvision_gb300.cameras import HostCamera
+    poses = [((30, 35, 40), (60, 60, 60)),          # inside the 64^3 box
+             ((32, 250, 30), (32, 500, 30)),       # looking away
+             ((32, -900, 32), (32, 32, 32)),       # far: a few tiles
+             ((140, -40, 60), (90, 90, 20))]       # tree partly off-screen
+    kinds = [0, 1, 0, 1]
+    mk = []
+    for i, ((pos, at), kind) in enumerate(zip(poses, kinds)):
+        w, h = [(336, 200), (64, 32), (320, 240), (160, 120)][i]
+        cam = HostCamera(kind)
+        cam.set_window_size(w, h)
+        cam.set_position(pos)
+        cam.look_at(np.asarray(at, np.float32))
+        out = torch.zeros(w * h, dtype=torch.int32, device="cuda")
+        mk.append((devs[0], cam.gpu_struct(), w, h, tex, out))
+    b = vg.FrameBatch(mk)
+    for rnd in range(3):
+        for j in mk:
+            j[5].fill_(0x5A5A5A5A)
+        b.launch()
+        torch.cuda.synchronize()
+        for j in mk:
+            assert np.array_equal(j[5].cpu().numpy(), _plain(vg, j)), f"round {rnd}"
+        # rotate the poses among the frames (each keeps its size)
+        nxt = []
+        for i, j in enumerate(mk):
+            pos, at = poses[(i + rnd + 1) % 4]
+            cam = HostCamera(kinds[(i + rnd + 1) % 4])
+            cam.set_window_size(j[2], j[3])
+            cam.set_position(pos)
+            cam.look_at(np.asarray(at, np.float32))
+            b.set_camera(i, cam.gpu_struct())
+            nxt.append((j[0], cam.gpu_struct(), j[2], j[3], j[4], j[5]))
+        mk = nxt
+    b.close()

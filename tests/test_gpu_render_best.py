@@ -163,6 +163,32 @@ def test_stream_order_holds_when_frames_overlap(tree64):
         assert np.array_equal(img, ref), f"frame {i}: {(img != ref).sum()} pixels differ"
 
 
+def test_host_frame_pinned_and_pageable(tree256):
+    """vox_cuda_render into a page-locked host frame (drawn in place over the
+    host link) and into a pageable one (drawn on the device, copied out): both
+    equal the oracle's frame, every pixel written."""
+    import ctypes as C
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import orbit_camera
+    ht, dt = tree256
+    vg().set_render_config(1, 1)
+    tex = wl.texture32(7)
+    L = vg().lib()
+    for frame in (3, 70):
+        cam = orbit_camera(frame, 120, 1920, 1080, (128, 128, 128), 1.5 * 256 * 3 ** 0.5)
+        ref, _ = orc.render_best(ht.ptr, cam.state(), 1920, 1080, tex)
+        pinned = torch.full((1920 * 1080,), GARBAGE, dtype=torch.int32).pin_memory()
+        pageable = np.full(1920 * 1080, GARBAGE, np.uint32)
+        cs = cam.gpu_struct()
+        for buf in (pinned.data_ptr(), pageable.ctypes.data):
+            rc = L.vox_cuda_render(dt.h, C.byref(cs), 1920, 1080, tex.ctypes.data_as(C.c_void_p),
+                                   C.c_void_p(buf), None)
+            assert rc == 0
+        img = pinned.numpy().view(np.uint32).reshape(1080, 1920)
+        assert np.array_equal(img, ref), f"pinned: {(img != ref).sum()} pixels differ"
+        assert np.array_equal(pageable.reshape(1080, 1920), ref)
+
+
 def test_setting_api_validates():
     with pytest.raises(vg().VoxCudaError):
         vg().set_render_config(2, 1)

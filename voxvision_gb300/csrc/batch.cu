@@ -36,6 +36,13 @@ namespace {
 
 constexpr uint32_t MAX_JOBS = 1024;
 
+// Device job table of one launch: a head, then one entry per frame in queue
+// order.  The head carries the queue's totals, so a captured graph stays
+// valid when cameras change the number of tiles between replays.
+struct alignas(16) BatchHead {
+    uint32_t njobs, total_tiles, total_clear, pad;
+};
+
 struct BatchJobDev {
     DevTree tree;
     vox_cuda_camera cam;
@@ -43,13 +50,18 @@ struct BatchJobDev {
     uint32_t *argb;
     uint32_t *status;
     uint32_t w, h;
-    uint32_t ntx, nty;      // tiles across / down for the batch's tile shape
-    uint32_t ctx, cty;      // tile where the tree's centre projects
-    uint32_t tile_base;     // first queue index of this frame's tiles
-    uint32_t pad;
+    uint32_t x0, y0, x1, y1;  // traced rectangle, rounded out to the tile shape
+    uint32_t ntx, nty;        // tiles across / down of the rectangle
+    uint32_t ctx, cty;        // tile where the tree's centre projects
+    uint32_t tile_base;       // first queue index of this frame's tiles
+    uint32_t clear_base;      // first clearing item of this frame (after all tiles)
 };
 
-// Queue index -> frame: the last job whose tile_base is <= tile.
+// Rows of the frame outside the traced rectangle that one clearing item zeroes.
+constexpr uint32_t CLEAR_ROWS = 8;
+
+// Queue index -> frame: the last job whose base is <= item (frames with no
+// item of that kind share their base with the next frame and are skipped).
 __device__ __forceinline__ uint32_t find_job(const uint32_t *base, uint32_t njobs, uint32_t tile)
 {
     uint32_t lo = 0, hi = njobs;
@@ -61,48 +73,109 @@ __device__ __forceinline__ uint32_t find_job(const uint32_t *base, uint32_t njob
 }
 
 template <int CAP, int TW, int TH>
-__global__ void __launch_bounds__(128) batch_kernel(const BatchJobDev *__restrict__ jobs, uint32_t njobs,
-                                                    uint32_t total_tiles, uint32_t grab,
+__global__ void __launch_bounds__(128) batch_kernel(const BatchHead *__restrict__ head, uint32_t grab,
                                                     uint32_t *__restrict__ counter)
 {
     constexpr int RPT = TW * TH / 32;   // rays per thread per tile
-    __shared__ uint32_t base[MAX_JOBS];
-    for (uint32_t i = threadIdx.x; i < njobs; i += blockDim.x) base[i] = jobs[i].tile_base;
+    __shared__ uint32_t tbase[MAX_JOBS], cbase[MAX_JOBS];
+    const BatchJobDev *jobs = reinterpret_cast<const BatchJobDev *>(head + 1);
+    const uint32_t njobs = head->njobs, ntiles = head->total_tiles, total = ntiles + head->total_clear;
+    for (uint32_t i = threadIdx.x; i < njobs; i += blockDim.x) {
+        tbase[i] = jobs[i].tile_base;
+        cbase[i] = jobs[i].clear_base;
+    }
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    const uint32_t lane = threadIdx.x & 31;
     for (;;) {
         uint32_t t0 = 0;
         if (lane == 0) t0 = atomicAdd(counter, grab);
         t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= total_tiles) break;
-        uint32_t t1 = min(t0 + grab, total_tiles);
-        for (uint32_t tile = t0; tile < t1; tile++) {
-            const BatchJobDev &J = jobs[find_job(base, njobs, tile)];
-            uint32_t local = tile - J.tile_base;
-            uint32_t ty = vox::centre_out(local / J.ntx, J.cty, J.nty);
-            uint32_t tx = vox::centre_out(local % J.ntx, J.ctx, J.ntx);
-            const DevTree t = J.tree;
-            const vox_cuda_camera cam = J.cam;
-            const uint32_t w = J.w, h = J.h;
+        if (t0 >= total) break;
+        uint32_t t1 = min(t0 + grab, total);
+        for (uint32_t item = t0; item < t1; item++) {
+            if (item < ntiles) {
+                const BatchJobDev &J = jobs[find_job(tbase, njobs, item)];
+                uint32_t local = item - J.tile_base;
+                uint32_t ty = vox::centre_out(local / J.ntx, J.cty, J.nty);
+                uint32_t tx = vox::centre_out(local % J.ntx, J.ctx, J.ntx);
+                const DevTree t = J.tree;
+                const vox_cuda_camera cam = J.cam;
+                const uint32_t w = J.w, x1 = J.x1, y1 = J.y1;
 #pragma unroll 1
-            for (int r = 0; r < RPT; r++) {
-                uint32_t p = (uint32_t)lane + 32u * (uint32_t)r;
-                uint32_t px = tx * TW + p % TW, py = ty * TH + p / TW;
-                if (px < w && py < h) {
-                    float dx, dy, dz;
-                    vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
-                    RayHit hh;
-                    vox::Counts c{0, 0, 0};
-                    bool overflow = false, hit = false;
-                    if (t.root != VOXP_EMPTY)
-                        hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1],
-                                                         cam.position[2], dx, dy, dz, hh, c, overflow);
-                    J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
-                    if (overflow) atomicOr(J.status, 1u);
+                for (int r = 0; r < RPT; r++) {
+                    uint32_t p = lane + 32u * (uint32_t)r;
+                    uint32_t px = J.x0 + tx * TW + p % TW, py = J.y0 + ty * TH + p / TW;
+                    if (px < x1 && py < y1) {
+                        float dx, dy, dz;
+                        vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
+                        RayHit hh;
+                        vox::Counts c{0, 0, 0};
+                        bool overflow = false, hit = false;
+                        if (t.root != VOXP_EMPTY)
+                            hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1],
+                                                             cam.position[2], dx, dy, dz, hh, c, overflow);
+                        J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
+                        if (overflow) atomicOr(J.status, 1u);
+                    }
+                }
+            } else {
+                // clearing item: CLEAR_ROWS rows, the parts outside the rectangle
+                uint32_t c = item - ntiles;
+                const BatchJobDev &J = jobs[find_job(cbase, njobs, c)];
+                const uint32_t w = J.w, y0r = (c - J.clear_base) * CLEAR_ROWS;
+                const uint32_t yend = min(y0r + CLEAR_ROWS, J.h);
+                const bool vec = (reinterpret_cast<uintptr_t>(J.argb) & 15u) == 0;
+                for (uint32_t y = y0r; y < yend; y++) {
+                    uint32_t *row = J.argb + (size_t)y * w;
+                    uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
+                    if (y >= J.y0 && y < J.y1) { b0 = J.x0; a1 = J.x1; b1 = w; }
+                    if (vec) {
+                        uint4 *r4 = reinterpret_cast<uint4 *>(row);
+                        for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+                        for (uint32_t i = a1 / 4 + lane; i < b1 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+                    } else {
+                        for (uint32_t i = a0 + lane; i < b0; i += 32) row[i] = 0u;
+                        for (uint32_t i = a1 + lane; i < b1; i += 32) row[i] = 0u;
+                    }
                 }
             }
         }
     }
+}
+
+// One frame's table entry for tile shape tw x th: the traced rectangle (the
+// tree's screen rectangle rounded out to whole tiles), its tiles outward from
+// where the tree's centre projects, and a clearing item per CLEAR_ROWS rows
+// unless the rectangle is the whole frame.  Advances the queue totals.
+void fill_job(BatchJobDev &d, const vox_cuda_frame_job &j, uint32_t tw, uint32_t th, BatchHead &head)
+{
+    std::memset(&d, 0, sizeof d);
+    d.tree = j.tree->dev;
+    d.cam = j.camera;
+    d.tex = j.texture;
+    d.argb = j.argb;
+    d.status = j.tree->d_status;
+    d.w = j.w;
+    d.h = j.h;
+    uint32_t r[4];
+    double c[2];
+    frame_rect_of(j.tree, j.camera, j.w, j.h, r, c);
+    if (r[2] > r[0] && r[3] > r[1]) {
+        d.x0 = r[0] / tw * tw;
+        d.y0 = r[1] / th * th;
+        d.x1 = std::min(j.w, (r[2] + tw - 1) / tw * tw);
+        d.y1 = std::min(j.h, (r[3] + th - 1) / th * th);
+        d.ntx = (d.x1 - d.x0 + tw - 1) / tw;
+        d.nty = (d.y1 - d.y0 + th - 1) / th;
+    }
+    double tx = (c[0] - d.x0) / tw, ty = (c[1] - d.y0) / th;
+    d.ctx = (d.ntx && tx >= 0) ? (uint32_t)std::min(tx, d.ntx - 1.0) : 0;   // NaN -> 0
+    d.cty = (d.nty && ty >= 0) ? (uint32_t)std::min(ty, d.nty - 1.0) : 0;
+    d.tile_base = head.total_tiles;
+    head.total_tiles += d.ntx * d.nty;
+    bool whole = d.x0 == 0 && d.y0 == 0 && d.x1 == j.w && d.y1 == j.h;
+    d.clear_base = head.total_clear;
+    head.total_clear += whole ? 0u : (j.h + CLEAR_ROWS - 1) / CLEAR_ROWS;
 }
 
 struct Shape {
@@ -111,16 +184,16 @@ struct Shape {
 const Shape kShapes[] = {{8, 4}, {16, 2}, {32, 1}, {8, 8}, {16, 4}};
 
 template <int CAP>
-cudaError_t launch_batch_cap(const vox_cuda_batch_config &c, const BatchJobDev *jobs, uint32_t njobs,
-                             uint32_t total, uint32_t *counter, int nsm, cudaStream_t s)
+cudaError_t launch_batch_cap(const vox_cuda_batch_config &c, const BatchHead *table, uint32_t *counter, int nsm,
+                             cudaStream_t s)
 {
     dim3 grid(nsm * c.blocks_per_sm), block(128);
     uint32_t g = c.tiles_per_grab;
-    if (c.tile_w == 8 && c.tile_h == 4) batch_kernel<CAP, 8, 4><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
-    else if (c.tile_w == 16 && c.tile_h == 2) batch_kernel<CAP, 16, 2><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
-    else if (c.tile_w == 32 && c.tile_h == 1) batch_kernel<CAP, 32, 1><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
-    else if (c.tile_w == 8 && c.tile_h == 8) batch_kernel<CAP, 8, 8><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
-    else batch_kernel<CAP, 16, 4><<<grid, block, 0, s>>>(jobs, njobs, total, g, counter);
+    if (c.tile_w == 8 && c.tile_h == 4) batch_kernel<CAP, 8, 4><<<grid, block, 0, s>>>(table, g, counter);
+    else if (c.tile_w == 16 && c.tile_h == 2) batch_kernel<CAP, 16, 2><<<grid, block, 0, s>>>(table, g, counter);
+    else if (c.tile_w == 32 && c.tile_h == 1) batch_kernel<CAP, 32, 1><<<grid, block, 0, s>>>(table, g, counter);
+    else if (c.tile_w == 8 && c.tile_h == 8) batch_kernel<CAP, 8, 8><<<grid, block, 0, s>>>(table, g, counter);
+    else batch_kernel<CAP, 16, 4><<<grid, block, 0, s>>>(table, g, counter);
     count_launch();
     return cudaGetLastError();
 }
@@ -141,11 +214,11 @@ struct vox_cuda_batch {
     int cap_class = 0;
     std::vector<vox_cuda_frame_job> jobs;     // caller's jobs, in caller order
     std::vector<uint32_t> order;              // queue position -> caller index
+    BatchHead head{};                         // queue totals of the current cameras
     std::vector<BatchJobDev> table;           // host copy, in queue order
-    BatchJobDev *h_stage = nullptr;           // pinned copy the graph reads
-    BatchJobDev *d_table = nullptr;
+    unsigned char *h_stage = nullptr;         // pinned copy of head + table that the graph reads
+    BatchHead *d_table = nullptr;             // device head + table
     uint32_t *d_counter = nullptr;            // work queue head (scratch)
-    uint32_t total_tiles = 0;
     vox_cuda_batch_config cfg{8, 4, 1, 4};
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -156,36 +229,29 @@ struct vox_cuda_batch {
 
 namespace {
 
+size_t table_bytes(uint32_t njobs) { return sizeof(BatchHead) + (size_t)njobs * sizeof(BatchJobDev); }
+
 void fill_table(vox_cuda_batch *b)
 {
-    uint32_t base = 0;
+    b->head = BatchHead{(uint32_t)b->jobs.size(), 0u, 0u, 0u};
     b->table.resize(b->jobs.size());
-    for (size_t q = 0; q < b->order.size(); q++) {
-        const vox_cuda_frame_job &j = b->jobs[b->order[q]];
-        BatchJobDev &d = b->table[q];
-        std::memset(&d, 0, sizeof d);
-        d.tree = j.tree->dev;
-        d.cam = j.camera;
-        d.tex = j.texture;
-        d.argb = j.argb;
-        d.status = j.tree->d_status;
-        d.w = j.w;
-        d.h = j.h;
-        vox::TileOrder o = tile_order(j.tree, j.camera, j.w, j.h, b->cfg.tile_w, b->cfg.tile_h);
-        d.ntx = o.nbx; d.nty = o.nby; d.ctx = o.cbx; d.cty = o.cby;
-        d.tile_base = base;
-        base += o.nbx * o.nby;
-    }
-    b->total_tiles = base;
+    for (size_t q = 0; q < b->order.size(); q++)
+        fill_job(b->table[q], b->jobs[b->order[q]], b->cfg.tile_w, b->cfg.tile_h, b->head);
+}
+
+// The pinned stage the graph's copy node reads: head, then the table.
+void stage_table(vox_cuda_batch *b)
+{
+    std::memcpy(b->h_stage, &b->head, sizeof(BatchHead));
+    std::memcpy(b->h_stage + sizeof(BatchHead), b->table.data(), b->table.size() * sizeof(BatchJobDev));
 }
 
 cudaError_t launch_kernel(vox_cuda_batch *b, cudaStream_t s)
 {
-    uint32_t n = (uint32_t)b->jobs.size();
     switch (b->cap_class) {
-    case 0: return launch_batch_cap<CAP0>(b->cfg, b->d_table, n, b->total_tiles, b->d_counter, b->nsm, s);
-    case 1: return launch_batch_cap<CAP1>(b->cfg, b->d_table, n, b->total_tiles, b->d_counter, b->nsm, s);
-    default: return launch_batch_cap<CAP2>(b->cfg, b->d_table, n, b->total_tiles, b->d_counter, b->nsm, s);
+    case 0: return launch_batch_cap<CAP0>(b->cfg, b->d_table, b->d_counter, b->nsm, s);
+    case 1: return launch_batch_cap<CAP1>(b->cfg, b->d_table, b->d_counter, b->nsm, s);
+    default: return launch_batch_cap<CAP2>(b->cfg, b->d_table, b->d_counter, b->nsm, s);
     }
 }
 
@@ -202,10 +268,10 @@ int build_graph(vox_cuda_batch *b)
 {
     drop_graph(b);
     fill_table(b);
-    std::memcpy(b->h_stage, b->table.data(), b->table.size() * sizeof(BatchJobDev));
+    stage_table(b);
     cudaStream_t s = b->cap_stream;
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return VOX_CUDA_ECUDA;
-    cudaError_t e = cudaMemcpyAsync(b->d_table, b->h_stage, b->table.size() * sizeof(BatchJobDev),
+    cudaError_t e = cudaMemcpyAsync(b->d_table, b->h_stage, table_bytes((uint32_t)b->table.size()),
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
     if (e == cudaSuccess) e = launch_kernel(b, s);
@@ -263,7 +329,7 @@ EXPORT int vox_cuda_batch_create(const vox_cuda_frame_job *jobs, uint32_t njobs,
         return (uint64_t)jobs[x].w * jobs[x].h > (uint64_t)jobs[y].w * jobs[y].h;
     });
     if (config) b->cfg = *config;
-    size_t tb = njobs * sizeof(BatchJobDev);
+    size_t tb = table_bytes(njobs);
     if (cudaMallocHost(&b->h_stage, tb) != cudaSuccess || cudaMalloc(&b->d_table, tb) != cudaSuccess ||
         cudaMalloc(&b->d_counter, sizeof(uint32_t)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -286,16 +352,10 @@ EXPORT int vox_cuda_batch_set_camera(vox_cuda_batch *b, uint32_t job, const vox_
 {
     if (!b || !camera || job >= b->jobs.size()) return VOX_CUDA_EINVAL;
     if (camera->kind != VOX_CUDA_CAMERA_SIMPLE && camera->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
+    // the frame's rectangle, and with it every later frame's queue range,
+    // follows the camera; the graph reads the totals from the table's head
     b->jobs[job].camera = *camera;
-    for (size_t q = 0; q < b->order.size(); q++) {
-        if (b->order[q] != job) continue;
-        BatchJobDev &d = b->table[q];
-        d.cam = *camera;
-        const vox_cuda_frame_job &j = b->jobs[job];
-        vox::TileOrder o = tile_order(j.tree, *camera, j.w, j.h, b->cfg.tile_w, b->cfg.tile_h);
-        d.ctx = o.cbx;
-        d.cty = o.cby;
-    }
+    fill_table(b);
     return VOX_CUDA_OK;
 }
 
@@ -305,7 +365,7 @@ EXPORT int vox_cuda_batch_launch(vox_cuda_batch *b, void *stream)
     // The graph reads h_stage when it runs: wait for the previous replay before
     // refreshing it with the current cameras.
     if (b->launched && cudaEventSynchronize(b->done) != cudaSuccess) return VOX_CUDA_ECUDA;
-    std::memcpy(b->h_stage, b->table.data(), b->table.size() * sizeof(BatchJobDev));
+    stage_table(b);
     cudaStream_t s = as_stream(stream);
     if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return VOX_CUDA_ECUDA;
     count_launch();
@@ -415,10 +475,12 @@ EXPORT int vox_cuda_batch_free(vox_cuda_batch *b)
 namespace {
 
 constexpr size_t NOALLOC_HEAD_BYTES = 256;
-constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD_BYTES + VOX_CUDA_NOALLOC_MAX_JOBS * sizeof(BatchJobDev);
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEAD_BYTES + sizeof(BatchHead) +
+                                 VOX_CUDA_NOALLOC_MAX_JOBS * sizeof(BatchJobDev);
 static_assert(NOALLOC_BYTES <= 16384, "no-allocation scratch must stay within 16 KiB");
 
-// [0, 4): work-queue head; [256, ...): job table.
+// [0, 4): work-queue head; [256, ...): job table (its head, then one entry
+// per frame).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
@@ -440,10 +502,9 @@ int noalloc_scratch(int dev, unsigned char **out)
 }
 
 template <int CAP>
-void launch_noalloc(const BatchJobDev *table, uint32_t njobs, uint32_t total, uint32_t *head, int nsm,
-                    cudaStream_t s)
+void launch_noalloc(const BatchHead *table, uint32_t *head, int nsm, cudaStream_t s)
 {
-    batch_kernel<CAP, 8, 4><<<nsm * 8, 128, 0, s>>>(table, njobs, total, 2, head);
+    batch_kernel<CAP, 8, 4><<<nsm * 8, 128, 0, s>>>(table, 2, head);
 }
 
 }  // namespace
@@ -479,34 +540,23 @@ EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32
         }
         order[k] = i;
     }
-    BatchJobDev table[VOX_CUDA_NOALLOC_MAX_JOBS];
-    uint32_t base = 0;
-    for (uint32_t q = 0; q < njobs; q++) {
-        const vox_cuda_frame_job &j = jobs[order[q]];
-        BatchJobDev &d = table[q];
-        std::memset(&d, 0, sizeof d);
-        d.tree = j.tree->dev;
-        d.cam = j.camera;
-        d.tex = j.texture;
-        d.argb = j.argb;
-        d.status = j.tree->d_status;
-        d.w = j.w;
-        d.h = j.h;
-        vox::TileOrder o = tile_order(j.tree, j.camera, j.w, j.h, 8, 4);
-        d.ntx = o.nbx; d.nty = o.nby; d.ctx = o.cbx; d.cty = o.cby;
-        d.tile_base = base;
-        base += o.nbx * o.nby;
-    }
+    // head and table staged on the host stack, copied into the array
+    struct {
+        BatchHead head;
+        BatchJobDev jobs[VOX_CUDA_NOALLOC_MAX_JOBS];
+    } stage;
+    stage.head = BatchHead{njobs, 0u, 0u, 0u};
+    for (uint32_t q = 0; q < njobs; q++) fill_job(stage.jobs[q], jobs[order[q]], 8, 4, stage.head);
     cudaStream_t s = as_stream(stream);
     uint32_t *head = reinterpret_cast<uint32_t *>(scratch);
-    BatchJobDev *dtable = reinterpret_cast<BatchJobDev *>(scratch + NOALLOC_HEAD_BYTES);
-    if (cudaMemcpyAsync(dtable, table, njobs * sizeof(BatchJobDev), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+    BatchHead *dtable = reinterpret_cast<BatchHead *>(scratch + NOALLOC_HEAD_BYTES);
+    if (cudaMemcpyAsync(dtable, &stage, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(head, 0, sizeof(uint32_t), s) != cudaSuccess)
         return VOX_CUDA_ECUDA;
     switch (cap) {
-    case 0: launch_noalloc<CAP0>(dtable, njobs, base, head, nsm, s); break;
-    case 1: launch_noalloc<CAP1>(dtable, njobs, base, head, nsm, s); break;
-    default: launch_noalloc<CAP2>(dtable, njobs, base, head, nsm, s); break;
+    case 0: launch_noalloc<CAP0>(dtable, head, nsm, s); break;
+    case 1: launch_noalloc<CAP1>(dtable, head, nsm, s); break;
+    default: launch_noalloc<CAP2>(dtable, head, nsm, s); break;
     }
     count_launch();
     return status_of(cudaGetLastError());
@@ -517,42 +567,30 @@ EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32
  * table the server allocated for one launch.
  * ------------------------------------------------------------------------- */
 
-size_t frame_job_entry_bytes() { return sizeof(BatchJobDev); }
+size_t frame_job_table_bytes(uint32_t njobs) { return table_bytes(njobs); }
 
 int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
                        uint32_t *d_counter, int nsm, cudaStream_t s)
 {
     if (njobs == 0 || njobs > MAX_JOBS) return VOX_CUDA_EINVAL;
-    BatchJobDev *table = static_cast<BatchJobDev *>(h_table);
-    uint32_t base = 0;
+    BatchHead *head = static_cast<BatchHead *>(h_table);
+    BatchJobDev *table = reinterpret_cast<BatchJobDev *>(head + 1);
+    *head = BatchHead{njobs, 0u, 0u, 0u};
     int cap = 0;
     for (uint32_t q = 0; q < njobs; q++) {
-        const vox_cuda_frame_job &j = jobs[q];
-        BatchJobDev &d = table[q];
-        std::memset(&d, 0, sizeof d);
-        d.tree = j.tree->dev;
-        d.cam = j.camera;
-        d.tex = j.texture;
-        d.argb = j.argb;
-        d.status = j.tree->d_status;
-        d.w = j.w;
-        d.h = j.h;
-        vox::TileOrder o = tile_order(j.tree, j.camera, j.w, j.h, 8, 4);
-        d.ntx = o.nbx; d.nty = o.nby; d.ctx = o.cbx; d.cty = o.cby;
-        d.tile_base = base;
-        base += o.nbx * o.nby;
-        cap = std::max(cap, j.tree->cap_class);
+        fill_job(table[q], jobs[q], 8, 4, *head);
+        cap = std::max(cap, jobs[q].tree->cap_class);
     }
-    if (cudaMemcpyAsync(d_table, table, njobs * sizeof(BatchJobDev), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+    if (cudaMemcpyAsync(d_table, h_table, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s) != cudaSuccess)
         return VOX_CUDA_ECUDA;
     vox_cuda_batch_config c{8, 4, 2, 4};
-    const BatchJobDev *dt = static_cast<const BatchJobDev *>(d_table);
+    const BatchHead *dt = static_cast<const BatchHead *>(d_table);
     cudaError_t e;
     switch (cap) {
-    case 0: e = launch_batch_cap<CAP0>(c, dt, njobs, base, d_counter, nsm, s); break;
-    case 1: e = launch_batch_cap<CAP1>(c, dt, njobs, base, d_counter, nsm, s); break;
-    default: e = launch_batch_cap<CAP2>(c, dt, njobs, base, d_counter, nsm, s); break;
+    case 0: e = launch_batch_cap<CAP0>(c, dt, d_counter, nsm, s); break;
+    case 1: e = launch_batch_cap<CAP1>(c, dt, d_counter, nsm, s); break;
+    default: e = launch_batch_cap<CAP2>(c, dt, d_counter, nsm, s); break;
     }
     return status_of(e);
 }

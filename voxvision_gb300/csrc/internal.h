@@ -60,13 +60,6 @@ __device__ __forceinline__ uint32_t centre_out(uint32_t k, uint32_t c, uint32_t 
     return (c < n - 1 - c) ? c + m + 1 + j : c - m - 1 - j;
 }
 
-// Block tiles are issued rows-first outward from the tile where the tree's
-// centre projects: the rays that walk the tree longest start first, so the
-// frame does not wait on late starters.  Every tile is drawn exactly once.
-struct TileOrder {
-    uint32_t nbx, nby, cbx, cby;
-};
-
 // Work of one BEST frame: the screen rectangle that the tree's bounding box
 // can project into (pixels outside it cannot reach the tree and are misses),
 // cut in 16x8-pixel block tiles issued outward from the tile where the tree's
@@ -81,9 +74,11 @@ struct FramePlan {
 
 constexpr int TILE_W = 16, TILE_H = 8;   // render block tile; warps are 8x4
 
-/* Order in which the render kernel issues its block tiles for this camera. */
-vox::TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
-                          uint32_t tile_w = TILE_W, uint32_t tile_h = TILE_H);
+/* The screen rectangle [rect[0], rect[2]) x [rect[1], rect[3]) of a w x h
+ * frame outside which no ray can reach the tree (multiples of 8 x 4; empty
+ * for an empty tree), and where the tree's centre projects. */
+void frame_rect_of(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h, uint32_t rect[4],
+                   double centre_px[2]);
 
 /* The plan of a BEST frame; cull = false traces the whole frame.
  * Conservative: every pixel whose ray can enter the tree's bounding box lies
@@ -92,9 +87,10 @@ void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, 
                 vox::FramePlan &p);
 
 /* The batched frame kernel over a job table the caller allocated for one
- * launch (batch.cu): fills h_table (pinned, frame_job_entry_bytes() per job),
- * copies it to d_table, zeroes *d_counter and launches, all on s. */
-size_t frame_job_entry_bytes();
+ * launch (batch.cu): fills h_table (pinned, frame_job_table_bytes(njobs)
+ * bytes, 16-byte aligned), copies it to d_table, zeroes *d_counter and
+ * launches, all on s. */
+size_t frame_job_table_bytes(uint32_t njobs);
 int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
                        uint32_t *d_counter, int nsm, cudaStream_t s);
 

@@ -279,7 +279,7 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
         }
     }
     if (!jobs.empty()) {
-        size_t tb = (jobs.size() * frame_job_entry_bytes() + 255) & ~(size_t)255;
+        size_t tb = (frame_job_table_bytes((uint32_t)jobs.size()) + 255) & ~(size_t)255;
         L->h_table = s->pinned.get(tb, &L->h_table_cls);
         int rc = VOX_CUDA_ENOMEM;
         if (L->h_table && cudaMallocAsync(&L->d_table, tb + 256, st) == cudaSuccess) {

@@ -32,7 +32,6 @@
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
 using vox::Counts;
-using vox::TileOrder;
 using vox::centre_out;
 using vox::DevTree;
 using vox::RayHit;
@@ -407,44 +406,6 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 void count_launch() { g_launches++; }
 
-// Screen position of the centre of the tree's bounding box (inverse of
-// screen2world), clamped to the frame; the frame centre when it lies behind
-// the camera.  Only used to order the tiles.
-TileOrder tile_order(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
-                     uint32_t tile_w, uint32_t tile_h)
-{
-    TileOrder o;
-    o.nbx = (w + tile_w - 1) / tile_w;
-    o.nby = (h + tile_h - 1) / tile_h;
-    double v[3], c[3];
-    for (int i = 0; i < 3; i++) v[i] = 0.5 * ((double)t->bbox[i] + t->bbox[3 + i]) - cam.position[i];
-    double shift = 0.0;
-    if (cam.kind == VOX_CUDA_CAMERA_DOOM) {
-        c[0] = v[0] * cam.cosphi + v[1] * cam.sinphi;
-        c[1] = v[1] * cam.cosphi - v[0] * cam.sinphi;
-        c[2] = v[2];
-        shift = cam.k;
-    } else {
-        // rotate by the conjugate quaternion: v + w t + u x t, t = 2 (u x v), u = -q.xyz
-        double qw = cam.rotation[0], ux = -cam.rotation[1], uy = -cam.rotation[2], uz = -cam.rotation[3];
-        double tx = 2 * (uy * v[2] - uz * v[1]), ty = 2 * (uz * v[0] - ux * v[2]), tz = 2 * (ux * v[1] - uy * v[0]);
-        c[0] = v[0] + qw * tx + (uy * tz - uz * ty);
-        c[1] = v[1] + qw * ty + (uz * tx - ux * tz);
-        c[2] = v[2] + qw * tz + (ux * ty - uy * tx);
-    }
-    double sx = 0.5 * w, sy = 0.5 * h;
-    if (c[1] > 1e-6 && cam.mul != 0.0f) {
-        sx = (c[0] / c[1] + cam.xsub) / cam.mul;
-        sy = (cam.ysub + shift - c[2] / c[1]) / cam.mul;
-    }
-    if (!(sx >= 0)) sx = 0;               // also catches NaN
-    if (!(sy >= 0)) sy = 0;
-    if (sx > w - 1) sx = w - 1;
-    if (sy > h - 1) sy = h - 1;
-    o.cbx = (uint32_t)sx / tile_w;
-    o.cby = (uint32_t)sy / tile_h;
-    return o;
-}
 
 
 // Linear map of screen2world: direction = M * (mul*sx - xsub, 1, ysub' - mul*sy)
@@ -595,6 +556,18 @@ void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, 
     uint64_t outside = (uint64_t)w * h - (uint64_t)(p.x1 - p.x0) * (p.y1 - p.y0);
     p.nclear = outside ? std::min<uint32_t>(64u, (h + 3) / 4) : 0;
     if (p.ntiles + p.nclear == 0) p.nclear = 1;
+}
+
+void frame_rect_of(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h, uint32_t rect[4],
+                   double centre_px[2])
+{
+    if (t->dev.root == VOXP_EMPTY) {
+        rect[0] = rect[1] = rect[2] = rect[3] = 0;
+        centre_px[0] = 0.5 * w;
+        centre_px[1] = 0.5 * h;
+        return;
+    }
+    frame_rect(t->bbox, cam, w, h, rect, centre_px);
 }
 
 // ======================================================================== API
@@ -829,6 +802,24 @@ EXPORT int vox_cuda_render_device(const vox_cuda_tree *t, const vox_cuda_camera 
     return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream)));
 }
 
+// The device's address of a host buffer that the GPU can write in place:
+// page-locked host memory (cudaHostAlloc, cudaHostRegister, torch pinned
+// tensors), which is mapped into the device's address space; nullptr for
+// pageable memory.
+static void *device_alias(void *host)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
+// Host-buffer frame: the texture is copied in; a page-locked frame is drawn
+// in place (the kernel's stores cross the host link while the frame is
+// traced, and no copy follows), a pageable one is drawn into device scratch
+// and copied out.
 EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                            const uint8_t *tex, uint32_t *argb, void *stream)
 {
@@ -837,13 +828,14 @@ EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     cudaStream_t s = as_stream(stream);
     size_t npx = (size_t)w * h;
     size_t b_tex = align256(32768);
+    uint32_t *in_place = static_cast<uint32_t *>(device_alias(argb));
     Scratch sc(s);
-    if (sc.get(b_tex + npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    if (sc.get(b_tex + (in_place ? 0 : npx * 4)) != cudaSuccess) return VOX_CUDA_ENOMEM;
     uint8_t *d_tex = static_cast<uint8_t *>(sc.p);
-    uint32_t *d_argb = reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
+    uint32_t *d_argb = in_place ? in_place : reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
     cudaError_t e = cudaMemcpyAsync(d_tex, tex, 32768, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, d_tex, d_argb, nullptr, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && !in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return VOX_CUDA_ECUDA;
     return check_tree_status(t, s);
 }
@@ -930,15 +922,16 @@ EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera
     cudaStream_t s = as_stream(stream);
     size_t npx = (size_t)w * h;
     size_t b_tex = align256(32768);
+    uint32_t *in_place = static_cast<uint32_t *>(device_alias(argb));
     Scratch sc(s);
-    if (sc.get(b_tex + npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    if (sc.get(b_tex + (in_place ? 0 : npx * 4)) != cudaSuccess) return VOX_CUDA_ENOMEM;
     uint8_t *d_tex = static_cast<uint8_t *>(sc.p);
-    uint32_t *d_argb = reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
+    uint32_t *d_argb = in_place ? in_place : reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
     cudaError_t e = cudaMemcpyAsync(d_tex, tex, 32768, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
         rc = vox_cuda_render_quality_device(t, cam, w, h, quality, d_tex, d_argb, stream);
         if (rc) return rc;
-        e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+        if (!in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
     }
     if (e != cudaSuccess) return VOX_CUDA_ECUDA;
     return check_tree_status(t, s);
