@@ -261,15 +261,20 @@ int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njob
 
 /* ---- Request server --------------------------------------------------------
  * Frame and ball-collision requests from any number of client threads over
- * resident trees, admitted by a device-memory budget and batched
- * continuously: everything admitted since the previous launch goes out in
- * the next one, on the next of several streams, so requests that arrive
- * while others run overlap with them on the device.  Each result equals
- * the plain entry point's for the same request alone.
+ * resident trees, admitted by memory budgets and batched continuously:
+ * everything admitted since the previous launch goes out in the next one, on
+ * the next of several streams, so requests that arrive while others run
+ * overlap with them on the device.  Results are written by the kernels in
+ * place into pinned host memory (no device buffer, no copy per request).
+ * The device budget holds the resident trees and the per-launch job tables
+ * (256 bytes per frame); the pinned-host budget holds each admitted
+ * request's result (w*h*4 bytes, or n) and staged ball inputs (16 bytes per
+ * ball), in power-of-two size classes from 4 KiB.  Each result equals the
+ * plain entry point's for the same request alone.
  * Replaces: applications calling vox_render / vox_tree_ball_collidep from
  * many threads (renderer.h:208 is callable from any thread). */
 typedef struct {
-    uint64_t budget_bytes;       /* device bytes for resident trees + request buffers */
+    uint64_t budget_bytes;       /* device bytes for resident trees + job tables      */
     uint64_t host_budget_bytes;  /* pinned host bytes for results and staged inputs   */
     uint32_t max_inflight;   /* requests admitted at once                         */
     uint32_t max_batch;      /* requests per launch (1..1024)                     */
@@ -279,8 +284,9 @@ typedef struct {
 
 typedef struct {
     uint64_t submitted, completed, rejected, launches;
-    uint64_t bytes_in_use, peak_bytes;
+    uint64_t bytes_in_use, peak_bytes;            /* device budget */
     uint64_t pending, inflight;
+    uint64_t host_bytes_in_use, host_peak_bytes;  /* pinned-host budget */
 } vox_cuda_server_stats;
 
 typedef struct vox_cuda_server vox_cuda_server;
@@ -309,6 +315,32 @@ int vox_cuda_server_release(vox_cuda_server *srv, uint64_t ticket);
 int vox_cuda_server_get_stats(vox_cuda_server *srv, vox_cuda_server_stats *stats);
 /* Finish all queued requests, then stop. */
 int vox_cuda_server_destroy(vox_cuda_server *srv);
+
+/* Replay a request trace against a server, for capacity measurements (no
+ * counterpart in the reference).  Requests are submitted from the calling
+ * thread at their arrival times (seconds after the call starts, ascending);
+ * `collectors` threads (1..64) wait for them in arrival order, record the
+ * server's submission, launch and completion times and release them.
+ * Returns when every request has completed (out[i].status is its status;
+ * a submission refused by the server keeps that error). */
+typedef struct {
+    uint32_t kind;               /* 0 BEST frame, 1 ball batch          */
+    uint32_t tree_id;
+    vox_cuda_camera camera;      /* frame                               */
+    uint32_t w, h;               /* frame                               */
+    const float *centres;        /* ball batch, n x 3 (host)            */
+    const float *radii;          /* ball batch, n (host)                */
+    uint32_t n;                  /* ball batch                          */
+    double arrival_s;
+} vox_cuda_replay_request;
+
+typedef struct {
+    int32_t status;
+    uint64_t submit_ns, launch_ns, done_ns;
+} vox_cuda_replay_result;
+
+int vox_cuda_server_replay(vox_cuda_server *srv, const vox_cuda_replay_request *requests, uint32_t n,
+                           uint32_t collectors, vox_cuda_replay_result *results);
 
 /* Library version and the number of kernel launches made so far by this
  * process (all entry points); used to report launch counts. */

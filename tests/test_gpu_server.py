@@ -97,23 +97,33 @@ def test_mixed_requests_equal_requests_alone(setup):
     assert stats["launches"] >= 1
 
 
+def _pinned_class(nbytes):
+    c = 4096
+    while c < nbytes:
+        c <<= 1
+    return c
+
+
 def test_tight_budget_queues_but_stays_exact(setup):
-    """A budget that holds the trees plus about two 640x480 frames forces
-    admission to wait for memory; results are unchanged."""
+    """A pinned-host budget that holds about two 640x480 results (plus two
+    of the largest ball requests) forces admission to wait for memory;
+    results are unchanged and the budget is never exceeded."""
     vg, wl, hosts, trees, tex = setup
-    tree_bytes = sum(t.info()["device_bytes"] for t in trees)
     reqs = _requests(wl, 24, 2)
-    cfg = vg.ServerConfig(tree_bytes + 2 * 640 * 480 * 4 + 4 * 20000 * 17, 1 << 30, 8, 4, 2, 2)
+    host_budget = 2 * _pinned_class(640 * 480 * 4) + 2 * (_pinned_class(20000) + _pinned_class(20000 * 16))
+    cfg = vg.ServerConfig(1 << 34, host_budget, 8, 4, 2, 2)
     results, stats = _run_mixed(vg, trees, tex, reqs, cfg, nthreads=3)
     for q, got in zip(reqs, results):
         assert np.array_equal(got, _alone(trees, tex, q)), q[0]
-    assert stats["peak_bytes"] <= cfg.budget_bytes
+    assert 0 < stats["host_peak_bytes"] <= host_budget
 
 
 def test_budget_refusal_and_bounded_wait(setup):
+    """A frame whose result could never fit the pinned-host budget is refused
+    at submission; two that fit one at a time are served one after the
+    other, the second's wait bounded."""
     vg, wl, hosts, trees, tex = setup
-    tree_bytes = sum(t.info()["device_bytes"] for t in trees)
-    srv = vg.Server(tex, vg.ServerConfig(tree_bytes + 320 * 240 * 4, 1 << 30, 4, 4, 1, 1))
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, _pinned_class(320 * 240 * 4) + 4096, 4, 4, 1, 1))
     ids = [srv.add_tree(t) for t in trees]
     from voxvision_gb300.cameras import HostCamera
     cam = HostCamera(0)
@@ -132,4 +142,28 @@ def test_budget_refusal_and_bounded_wait(setup):
     a1, _ = srv.result(t1)
     a2, _ = srv.result(t2)
     assert np.array_equal(a1, a2)
+    assert np.array_equal(a1, _alone(trees, tex, ("frame", 0, cam.gpu_struct(), 320, 240)))
+    srv.close()
+
+
+def test_replay_serves_a_poisson_trace(setup):
+    """vox_cuda_server_replay: a trace of frames and ball batches at Poisson
+    arrival times; every request completes, with its server times in order
+    (result exactness is the mixed-request test's)."""
+    vg, wl, hosts, trees, tex = setup
+    reqs = _requests(wl, 40, 4)
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, 1 << 32, 64, 16, 4, 8))
+    ids = [srv.add_tree(t) for t in trees]
+    arrivals = np.cumsum(np.random.default_rng(4).exponential(1 / 2000.0, len(reqs)))
+    trace = []
+    for q, at in zip(reqs, arrivals):
+        if q[0] == "frame":
+            trace.append(("frame", ids[q[1]], q[2], q[3], q[4], float(at)))
+        else:
+            trace.append(("balls", ids[q[1]], q[2], q[3], float(at)))
+    res = srv.replay(trace, collectors=3)
+    assert (res[:, 0] == 0).all()
+    assert (res[:, 1] <= res[:, 2]).all() and (res[:, 2] <= res[:, 3]).all()
+    st = srv.stats()
+    assert st["completed"] == st["submitted"] == len(reqs)
     srv.close()

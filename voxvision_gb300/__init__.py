@@ -14,8 +14,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, BatchConfig, CameraStruct,
-                   FrameJob, RenderConfig, ServerConfig, ServerStats, TreeInfo, VoxCudaError, available, check,
-                   lib)
+                   FrameJob, RenderConfig, ReplayRequest, ReplayResult, ServerConfig, ServerStats, TreeInfo,
+                   VoxCudaError, available, check, lib)
 
 __all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Server", "ServerConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
            "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size",
@@ -315,6 +315,30 @@ class Server:
 
     def release(self, ticket: int):
         check(lib().vox_cuda_server_release(self.h, ticket), "vox_cuda_server_release")
+
+    def replay(self, requests, collectors: int = 8):
+        """vox_cuda_server_replay over a trace: a list of ("frame", tree_id,
+        camera, w, h, arrival_s) and ("balls", tree_id, centres, radii,
+        arrival_s) tuples, arrivals ascending.  Returns an (n, 4) int64 array
+        of status, submit, launch and done times (ns)."""
+        n = len(requests)
+        arr = (ReplayRequest * max(n, 1))()
+        keep = []
+        for i, q in enumerate(requests):
+            r = arr[i]
+            if q[0] == "frame":
+                _, tid, cam, w, h, at = q
+                r.kind, r.tree_id, r.camera, r.w, r.h, r.arrival_s = 0, tid, cam, w, h, at
+            else:
+                _, tid, c, rad, at = q
+                c = np.ascontiguousarray(c, dtype=np.float32)
+                rad = np.ascontiguousarray(rad, dtype=np.float32)
+                keep += [c, rad]
+                r.kind, r.tree_id, r.n, r.arrival_s = 1, tid, rad.shape[0], at
+                r.centres, r.radii = c.ctypes.data, rad.ctypes.data
+        out = (ReplayResult * max(n, 1))()
+        check(lib().vox_cuda_server_replay(self.h, arr, n, collectors, out), "vox_cuda_server_replay")
+        return np.array([(o.status, o.submit_ns, o.launch_ns, o.done_ns) for o in out[:n]], dtype=np.int64)
 
     def stats(self) -> dict:
         s = ServerStats()

@@ -68,9 +68,23 @@ class RenderConfig(C.Structure):
     _fields_ = [("cull", C.c_uint32), ("overlap", C.c_uint32)]
 
 
+class ReplayRequest(C.Structure):
+    """vox_cuda_replay_request (include/voxtrees_cuda.h)."""
+    _fields_ = [("kind", C.c_uint32), ("tree_id", C.c_uint32), ("camera", CameraStruct), ("w", C.c_uint32),
+                ("h", C.c_uint32), ("centres", C.c_void_p), ("radii", C.c_void_p), ("n", C.c_uint32),
+                ("arrival_s", C.c_double)]
+
+
+class ReplayResult(C.Structure):
+    """vox_cuda_replay_result (include/voxtrees_cuda.h)."""
+    _fields_ = [("status", C.c_int32), ("submit_ns", C.c_uint64), ("launch_ns", C.c_uint64),
+                ("done_ns", C.c_uint64)]
+
+
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "rejected", "launches", "bytes_in_use",
-                                          "peak_bytes", "pending", "inflight")]
+                                          "peak_bytes", "pending", "inflight", "host_bytes_in_use",
+                                          "host_peak_bytes")]
 
 
 _lib = None
@@ -118,6 +132,7 @@ SIGNATURES = {
     "vox_cuda_server_release": (C.c_int, [_vp, C.c_uint64]),
     "vox_cuda_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats)]),
     "vox_cuda_server_destroy": (C.c_int, [_vp]),
+    "vox_cuda_server_replay": (C.c_int, [_vp, C.POINTER(ReplayRequest), _u32, _u32, C.POINTER(ReplayResult)]),
     "vox_cuda_render_counts_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp, _vp]),
     "vox_cuda_ray_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
     "vox_cuda_ball_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),

@@ -8,10 +8,16 @@
  * order while the budget and the in-flight slots allow, and put everything
  * admitted since the previous launch into one launch on the next of several
  * streams -- all frames into one persistent work-queue kernel (the batched
- * kernel of batch.cu), each ball request into the ball kernel, then the
- * copies of the results to pinned host memory.  Requests that arrive while
- * earlier launches are still on the GPU therefore go out in the next launch
- * and overlap with them on the device instead of waiting for them.
+ * kernel of batch.cu), each ball request into the ball kernel.  Results are
+ * written in place into the pinned host buffers the clients read (frames by
+ * the frame kernel's stores, hits by the ball kernel's, which also reads its
+ * staged inputs from pinned memory): on GB300 these stores cross the host
+ * link while the kernels run, so a request needs no device buffer and no
+ * copy.  The device budget holds the resident trees and the per-launch job
+ * tables; the pinned-host budget holds the results and staged inputs.
+ * Requests that arrive while earlier launches are still on the GPU go out
+ * in the next launch and overlap with them on the device instead of waiting
+ * for them.
  *
  * Every result is the one the plain entry points give for the same request
  * alone (vox_cuda_render_device, vox_cuda_ball_batch): same kernels, same
@@ -103,8 +109,7 @@ struct Request {
     std::vector<float> centres, radii;
     uint64_t dev_bytes = 0;         // charged to the device budget while admitted
     uint64_t host_bytes = 0;        // charged to the pinned-host budget while admitted
-    void *d_buf = nullptr;          // frame, or centres | radii | hits
-    void *h_res = nullptr;          // pinned result
+    void *h_res = nullptr;          // pinned result, written in place by the kernels
     size_t h_cls = 0, res_bytes = 0;
     void *h_in = nullptr;           // pinned ball inputs
     size_t h_in_cls = 0;
@@ -125,7 +130,6 @@ struct Launch {
     std::atomic<uint64_t> t_cb{0};       // completion time seen by the callback
     bool has_callback = false;      // then only `finished` may retire the launch
     // buffers to give back once retired (taken off the requests under the lock)
-    std::vector<void *> dev_free;
     std::vector<std::pair<void *, size_t>> host_free;
 };
 
@@ -147,7 +151,7 @@ struct vox_cuda_server {
     std::vector<Launch *> inflight;
     std::unordered_map<uint64_t, Request *> reqs;
     uint64_t next_ticket = 1;
-    uint64_t used = 0, peak = 0, tree_bytes = 0, host_used = 0;
+    uint64_t used = 0, peak = 0, tree_bytes = 0, host_used = 0, host_peak = 0;
     uint64_t submitted = 0, completed = 0, rejected = 0, launches = 0;
     uint32_t inflight_reqs = 0;
     uint32_t building = 0;          // launches being built outside the lock
@@ -198,8 +202,6 @@ void retire(vox_cuda_server *s, std::vector<Launch *> &out)
         Launch *L = s->inflight[i];
         if (!launch_finished(L)) { i++; continue; }
         for (Request *r : L->reqs) {
-            if (r->d_buf) L->dev_free.push_back(r->d_buf);
-            r->d_buf = nullptr;
             if (r->h_in) L->host_free.push_back({r->h_in, r->h_in_cls});
             r->h_in = nullptr;
             s->used -= r->dev_bytes;
@@ -219,7 +221,6 @@ void retire(vox_cuda_server *s, std::vector<Launch *> &out)
 // Outside the lock: give a retired launch's buffers back (stream-ordered).
 void release_launch(vox_cuda_server *s, Launch *L)
 {
-    for (void *p : L->dev_free) cudaFreeAsync(p, L->stream);
     for (auto &hp : L->host_free) s->pinned.put(hp.first, hp.second);
     if (L->d_table) cudaFreeAsync(L->d_table, L->stream);
     s->pinned.put(L->h_table, L->h_table_cls);
@@ -244,38 +245,36 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
         size_t out_bytes = r->kind == FRAME ? (size_t)r->w * r->h * 4 : (size_t)r->n;
         r->res_bytes = out_bytes;
         r->h_res = s->pinned.get(out_bytes, &r->h_cls);
-        if (!r->h_res) { r->status = VOX_CUDA_ENOMEM; continue; }
+        void *d_res = nullptr;
+        if (!r->h_res || cudaHostGetDevicePointer(&d_res, r->h_res, 0) != cudaSuccess) {
+            r->status = VOX_CUDA_ENOMEM;
+            continue;
+        }
         if (r->kind == FRAME) {
-            if (cudaMallocAsync(&r->d_buf, out_bytes, st) != cudaSuccess) { r->status = VOX_CUDA_ENOMEM; continue; }
             vox_cuda_frame_job j;
             j.tree = s->trees[r->tree];
             j.camera = r->cam;
             j.w = r->w;
             j.h = r->h;
             j.texture = s->d_tex;
-            j.argb = static_cast<uint32_t *>(r->d_buf);
+            j.argb = static_cast<uint32_t *>(d_res);
             jobs.push_back(j);
             frames.push_back(r);
         } else {
             size_t n = r->n, in_bytes = n * 16;
+            void *d_in = nullptr;
             r->h_in = s->pinned.get(in_bytes, &r->h_in_cls);
-            if (!r->h_in || cudaMallocAsync(&r->d_buf, in_bytes + n + 256, st) != cudaSuccess) {
+            if (!r->h_in || cudaHostGetDevicePointer(&d_in, r->h_in, 0) != cudaSuccess) {
                 r->status = VOX_CUDA_ENOMEM;
                 continue;
             }
             std::memcpy(r->h_in, r->centres.data(), n * 12);
             std::memcpy(static_cast<char *>(r->h_in) + n * 12, r->radii.data(), n * 4);
-            char *d = static_cast<char *>(r->d_buf);
-            if (cudaMemcpyAsync(d, r->h_in, in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
-                r->status = VOX_CUDA_ECUDA;
-                continue;
-            }
-            int rc = vox_cuda_ball_batch_device(s->trees[r->tree], reinterpret_cast<float *>(d),
-                                                reinterpret_cast<float *>(d + n * 12), n,
-                                                reinterpret_cast<uint8_t *>(d + in_bytes), st);
-            if (rc) { r->status = rc; continue; }
-            if (cudaMemcpyAsync(r->h_res, d + in_bytes, n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-                r->status = VOX_CUDA_ECUDA;
+            const char *d = static_cast<const char *>(d_in);
+            int rc = vox_cuda_ball_batch_device(s->trees[r->tree], reinterpret_cast<const float *>(d),
+                                                reinterpret_cast<const float *>(d + n * 12), n,
+                                                static_cast<uint8_t *>(d_res), st);
+            if (rc) r->status = rc;
         }
     }
     if (!jobs.empty()) {
@@ -287,11 +286,8 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
             rc = enqueue_frame_jobs(jobs.data(), (uint32_t)jobs.size(), L->h_table, L->d_table, counter,
                                     s->nsm, st);
         }
-        for (Request *r : frames) {
-            if (rc) { r->status = rc; continue; }
-            if (cudaMemcpyAsync(r->h_res, r->d_buf, r->res_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-                r->status = VOX_CUDA_ECUDA;
-        }
+        if (rc)
+            for (Request *r : frames) r->status = rc;
     }
     // completion is seen through the event; the callback only wakes the worker
     if (cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming) != cudaSuccess ||
@@ -322,6 +318,7 @@ void admit(vox_cuda_server *s)
         s->used += r->dev_bytes;
         s->host_used += r->host_bytes;
         s->peak = std::max(s->peak, s->used);
+        s->host_peak = std::max(s->host_peak, s->host_used);
         s->inflight_reqs++;
         s->admitted.push_back(r);
         if (s->admitted.size() >= s->cfg.max_batch) break;
@@ -366,9 +363,12 @@ void worker_loop(vox_cuda_server *s)
     }
 }
 
+// device bytes a request holds while admitted: its share of the launch's job
+// table (its result and inputs live in pinned host memory)
 uint64_t request_bytes(Kind k, uint64_t a, uint64_t b)
 {
-    return k == FRAME ? a * b * 4 : a * 17 + 512;
+    (void)a; (void)b;
+    return k == FRAME ? 256 : 0;
 }
 
 // pinned host bytes a request holds while admitted: its result, and for ball
@@ -544,6 +544,8 @@ EXPORT int vox_cuda_server_get_stats(vox_cuda_server *s, vox_cuda_server_stats *
     st->peak_bytes = s->peak;
     st->pending = s->pending.size();
     st->inflight = s->inflight_reqs;
+    st->host_bytes_in_use = s->host_used;
+    st->host_peak_bytes = s->host_peak;
     return VOX_CUDA_OK;
 }
 
@@ -566,5 +568,72 @@ EXPORT int vox_cuda_server_destroy(vox_cuda_server *s)
     }
     cudaFree(s->d_tex);
     delete s;
+    return VOX_CUDA_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * Trace replay: a request trace submitted at its arrival times from a native
+ * thread, completions collected by `collectors` threads that wait on the
+ * tickets in arrival order and release them.  The submitting thread sleeps
+ * until shortly before each arrival and spins the rest, so arrivals keep
+ * their spacing at tens of kHz; per-request times are the server's own.
+ * ------------------------------------------------------------------------- */
+
+EXPORT int vox_cuda_server_replay(vox_cuda_server *s, const vox_cuda_replay_request *reqs, uint32_t n,
+                                  uint32_t collectors, vox_cuda_replay_result *out)
+{
+    if (!s || (n && (!reqs || !out)) || collectors == 0 || collectors > 64) return VOX_CUDA_EINVAL;
+    for (uint32_t i = 0; i < n; i++) {
+        const vox_cuda_replay_request &q = reqs[i];
+        if (q.kind > 1 || !(q.arrival_s >= 0.0) || (i && q.arrival_s < reqs[i - 1].arrival_s))
+            return VOX_CUDA_EINVAL;
+        if (q.kind == 1 && (!q.centres || !q.radii || q.n == 0)) return VOX_CUDA_EINVAL;
+    }
+    std::vector<std::atomic<uint64_t>> tickets(n);     // 0: not submitted yet
+    std::vector<std::atomic<int>> submit_rc(n);
+    for (uint32_t i = 0; i < n; i++) { tickets[i].store(0); submit_rc[i].store(VOX_CUDA_OK); out[i] = {}; }
+    std::atomic<uint32_t> next{0};
+    auto collect = [&]() {
+        for (;;) {
+            uint32_t i = next.fetch_add(1);
+            if (i >= n) return;
+            uint64_t tk = 0;
+            // wait for the submitter to reach request i (it always does, or
+            // records why it could not)
+            while ((tk = tickets[i].load(std::memory_order_acquire)) == 0 && submit_rc[i].load() == VOX_CUDA_OK)
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            if (tk == 0) { out[i].status = submit_rc[i].load(); continue; }
+            int rc = VOX_CUDA_ETIMEOUT;
+            for (int k = 0; k < 600 && rc == VOX_CUDA_ETIMEOUT; k++)   // at most 10 minutes
+                rc = vox_cuda_server_wait(s, tk, 1000);
+            uint64_t times[3] = {0, 0, 0};
+            if (rc != VOX_CUDA_ETIMEOUT) {
+                vox_cuda_server_result(s, tk, nullptr, nullptr, times);
+                vox_cuda_server_release(s, tk);
+            }
+            out[i].status = rc;
+            out[i].submit_ns = times[0];
+            out[i].launch_ns = times[1];
+            out[i].done_ns = times[2];
+        }
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t c = 0; c < collectors; c++) pool.emplace_back(collect);
+    const uint64_t t0 = now_ns();
+    for (uint32_t i = 0; i < n; i++) {
+        const vox_cuda_replay_request &q = reqs[i];
+        const uint64_t due = t0 + (uint64_t)(q.arrival_s * 1e9);
+        for (;;) {
+            uint64_t t = now_ns();
+            if (t >= due) break;
+            if (due - t > 200000) std::this_thread::sleep_for(std::chrono::nanoseconds(due - t - 100000));
+        }
+        uint64_t tk = 0;
+        int rc = q.kind == 0 ? vox_cuda_server_submit_frame(s, q.tree_id, &q.camera, q.w, q.h, &tk)
+                             : vox_cuda_server_submit_balls(s, q.tree_id, q.centres, q.radii, q.n, &tk);
+        if (rc) submit_rc[i].store(rc);
+        else tickets[i].store(tk, std::memory_order_release);
+    }
+    for (auto &th : pool) th.join();
     return VOX_CUDA_OK;
 }
