@@ -278,9 +278,10 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
     import ctypes as C
     from voxvision_gb300 import workloads as wl
     from voxvision_gb300.cameras import HostCamera
-    # 128 requests admitted at once: a few milliseconds of GPU work, enough to
-    # keep it busy; more would only hold more pinned result memory
-    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 24 << 30, 128, 128, 4, 8))
+    # 256 requests admitted at once (a few milliseconds of GPU work; more would
+    # only hold more pinned result memory), up to 64 per launch, 32 launches
+    # in flight on 16 streams
+    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 24 << 30, 256, 64, 16, 32))
     ids = [srv.add_tree(t[2]) for t in trees]
     rng = np.random.default_rng(seed)
     ball_pool = []

@@ -133,8 +133,8 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-template <int CAP, bool COUNT>
-__global__ void __launch_bounds__(128) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
+template <int CAP, bool COUNT, int MINB>
+__global__ void __launch_bounds__(128, MINB) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
                                                      FramePlan p, const uint8_t *__restrict__ tex,
                                                      uint32_t *__restrict__ argb,
                                                      unsigned long long *__restrict__ counts,
@@ -332,19 +332,36 @@ cudaError_t launch_balls(const vox_cuda_tree *t, const float *c, const float *r,
 // Process-wide settings of the BEST frame kernel (vox_cuda_render_set_config).
 std::atomic<uint32_t> g_render_cull{1}, g_render_overlap{1};
 
+// Two builds of the frame kernel draw the same frame.  A frame that is
+// waited for on its own (the host-buffer calls) is bound by its slowest
+// warps, which run fastest with the registers they want (8 blocks per SM).
+// Frames enqueued back to back (the device calls) overlap one another, and
+// there more warps per SM hide more latency: 12 blocks per SM, at the cost of
+// a few spilled registers.
+constexpr int MINB_ALONE = 8, MINB_PIPELINED = 12;
+
 template <bool COUNT>
 cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
-                          const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s)
+                          const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s,
+                          bool pipelined = false)
 {
     // the counting kernel counts the reference's work: every pixel traced
     FramePlan p;
     plan_frame(t, cam, w, h, !COUNT && g_render_cull.load(), p);
     void (*kern)(DevTree, vox_cuda_camera, uint32_t, uint32_t, FramePlan, const uint8_t *, uint32_t *,
                  unsigned long long *, uint32_t *);
-    switch (t->cap_class) {
-    case 0: kern = render_kernel<CAP0, COUNT>; break;
-    case 1: kern = render_kernel<CAP1, COUNT>; break;
-    default: kern = render_kernel<CAP2, COUNT>; break;
+    if (pipelined && !COUNT) {
+        switch (t->cap_class) {
+        case 0: kern = render_kernel<CAP0, COUNT, MINB_PIPELINED>; break;
+        case 1: kern = render_kernel<CAP1, COUNT, MINB_PIPELINED>; break;
+        default: kern = render_kernel<CAP2, COUNT, MINB_PIPELINED>; break;
+        }
+    } else {
+        switch (t->cap_class) {
+        case 0: kern = render_kernel<CAP0, COUNT, MINB_ALONE>; break;
+        case 1: kern = render_kernel<CAP1, COUNT, MINB_ALONE>; break;
+        default: kern = render_kernel<CAP2, COUNT, MINB_ALONE>; break;
+        }
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.ntiles + p.nclear);
@@ -799,7 +816,7 @@ EXPORT int vox_cuda_render_device(const vox_cuda_tree *t, const vox_cuda_camera 
 {
     int rc = check_render_args(t, cam, w, h, tex, argb);
     if (rc) return rc;
-    return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream)));
+    return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true));
 }
 
 // The device's address of a host buffer that the GPU can write in place:
@@ -909,7 +926,7 @@ EXPORT int vox_cuda_render_quality_device(const vox_cuda_tree *t, const vox_cuda
     if (rc) return rc;
     if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
     if ((quality & VOX_CUDA_QUALITY_MODE_MASK) == VOX_CUDA_QUALITY_BEST)
-        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream)));
+        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true));
     return status_of(launch_render_squares(t, *cam, w, h, quality, tex, argb, as_stream(stream)));
 }
 
