@@ -189,6 +189,27 @@ def test_host_frame_pinned_and_pageable(tree256):
         assert np.array_equal(pageable.reshape(1080, 1920), ref)
 
 
+def test_host_calls_follow_texture_changes(tree64):
+    """The host-buffer call keeps the last texture on the device and uploads
+    a new one only when its bytes change: frames drawn with textures A, B, A,
+    and A edited in place, each equal the oracle's frame with that texture."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    ht, dt = tree64
+    cam = HostCamera(0)
+    cam.set_window_size(160, 120)
+    cam.set_position((150.0, -80.0, 90.0))
+    cam.look_at(np.array([32.0, 32.0, 32.0], np.float32))
+    a, b = wl.texture32(7), wl.texture32(11)
+    edited = a.copy()
+    for tex in (a, b, a, edited):
+        if tex is edited:
+            edited[::3] ^= 0x5A                       # same buffer object as before, new bytes
+        img = dt.render(cam.gpu_struct(), 160, 120, tex)
+        ref, _ = orc.render_best(ht.ptr, cam.state(), 160, 120, tex)
+        assert np.array_equal(img, ref)
+
+
 def test_setting_api_validates():
     with pytest.raises(vg().VoxCudaError):
         vg().set_render_config(2, 1)

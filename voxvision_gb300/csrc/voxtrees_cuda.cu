@@ -833,6 +833,75 @@ static void *device_alias(void *host)
     return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
 }
 
+// Per host thread and device: what the synchronous host-buffer frame calls
+// reuse from one call to the next.  A call returns only after its stream has
+// finished with these, so the next call of the same thread may use them
+// whatever stream it names.
+struct HostCallState {
+    uint8_t *d_tex = nullptr;      // device copy of the texture last used
+    uint8_t *h_tex = nullptr;      // pinned: the bytes d_tex holds (valid if tex_ok)
+    uint32_t *h_status = nullptr;  // pinned: the tree's status word read back
+    bool tex_ok = false;
+    ~HostCallState()               // at thread exit; errors after the CUDA context is gone are moot
+    {
+        if (d_tex) cudaFree(d_tex);
+        if (h_tex) cudaFreeHost(h_tex);
+    }
+};
+
+static HostCallState *host_call_state()
+{
+    constexpr int MAXDEV = 64;
+    thread_local HostCallState st[MAXDEV];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) return nullptr;
+    HostCallState &h = st[dev];
+    if (!h.d_tex) {
+        void *p = nullptr;
+        if (cudaMallocHost(&p, 32768 + 256) != cudaSuccess) return nullptr;
+        if (cudaMalloc(&h.d_tex, 32768) != cudaSuccess) {
+            cudaFreeHost(p);
+            h.d_tex = nullptr;
+            return nullptr;
+        }
+        h.h_tex = static_cast<uint8_t *>(p);
+        h.h_status = reinterpret_cast<uint32_t *>(static_cast<uint8_t *>(p) + 32768);
+    }
+    return &h;
+}
+
+// The texture on the device for a host-buffer call: uploaded only when its
+// bytes differ from the previous call's.
+static cudaError_t host_call_texture(HostCallState *hc, const uint8_t *tex, cudaStream_t s)
+{
+    if (hc->tex_ok && std::memcmp(hc->h_tex, tex, 32768) == 0) return cudaSuccess;
+    std::memcpy(hc->h_tex, tex, 32768);
+    hc->tex_ok = false;
+    cudaError_t e = cudaMemcpyAsync(hc->d_tex, hc->h_tex, 32768, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) hc->tex_ok = true;
+    return e;
+}
+
+// Ends a host-buffer call: reads the tree's status word back through pinned
+// memory with the stream's one synchronisation; clears it if set.  On an
+// enqueue error the stream is drained first, so no copy still reads the
+// thread's buffers when the call returns.
+static int host_call_finish(HostCallState *hc, const vox_cuda_tree *t, cudaStream_t s, cudaError_t e)
+{
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc->h_status, t->d_status, 4, cudaMemcpyDeviceToHost, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        hc->tex_ok = false;
+        return VOX_CUDA_ECUDA;
+    }
+    if (*hc->h_status) {
+        cudaMemsetAsync(t->d_status, 0, 4, s);
+        cudaStreamSynchronize(s);
+        return VOX_CUDA_ESTACK;
+    }
+    return VOX_CUDA_OK;
+}
+
 // Host-buffer frame: the texture is copied in; a page-locked frame is drawn
 // in place (the kernel's stores cross the host link while the frame is
 // traced, and no copy follows), a pageable one is drawn into device scratch
@@ -844,17 +913,16 @@ EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     if (rc) return rc;
     cudaStream_t s = as_stream(stream);
     size_t npx = (size_t)w * h;
-    size_t b_tex = align256(32768);
+    HostCallState *hc = host_call_state();
+    if (!hc) return VOX_CUDA_ENOMEM;
     uint32_t *in_place = static_cast<uint32_t *>(device_alias(argb));
     Scratch sc(s);
-    if (sc.get(b_tex + (in_place ? 0 : npx * 4)) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    uint8_t *d_tex = static_cast<uint8_t *>(sc.p);
-    uint32_t *d_argb = in_place ? in_place : reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
-    cudaError_t e = cudaMemcpyAsync(d_tex, tex, 32768, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, d_tex, d_argb, nullptr, s);
+    if (!in_place && sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    uint32_t *d_argb = in_place ? in_place : static_cast<uint32_t *>(sc.p);
+    cudaError_t e = host_call_texture(hc, tex, s);
+    if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, hc->d_tex, d_argb, nullptr, s);
     if (e == cudaSuccess && !in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return VOX_CUDA_ECUDA;
-    return check_tree_status(t, s);
+    return host_call_finish(hc, t, s, e);
 }
 
 EXPORT int vox_cuda_render_counts_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
@@ -938,18 +1006,20 @@ EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera
     if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
     cudaStream_t s = as_stream(stream);
     size_t npx = (size_t)w * h;
-    size_t b_tex = align256(32768);
+    HostCallState *hc = host_call_state();
+    if (!hc) return VOX_CUDA_ENOMEM;
     uint32_t *in_place = static_cast<uint32_t *>(device_alias(argb));
     Scratch sc(s);
-    if (sc.get(b_tex + (in_place ? 0 : npx * 4)) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    uint8_t *d_tex = static_cast<uint8_t *>(sc.p);
-    uint32_t *d_argb = in_place ? in_place : reinterpret_cast<uint32_t *>(static_cast<char *>(sc.p) + b_tex);
-    cudaError_t e = cudaMemcpyAsync(d_tex, tex, 32768, cudaMemcpyHostToDevice, s);
+    if (!in_place && sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    uint32_t *d_argb = in_place ? in_place : static_cast<uint32_t *>(sc.p);
+    cudaError_t e = host_call_texture(hc, tex, s);
     if (e == cudaSuccess) {
-        rc = vox_cuda_render_quality_device(t, cam, w, h, quality, d_tex, d_argb, stream);
-        if (rc) return rc;
+        rc = vox_cuda_render_quality_device(t, cam, w, h, quality, hc->d_tex, d_argb, stream);
+        if (rc) {
+            host_call_finish(hc, t, s, cudaErrorUnknown);
+            return rc;
+        }
         if (!in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
     }
-    if (e != cudaSuccess) return VOX_CUDA_ECUDA;
-    return check_tree_status(t, s);
+    return host_call_finish(hc, t, s, e);
 }
