@@ -309,9 +309,11 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
                 reqs.append(("balls", ids[tb], c, r, float(arrivals[i])))
         return reqs
 
-    # warm the server's pinned result pool (pinning new memory runs at about
-    # 14 GB/s and would otherwise land in the first timed seconds)
-    srv.replay(make_requests(1024, np.zeros(1024)))
+    # warm the server's pinned result pool with a trace at the highest rate
+    # (pinning new memory runs at about 14 GB/s; growing the pool inside a
+    # timed trace would show up as latency)
+    top = max(rates)
+    srv.replay(make_requests(2 * top // 10, np.cumsum(rng.exponential(1.0 / top, 2 * top // 10))))
     out = {}
     for rate in rates:
         n = max(200, int(rate * duration))
