@@ -89,6 +89,32 @@ const uint32_t *vox_context_pixels(const struct vox_rnd_ctx *ctx);
 /* VOX_CUDA_OK or the error of the last vox_render / vox_redraw. */
 int vox_context_status(const struct vox_rnd_ctx *ctx);
 
+/* Light manager (src/voxrnd/lights.h:14-83): an ambient light and soft
+ * shadowless lights bound by spheres (brightest at the centre, fading
+ * linearly to zero at the surface), kept in an M-tree.  Colours are rgb in
+ * [0, 1].  A context with a light manager colours each hit as the reference's
+ * get_color does (renderer.c:40-49): min(light, 1) * texel per channel. */
+struct vox_light_manager;
+/* lights.h:79: ambient light 1, 1, 1; no lights. */
+struct vox_light_manager *vox_make_light_manager(void);
+/* lights.h:82 */
+void vox_destroy_light_manager(struct vox_light_manager *light_manager);
+/* lights.h:73: 1 if the colour is valid, 0 otherwise (nothing changes). */
+int vox_set_ambient_light(struct vox_light_manager *light_manager, const vox_dot color);
+/* lights.h:38: 1 if inserted (valid colour, radius > 0, no light with this
+ * centre and radius yet), 0 otherwise. */
+int vox_insert_shadowless_light(struct vox_light_manager *light_manager, const vox_dot center, float radius,
+                                const vox_dot color);
+/* lights.h:48: 1 if a light with this centre and radius was removed. */
+int vox_delete_shadowless_light(struct vox_light_manager *light_manager, const vox_dot center, float radius);
+/* lights.h:53 */
+void vox_delete_shadowless_lights(struct vox_light_manager *light_manager);
+/* lights.h:58 */
+int vox_shadowless_lights_number(const struct vox_light_manager *light_manager);
+/* renderer.h:184: NULL draws without lights (grey texels).  The device copy
+ * of the lights follows changes to the manager at the next vox_render. */
+void vox_context_set_light_manager(struct vox_rnd_ctx *ctx, struct vox_light_manager *light_manager);
+
 /* Collision detector (src/voxrnd/cd.h:25-60): keeps an attached camera out
  * of the context's scene.  Allocated with malloc; release with free(). */
 struct vox_cd;

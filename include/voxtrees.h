@@ -75,6 +75,35 @@ int vox_tree_ball_collidep(const struct vox_node *tree, const vox_dot center, fl
 /* Drop the cached device copy of the tree rooted at `root` (no-op if none). */
 void vox_cuda_forget_tree(const struct vox_node *root);
 
+/* ---- M-trees of spheres (mtree.h:17-146): the light manager keeps its
+ * lights in one.  Same layout, same insertion, split and removal steps (the
+ * order in which a search visits spheres follows from them).  The block
+ * variant vox_mtree_spheres_containing needs clang blocks and is not
+ * provided; vox_mtree_spheres_containing_f is. */
+struct vox_sphere {           /* mtree.h:17-40 */
+    vox_dot center;
+    vox_dot color;
+    float radius;
+    float sqr_radius;         /* set by the library */
+};
+
+struct vox_mtree_node;
+
+/* mtree.h:73 -- 1 if added (radius > 0 and no sphere with the same centre
+ * and radius in the tree), 0 otherwise; *root may change. */
+int vox_mtree_add_sphere(struct vox_mtree_node **root, const struct vox_sphere *s);
+/* mtree.h:86 -- 1 if a sphere with the same centre and radius was removed. */
+int vox_mtree_remove_sphere(struct vox_mtree_node **root, const struct vox_sphere *s);
+/* mtree.h:91 */
+void vox_mtree_destroy(struct vox_mtree_node *root);
+/* mtree.h:104 -- the leaf holding a sphere with the same centre and radius, or NULL. */
+struct vox_mtree_node *vox_mtree_contains_sphere(const struct vox_mtree_node *root, const struct vox_sphere *s);
+/* mtree.h:110 -- number of spheres. */
+unsigned int vox_mtree_items(const struct vox_mtree_node *root);
+/* mtree.h:138-140 -- call callback(s, arg) for every sphere containing dot. */
+void vox_mtree_spheres_containing_f(const struct vox_mtree_node *root, const vox_dot dot,
+                                    void (*callback)(const struct vox_sphere *s, void *arg), void *arg);
+
 #ifdef __cplusplus
 }
 #endif

@@ -137,6 +137,28 @@ int vox_cuda_render_device(const vox_cuda_tree *tree, const vox_cuda_camera *cam
                            uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
                            void *stream);
 
+/* Lights.  A snapshot of a light manager (include/voxrnd.h) on the device;
+ * frames drawn with it are coloured as the reference's get_color with a
+ * light manager (renderer.c:40-49, lights.c:91-116): ambient light plus the
+ * contribution of every light sphere containing the hit, summed in the
+ * M-tree's order, min(light, 1) * texel per channel.  Changes to the manager
+ * after the upload are not seen: upload again.  M-trees deeper than 9
+ * levels: VOX_CUDA_EDEPTH.  No counterpart in the reference beyond the
+ * drop-in context (vox_context_set_light_manager), which uses these. */
+typedef struct vox_cuda_lights vox_cuda_lights;
+struct vox_light_manager;
+int vox_cuda_lights_upload(const struct vox_light_manager *light_manager, vox_cuda_lights **out);
+int vox_cuda_lights_free(vox_cuda_lights *lights);
+/* A frame of any quality lit by `lights` (NULL: grey texels, as
+ * vox_cuda_render_quality); host buffers as vox_cuda_render, device
+ * buffers as vox_cuda_render_device. */
+int vox_cuda_render_lit(const vox_cuda_tree *tree, const vox_cuda_camera *camera, uint32_t w, uint32_t h,
+                        unsigned int quality, const uint8_t *texture, const vox_cuda_lights *lights,
+                        uint32_t *argb, void *stream);
+int vox_cuda_render_lit_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera, uint32_t w, uint32_t h,
+                               unsigned int quality, const uint8_t *texture, const vox_cuda_lights *lights,
+                               uint32_t *argb, void *stream);
+
 /* Settings of the BEST-quality frame kernel behind vox_cuda_render*,
  * process-wide (no counterpart in the reference, whose renderer has no
  * kernel).  cull = 1: trace only the rectangle of vox_cuda_frame_rect for the

@@ -7,7 +7,8 @@
  *   src/voxtrees/tree.c      vox_make_tree and its scalar helpers
  *   src/voxtrees/geom.c      hit_box, hit_plane_within_box, metrics, ...
  *   src/voxtrees/search.c    vox_ray_tree_intersection, vox_tree_ball_collidep
- *   src/voxrnd/renderer.c    vox_render (BEST branch), get_color
+ *   src/voxrnd/renderer.c    vox_render (every quality), get_color
+ *   src/voxrnd/lights.c      the light manager; src/voxtrees/mtree.c its M-tree
  *   src/voxrnd/simple-camera.c, doom-camera.c, vect-ops.c   screen2world
  */
 #include "oracle.h"
@@ -564,15 +565,346 @@ void orc_screen2world(const orc_camera *cam, int sx, int sy, float *ray)
     for (int i = 0; i < 3; i++) ray[i] = v[i] + cam->rotation[0] * t[i] + t2[i];
 }
 
-/* renderer.c:27-39 get_color, no light manager; SDL_MapRGB on ARGB8888 */
-static uint32_t get_color(const uint8_t *tex, const float *inter)
+/* ------------------------------------------------------------------ */
+/* light manager and its M-tree (src/voxrnd/lights.c,                  */
+/* src/voxtrees/mtree.c), restated recursively as the reference has it  */
+/* ------------------------------------------------------------------ */
+
+#define ORC_MT_MAX 9                                  /* mtree.h:44 */
+
+typedef struct {                                      /* mtree.h:17-40 */
+    float center[3], color[3], radius, sqr_radius;
+} orc_sphere;
+
+typedef struct orc_mt {                               /* mtree.h:46-56 */
+    orc_sphere bs;
+    struct orc_mt *parent;
+    unsigned leaf, num;
+    struct orc_mt *children[ORC_MT_MAX + 1];
+    orc_sphere *spheres;
+} orc_mt;
+
+struct orc_lights {                                   /* lights.c:11-14 */
+    float ambient[3];
+    orc_mt *root;
+};
+
+static orc_mt *mt_alloc(int leaf)                     /* mtree.c:11-19 */
+{
+    orc_mt *n = calloc(1, sizeof *n);
+    n->leaf = leaf;
+    if (leaf) n->spheres = calloc(ORC_MT_MAX + 1, sizeof(orc_sphere));
+    return n;
+}
+
+static const orc_sphere *mt_item(const orc_mt *n, unsigned i)
+{
+    return n->leaf ? &n->spheres[i] : &n->children[i]->bs;
+}
+
+static int mt_bounding(const orc_sphere *s, orc_sphere *b)   /* mtree.c:21-56, scalar branch */
+{
+    float dist = sqrtf(sqr_metric(s->center, b->center));
+    float crit = (1 + (b->radius - s->radius) / dist) / 2;
+    int changed = 1;
+    if (crit < 0) {
+        *b = *s;
+    } else if (crit < 1) {
+        b->radius = (s->radius + b->radius + dist) / 2;
+        b->sqr_radius = pow(b->radius, 2);
+        for (int i = 0; i < 3; i++) b->center[i] = b->center[i] - s->center[i];   /* vox_dot_sub */
+        for (int i = 0; i < 3; i++) b->center[i] = crit * b->center[i];           /* vox_dot_scmul */
+        for (int i = 0; i < 3; i++) b->center[i] = b->center[i] + s->center[i];   /* vox_dot_add */
+    } else {
+        changed = 0;
+    }
+    return changed;
+}
+
+static int mt_node_bounding(orc_mt *n)                /* mtree.c:58-74 */
+{
+    int changed = 0;
+    n->bs = *mt_item(n, 0);
+    for (unsigned i = 1; i < n->num; i++) changed += mt_bounding(mt_item(n, i), &n->bs);
+    return !!changed;
+}
+
+static void mt_propagate(orc_mt *n)                   /* mtree.c:76-87 */
+{
+    if (n != NULL && mt_node_bounding(n)) mt_propagate(n->parent);
+}
+
+static orc_mt *mt_split(orc_mt *n)                    /* mtree.c:89-180 */
+{
+    float c1[3], c2[3], maxd = 0;
+    memcpy(c1, mt_item(n, 0)->center, 12);            /* defined when all centres coincide */
+    memcpy(c2, mt_item(n, 0)->center, 12);
+    for (unsigned i = 0; i < n->num; i++)
+        for (unsigned j = i + 1; j < n->num; j++) {
+            float d = sqr_metric(mt_item(n, i)->center, mt_item(n, j)->center);
+            if (d > maxd) { memcpy(c1, mt_item(n, i)->center, 12); memcpy(c2, mt_item(n, j)->center, 12); maxd = d; }
+        }
+    orc_mt *parent = n->parent, *res = parent;
+    orc_mt *n1 = mt_alloc(n->leaf), *n2 = mt_alloc(n->leaf);
+    n1->parent = n2->parent = parent;
+    for (unsigned i = 0; i < n->num; i++) {
+        float d1 = sqr_metric(mt_item(n, i)->center, c1), d2 = sqr_metric(mt_item(n, i)->center, c2);
+        orc_mt *w = d1 < d2 ? n1 : n2;
+        if (n->leaf) w->spheres[w->num] = n->spheres[i];
+        else { w->children[w->num] = n->children[i]; n->children[i]->parent = w; }
+        w->num++;
+    }
+    mt_node_bounding(n1);
+    mt_node_bounding(n2);
+    if (parent) {
+        for (unsigned i = 0; i < parent->num; i++)
+            if (parent->children[i] == n) parent->children[i] = n1;
+        parent->children[parent->num++] = n2;
+        mt_propagate(parent);
+        if (parent->num == ORC_MT_MAX + 1) res = mt_split(parent);
+    } else {
+        res = mt_alloc(0);
+        res->num = 2;
+        res->children[0] = n1;
+        res->children[1] = n2;
+        mt_node_bounding(res);
+        n1->parent = n2->parent = res;
+    }
+    free(n->spheres);
+    free(n);
+    return res;
+}
+
+static orc_mt *mt_contains(orc_mt *n, const orc_sphere *s)   /* mtree.c:182-216 */
+{
+    if (n == NULL || !(sqr_metric(s->center, n->bs.center) < n->bs.sqr_radius)) return NULL;
+    if (n->leaf) {
+        for (unsigned i = 0; i < n->num; i++)
+            if (memcmp(n->spheres[i].center, s->center, 12) == 0 && n->spheres[i].radius == s->radius) return n;
+        return NULL;
+    }
+    for (unsigned i = 0; i < n->num; i++) {
+        orc_mt *r = mt_contains(n->children[i], s);
+        if (r) return r;
+    }
+    return NULL;
+}
+
+static orc_mt *mt_add(orc_mt *n, const orc_sphere *s)        /* mtree.c:218-253 */
+{
+    orc_mt *res = n;
+    float sqr_radius = pow(s->radius, 2);
+    if (n == NULL) {
+        res = mt_alloc(1);
+        res->bs = *s;
+        res->bs.sqr_radius = sqr_radius;
+        res->num = 1;
+        res->spheres[0] = *s;
+        res->spheres[0].sqr_radius = sqr_radius;
+    } else if (n->leaf) {
+        n->spheres[n->num] = *s;
+        n->spheres[n->num].sqr_radius = sqr_radius;
+        n->num++;
+        mt_propagate(n);
+        if (n->num == ORC_MT_MAX + 1) res = mt_split(n);
+    } else {
+        orc_mt *child = n->children[0];
+        float mind = INFINITY;
+        for (unsigned i = 0; i < n->num; i++) {
+            float d = sqr_metric(s->center, n->children[i]->bs.center);
+            if (d < mind) { mind = d; child = n->children[i]; }
+        }
+        res = mt_add(child, s);
+    }
+    return res;
+}
+
+static void mt_free(orc_mt *n)
+{
+    if (!n) return;
+    if (n->leaf) free(n->spheres);
+    else for (unsigned i = 0; i < n->num; i++) mt_free(n->children[i]);
+    free(n);
+}
+
+static orc_mt *mt_delete_leaf(orc_mt *n)              /* mtree.c:269-322 */
+{
+    orc_mt *parent = n->parent;
+    mt_free(n);
+    if (parent == NULL) return NULL;
+    unsigned i;
+    for (i = 0; i < parent->num; i++)
+        if (parent->children[i] == n) break;
+    if (parent->num == 2) {
+        orc_mt *other = parent->children[1 - i], *top = parent->parent;
+        free(parent);
+        other->parent = top;
+        if (top == NULL) return other;
+        for (i = 0; i < top->num; i++)
+            if (top->children[i] == parent) break;
+        top->children[i] = other;
+        mt_propagate(top);
+        return top;
+    }
+    parent->num--;
+    memmove(&parent->children[i], &parent->children[i + 1], sizeof(orc_mt *) * (parent->num - i));
+    parent->children[parent->num] = NULL;
+    mt_propagate(parent);
+    return parent;
+}
+
+orc_lights *orc_lights_new(void)                      /* lights.c:16-23 */
+{
+    orc_lights *l = calloc(1, sizeof *l);
+    l->ambient[0] = l->ambient[1] = l->ambient[2] = 1;
+    return l;
+}
+
+void orc_lights_free(orc_lights *l)
+{
+    if (!l) return;
+    mt_free(l->root);
+    free(l);
+}
+
+static int valid_light(const float *c)                /* lights.c:81-89 */
+{
+    for (int i = 0; i < 3; i++)
+        if (c[i] < 0 || c[i] > 1) return 0;
+    return 1;
+}
+
+int orc_lights_ambient(orc_lights *l, const float *color)
+{
+    if (!valid_light(color)) return 0;
+    memcpy(l->ambient, color, 12);
+    return 1;
+}
+
+int orc_lights_insert(orc_lights *l, const float *center, float radius, const float *color)
+{
+    if (!valid_light(color)) return 0;                /* lights.c:46-58 */
+    orc_sphere s;
+    memset(&s, 0, sizeof s);
+    memcpy(s.center, center, 12);
+    memcpy(s.color, color, 12);
+    s.radius = radius;
+    if (!(s.radius > 0) || mt_contains(l->root, &s)) return 0;   /* mtree.c:255-267 */
+    orc_mt *n = mt_add(l->root, &s);
+    if (n->parent == NULL) l->root = n;
+    return 1;
+}
+
+int orc_lights_delete(orc_lights *l, const float *center, float radius)
+{
+    orc_sphere s;                                     /* lights.c:60-68, mtree.c:324-368 */
+    memset(&s, 0, sizeof s);
+    memcpy(s.center, center, 12);
+    s.radius = radius;
+    orc_mt *leaf = mt_contains(l->root, &s);
+    if (!(s.radius > 0) || leaf == NULL) return 0;
+    orc_mt *last = leaf;
+    if (leaf->num == 1) {
+        last = mt_delete_leaf(leaf);
+    } else {
+        unsigned i;
+        for (i = 0; i < leaf->num; i++)
+            if (memcmp(leaf->spheres[i].center, s.center, 12) == 0 && leaf->spheres[i].radius == s.radius) break;
+        memmove(&leaf->spheres[i], &leaf->spheres[i + 1], sizeof(orc_sphere) * (leaf->num - i - 1));
+        leaf->num--;
+        mt_propagate(leaf);
+    }
+    if (last == NULL || last->parent == NULL) l->root = last;
+    return 1;
+}
+
+static unsigned mt_items(const orc_mt *n)
+{
+    if (!n) return 0;
+    if (n->leaf) return n->num;
+    unsigned c = 0;
+    for (unsigned i = 0; i < n->num; i++) c += mt_items(n->children[i]);
+    return c;
+}
+
+int orc_lights_count(const orc_lights *l) { return (int)mt_items(l->root); }
+
+typedef struct { float inter[3], color[3]; int n; } light_acc;
+
+static void light_cb(const orc_sphere *s, light_acc *a)   /* lights.c:91-102 */
+{
+    float dist = fminf(s->radius, sqrtf(sqr_metric(s->center, a->inter)));
+    float add = 1 - dist / s->radius;
+    a->color[0] = a->color[0] + add * s->color[0];
+    a->color[1] = a->color[1] + add * s->color[1];
+    a->color[2] = a->color[2] + add * s->color[2];
+    a->n++;
+}
+
+static void mt_search(const orc_mt *n, light_acc *a)   /* mtree.c:463-493 */
+{
+    if (n == NULL || !(sqr_metric(n->bs.center, a->inter) < n->bs.sqr_radius)) return;
+    if (n->leaf) {
+        if (n->num == 1) { light_cb(&n->spheres[0], a); return; }
+        for (unsigned i = 0; i < n->num; i++)
+            if (sqr_metric(n->spheres[i].center, a->inter) < n->spheres[i].sqr_radius) light_cb(&n->spheres[i], a);
+        return;
+    }
+    for (unsigned i = 0; i < n->num; i++) mt_search(n->children[i], a);
+}
+
+int orc_lights_get(const orc_lights *l, const float *p, float *light)   /* lights.c:104-116 */
+{
+    light_acc a;
+    memcpy(a.inter, p, 12);
+    memcpy(a.color, l->ambient, 12);
+    a.n = 0;
+    mt_search(l->root, &a);
+    memcpy(light, a.color, 12);
+    return a.n;
+}
+
+/* The reference's own M-tree invariants (tests/tests.c:779-808): at most
+ * MAX items a node, inner nodes with two or more children whose parent link
+ * points back, every item inside its node's bounding sphere within 0.5.
+ * Returns 0 when they hold. */
+static int mt_verify(const orc_mt *n)
+{
+    if (!n) return 0;
+    if (n->num > ORC_MT_MAX) return 1;
+    for (unsigned i = 0; i < n->num; i++) {
+        const orc_sphere *s = mt_item(n, i);
+        float dist = sqrtf(sqr_metric(s->center, n->bs.center));
+        if (!(s->radius + dist < n->bs.radius + 0.5f)) return 2;
+        if (!n->leaf) {
+            if (n->num < 2 || n->children[i] == NULL || n->children[i]->parent != n) return 3;
+            if (mt_verify(n->children[i])) return 4;
+        }
+    }
+    return 0;
+}
+
+int orc_lights_verify(const orc_lights *l) { return mt_verify(l->root); }
+
+/* renderer.c:27-52 get_color; SDL_MapRGB on ARGB8888.  Without a light
+ * manager the texel is grey; with one, min(light, 1) * texel per channel,
+ * converted to 8 bits as C converts a float to Uint8 (truncation). */
+static uint32_t get_color_lit(const uint8_t *tex, const orc_lights *lights, const float *inter)
 {
     int x = abs((int)(inter[0] / orc_voxel[0])) & 31;
     int y = abs((int)(inter[1] / orc_voxel[1])) & 31;
     int z = abs((int)(inter[2] / orc_voxel[2])) & 31;
-    uint32_t c = tex[x * 1024 + y * 32 + z];
-    return 0xFF000000u | (c << 16) | (c << 8) | c;
+    uint8_t c = tex[x * 1024 + y * 32 + z];
+    if (lights == NULL) return 0xFF000000u | ((uint32_t)c << 16) | ((uint32_t)c << 8) | c;
+    float light[3];
+    orc_lights_get(lights, inter, light);
+    uint8_t r = fminf(light[0], 1.0) * c;
+    uint8_t g = fminf(light[1], 1.0) * c;
+    uint8_t b = fminf(light[2], 1.0) * c;
+    return 0xFF000000u | ((uint32_t)r << 16) | ((uint32_t)g << 8) | b;
 }
+
+static uint32_t get_color(const uint8_t *tex, const float *inter) { return get_color_lit(tex, NULL, inter); }
 
 static const int zorder[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}; /* renderer.c:23-25 */
 
@@ -618,6 +950,7 @@ typedef struct {
     unsigned quality;
     const uint8_t *tex;
     uint32_t *argb;
+    const orc_lights *lights;
 } quality_ctx;
 
 static float sqr_norm(const float *a)
@@ -647,11 +980,11 @@ static void quality_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
             leaf = c1;
             if (c1) {
                 iend = 15;
-                out[0] = get_color(x->tex, inter1);
+                out[0] = get_color_lit(x->tex, x->lights, inter1);
                 orc_screen2world(x->cam, xstart + 3, ystart + 3, dir2);
                 const struct orc_node *c2 = orc_ray(x->tree, origin, dir2, inter2, NULL, c);
                 if (c2) {
-                    out[15] = get_color(x->tex, inter2);
+                    out[15] = get_color_lit(x->tex, x->lights, inter2);
                     float d1 = sqr_metric(inter1, origin);
                     float d2 = sqr_norm(dir1);
                     float criteria = d1 / d2 * sqr_metric(dir1, dir2);
@@ -677,7 +1010,7 @@ static void quality_work(void *vctx, size_t lo, size_t hi, orc_counts *c)
                     leaf = orc_ray(x->tree, origin, dir1, inter1, NULL, c);
                 }
             }
-            if (leaf) out[p] = merge ? out[prev_p] : get_color(x->tex, inter1);
+            if (leaf) out[p] = merge ? out[prev_p] : get_color_lit(x->tex, x->lights, inter1);
             prev_p = p;
         }
         for (int i = 0; i < 16; i++)
@@ -690,8 +1023,17 @@ int orc_render_quality(const struct orc_node *tree, const orc_camera *cam, int w
                        uint64_t *counts3, int nthreads)
 {
     if ((w & 0xf) || (h & 0x3)) return -1;
-    quality_ctx x = {tree, cam, w, w / 4, quality, texture, argb};
+    quality_ctx x = {tree, cam, w, w / 4, quality, texture, argb, NULL};
     run_pool((size_t)(w / 4) * (size_t)(h / 4), 64, nthreads, quality_work, &x, counts3);
+    return 0;
+}
+
+int orc_render_lit(const struct orc_node *tree, const orc_camera *cam, int w, int h, unsigned quality,
+                   const uint8_t *texture, const orc_lights *lights, uint32_t *argb, int nthreads)
+{
+    if ((w & 0xf) || (h & 0x3)) return -1;
+    quality_ctx x = {tree, cam, w, w / 4, quality, texture, argb, lights};
+    run_pool((size_t)(w / 4) * (size_t)(h / 4), 64, nthreads, quality_work, &x, NULL);
     return 0;
 }
 

@@ -110,6 +110,26 @@ int orc_render_quality(const struct orc_node *tree, const orc_camera *cam,
                        int w, int h, unsigned quality, const uint8_t *texture,
                        uint32_t *argb, uint64_t *counts3, int nthreads);
 
+/* Light manager (lights.c) with its M-tree (mtree.c), and frames of any
+ * quality coloured with it (renderer.c:27-52).  The M-tree code of the
+ * reference needs clang blocks and cannot be compiled here, so this
+ * restatement is checked against the reference's own M-tree test
+ * properties (orc_lights_verify, tests/tests.c:779-900) and against the
+ * product's independent restatement through the GPU tests. */
+typedef struct orc_lights orc_lights;
+orc_lights *orc_lights_new(void);
+void orc_lights_free(orc_lights *l);
+int orc_lights_ambient(orc_lights *l, const float *color);
+int orc_lights_insert(orc_lights *l, const float *center, float radius, const float *color);
+int orc_lights_delete(orc_lights *l, const float *center, float radius);
+int orc_lights_count(const orc_lights *l);
+/* vox_get_light: writes the light at p; returns how many spheres contain p. */
+int orc_lights_get(const orc_lights *l, const float *p, float *light);
+/* 0 when the reference's M-tree invariants hold. */
+int orc_lights_verify(const orc_lights *l);
+int orc_render_lit(const struct orc_node *tree, const orc_camera *cam, int w, int h, unsigned quality,
+                   const uint8_t *texture, const orc_lights *lights, uint32_t *argb, int nthreads);
+
 /* Pre-order dump of a tree: per node flags, dots_num, box (6 floats), centre
  * (3 floats, inner nodes), child mask (inner nodes) and an offset into the
  * dots array (leaves).  Returns the node count; arrays must be sized by

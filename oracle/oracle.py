@@ -56,6 +56,16 @@ def lib():
                                          vp, C.c_int]
         L.orc_render_quality.restype = C.c_int
         L.orc_ray_counts_per_ray.argtypes = [vp, sz, fp, fp, vp, C.c_int]
+        L.orc_lights_new.restype = vp
+        L.orc_lights_free.argtypes = [vp]
+        L.orc_lights_ambient.argtypes = [vp, fp]; L.orc_lights_ambient.restype = C.c_int
+        L.orc_lights_insert.argtypes = [vp, fp, C.c_float, fp]; L.orc_lights_insert.restype = C.c_int
+        L.orc_lights_delete.argtypes = [vp, fp, C.c_float]; L.orc_lights_delete.restype = C.c_int
+        L.orc_lights_count.argtypes = [vp]; L.orc_lights_count.restype = C.c_int
+        L.orc_lights_get.argtypes = [vp, fp, fp]; L.orc_lights_get.restype = C.c_int
+        L.orc_lights_verify.argtypes = [vp]; L.orc_lights_verify.restype = C.c_int
+        L.orc_render_lit.argtypes = [vp, C.POINTER(OrcCamera), C.c_int, C.c_int, C.c_uint, vp, vp, vp, C.c_int]
+        L.orc_render_lit.restype = C.c_int
         L.orc_dump.argtypes = [vp] * 8; L.orc_dump.restype = sz
         L.orc_from_dump.argtypes = [sz] + [vp] * 7; L.orc_from_dump.restype = vp
         _lib = L
@@ -199,3 +209,50 @@ def ray_counts_per_ray(root_ptr, origins, dirs, nthreads=None):
     out = np.zeros((o.shape[0], 3), np.uint32)
     lib().orc_ray_counts_per_ray(root_ptr, o.shape[0], _p(o), _p(d), _p(out), nthreads or nthreads_default())
     return out
+
+
+def _f3(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(3))
+
+
+class OracleLights:
+    """The oracle's light manager (lights.c / mtree.c restated)."""
+
+    def __init__(self):
+        self.ptr = lib().orc_lights_new()
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().orc_lights_free(self.ptr)
+            self.ptr = None
+
+    def ambient(self, color) -> bool:
+        return bool(lib().orc_lights_ambient(self.ptr, _p(_f3(color))))
+
+    def insert(self, center, radius, color) -> bool:
+        return bool(lib().orc_lights_insert(self.ptr, _p(_f3(center)), float(radius), _p(_f3(color))))
+
+    def delete(self, center, radius) -> bool:
+        return bool(lib().orc_lights_delete(self.ptr, _p(_f3(center)), float(radius)))
+
+    def count(self) -> int:
+        return int(lib().orc_lights_count(self.ptr))
+
+    def light(self, p):
+        """(light rgb, number of spheres containing p)."""
+        out = np.zeros(3, np.float32)
+        n = lib().orc_lights_get(self.ptr, _p(_f3(p)), _p(out))
+        return out, int(n)
+
+    def verify(self) -> int:
+        return int(lib().orc_lights_verify(self.ptr))
+
+
+def render_lit(tree_ptr, state: dict, w: int, h: int, quality: int, texture: np.ndarray, lights, nthreads=None):
+    tex = np.ascontiguousarray(texture, dtype=np.uint8)
+    out = np.zeros(w * h, np.uint32)
+    rc = lib().orc_render_lit(tree_ptr, C.byref(camera(state)), w, h, quality, _p(tex),
+                              lights.ptr if lights is not None else None, _p(out), nthreads or nthreads_default())
+    if rc != 0:
+        raise ValueError("bad geometry: width must be a multiple of 16 and height of 4")
+    return out.reshape(h, w)

@@ -19,7 +19,7 @@ from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENS
 
 __all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Server", "ServerConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
            "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size",
-           "frame_rect", "render_config", "set_render_config"]
+           "frame_rect", "render_config", "set_render_config", "LightManager", "DeviceLights"]
 
 
 def _p(a: np.ndarray):
@@ -145,6 +145,16 @@ class DeviceTree:
         return out
 
     # -------------------------------------------------------- device buffers
+    def render_lit(self, camera: CameraStruct, w: int, h: int, quality: int, texture: np.ndarray,
+                   lights: "DeviceLights | None", stream=None):
+        """vox_cuda_render_lit with host buffers: (h, w) uint32 ARGB."""
+        tex = np.ascontiguousarray(texture, dtype=np.uint8)
+        out = np.empty(w * h, np.uint32)
+        check(lib().vox_cuda_render_lit(self.h, C.byref(camera), w, h, quality, _p(tex),
+                                        lights.h if lights is not None else None, _p(out), stream),
+              "vox_cuda_render_lit")
+        return out.reshape(h, w)
+
     def rays_device(self, origins, dirs, leaf, slot=None, points=None, roots=None, n=None, stream=None):
         n = int(origins.shape[0]) if n is None else n
         check(lib().vox_cuda_ray_batch_device(self.h, _dptr(origins), _dptr(dirs), _dptr(roots), n,
@@ -188,6 +198,68 @@ def camera_struct(state: dict) -> CameraStruct:
 
 
 Camera = CameraStruct
+
+
+def _f3(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(3))
+
+
+class LightManager:
+    """The library's light manager (include/voxrnd.h, lights.h of the reference)."""
+
+    def __init__(self):
+        self.ptr = lib().vox_make_light_manager()
+        if not self.ptr:
+            raise MemoryError("vox_make_light_manager")
+
+    def close(self):
+        if self.ptr:
+            lib().vox_destroy_light_manager(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ambient(self, color) -> bool:
+        return bool(lib().vox_set_ambient_light(self.ptr, _p(_f3(color))))
+
+    def insert(self, center, radius, color) -> bool:
+        return bool(lib().vox_insert_shadowless_light(self.ptr, _p(_f3(center)), float(radius), _p(_f3(color))))
+
+    def delete(self, center, radius) -> bool:
+        return bool(lib().vox_delete_shadowless_light(self.ptr, _p(_f3(center)), float(radius)))
+
+    def clear(self):
+        lib().vox_delete_shadowless_lights(self.ptr)
+
+    def count(self) -> int:
+        return int(lib().vox_shadowless_lights_number(self.ptr))
+
+    def upload(self) -> "DeviceLights":
+        return DeviceLights(self)
+
+
+class DeviceLights:
+    """vox_cuda_lights: a snapshot of a LightManager on the device."""
+
+    def __init__(self, manager: LightManager):
+        h = C.c_void_p()
+        check(lib().vox_cuda_lights_upload(manager.ptr, C.byref(h)), "vox_cuda_lights_upload")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().vox_cuda_lights_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def frame_rect(bbox, cam: CameraStruct, w: int, h: int):

@@ -114,6 +114,11 @@ SIGNATURES = {
     "vox_cuda_frame_rect": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, _vp]),
     "vox_cuda_render_set_config": (C.c_int, [C.POINTER(RenderConfig)]),
     "vox_cuda_render_get_config": (C.c_int, [C.POINTER(RenderConfig)]),
+    "vox_cuda_lights_upload": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "vox_cuda_lights_free": (C.c_int, [_vp]),
+    "vox_cuda_render_lit": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp, _vp, _vp, _vp]),
+    "vox_cuda_render_lit_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp, _vp, _vp,
+                                             _vp]),
     "vox_cuda_batch_create": (C.c_int, [C.POINTER(FrameJob), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
     "vox_cuda_batch_set_camera": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct)]),
     "vox_cuda_batch_launch": (C.c_int, [_vp, _vp]),
@@ -161,6 +166,14 @@ SIGNATURES = {
     "vox_redraw": (None, [_vp]),
     "vox_context_pixels": (_vp, [_vp]),
     "vox_context_status": (C.c_int, [_vp]),
+    "vox_make_light_manager": (_vp, []),
+    "vox_destroy_light_manager": (None, [_vp]),
+    "vox_set_ambient_light": (C.c_int, [_vp, _vp]),
+    "vox_insert_shadowless_light": (C.c_int, [_vp, _vp, _f, _vp]),
+    "vox_delete_shadowless_light": (C.c_int, [_vp, _vp, _f]),
+    "vox_delete_shadowless_lights": (None, [_vp]),
+    "vox_shadowless_lights_number": (C.c_int, [_vp]),
+    "vox_context_set_light_manager": (None, [_vp, _vp]),
     "vox_make_cd": (_vp, []),
     "vox_cd_attach_camera": (None, [_vp, _vp, _f]),
     "vox_cd_attach_context": (None, [_vp, _vp]),

@@ -28,7 +28,7 @@ CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-fvisibility=hidden", "-ffp-contract=
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall"]
 
 CUDA_SOURCES = ["voxtrees_cuda.cu", "batch.cu", "server.cu"]
-C_SOURCES = ["host_tree.c", "cameras.c"]
+C_SOURCES = ["host_tree.c", "cameras.c", "lights.c"]
 CXX_SOURCES = ["flatten.cpp", "dropin_search.cpp", "renderer.cpp"]
 
 

@@ -17,6 +17,7 @@
 
 #include "../../include/voxrnd.h"
 #include "../../include/voxtrees_cuda.h"
+#include "lights_internal.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -41,6 +42,9 @@ struct vox_rnd_ctx {
     uint32_t *pixels = nullptr;                    // what vox_context_pixels returns
     cudaStream_t stream = nullptr;
     int status = VOX_CUDA_OK;
+    struct vox_light_manager *lights = nullptr;    // renderer.h:66
+    vox_cuda_lights *d_lights = nullptr;           // its device copy
+    uint64_t d_lights_version = 0;                 // the manager's version that copy holds
 };
 
 namespace {
@@ -62,6 +66,7 @@ void default_texture(uint8_t *tex)
 
 void release(vox_rnd_ctx *c)
 {
+    if (c->d_lights) vox_cuda_lights_free(c->d_lights);
     if (c->tree) vox_cuda_tree_free(c->tree);
     if (c->d_tex) cudaFree(c->d_tex);
     if (c->d_frame) cudaFree(c->d_frame);
@@ -131,6 +136,11 @@ EXPORT void vox_context_set_texture(struct vox_rnd_ctx *ctx, const uint8_t *text
     ctx->tex_dirty = true;
 }
 
+EXPORT void vox_context_set_light_manager(struct vox_rnd_ctx *ctx, struct vox_light_manager *light_manager)
+{
+    ctx->lights = light_manager;   // renderer.c:174-177; copied to the device at the next vox_render
+}
+
 EXPORT void vox_render(struct vox_rnd_ctx *ctx)
 {
     ctx->status = VOX_CUDA_EINVAL;
@@ -150,8 +160,19 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
             cudaSuccess) { ctx->status = VOX_CUDA_ECUDA; return; }
         ctx->tex_dirty = false;
     }
-    int rc = vox_cuda_render_quality_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
-                                            ctx->d_frame, ctx->stream);
+    if (ctx->lights && (!ctx->d_lights || ctx->d_lights_version != ctx->lights->version)) {
+        // the manager changed since the last frame (or is new): upload it again
+        if (ctx->d_lights) {
+            cudaStreamSynchronize(ctx->stream);
+            vox_cuda_lights_free(ctx->d_lights);
+            ctx->d_lights = nullptr;
+        }
+        int rc = vox_cuda_lights_upload(ctx->lights, &ctx->d_lights);
+        if (rc) { ctx->status = rc; return; }
+        ctx->d_lights_version = ctx->lights->version;
+    }
+    int rc = vox_cuda_render_lit_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
+                                        ctx->lights ? ctx->d_lights : nullptr, ctx->d_frame, ctx->stream);
     if (rc) { ctx->status = rc; return; }
     size_t bytes = (size_t)ctx->w * ctx->h * 4;
     if (cudaMemcpyAsync(ctx->h_stage, ctx->d_frame, bytes, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||

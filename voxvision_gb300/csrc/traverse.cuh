@@ -442,6 +442,97 @@ __device__ __forceinline__ uint32_t texel_color(const uint8_t *__restrict__ tex,
     return 0xFF000000u | (c << 16) | (c << 8) | c;
 }
 
+/* Lights of a light manager on the device (layout: lights_internal.h).
+ * nodes == nullptr: no bound lights, ambient only. */
+struct DevLights {
+    const float4 *nodes;     // 2 per M-tree node
+    const float4 *spheres;   // 2 per light sphere
+    float ar, ag, ab;        // ambient light
+    uint32_t on;             // 0: draw without lights (grey texels)
+};
+
+constexpr int LIGHT_STACK = 64;   // (children - 1) per level; the upload refuses deeper trees
+
+/* geom.c:133-139 vox_sqr_metric: ((dx*dx + dy*dy) + dz*dz). */
+__device__ __forceinline__ float sqr_dist(float ax, float ay, float az, float bx, float by, float bz)
+{
+    float x = __fsub_rn(ax, bx), y = __fsub_rn(ay, by), z = __fsub_rn(az, bz);
+    return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+}
+
+/* lights.c:91-102 get_color_callback: the light of one sphere containing p. */
+__device__ __forceinline__ void add_light(const float4 &sa, const float4 &sb, float px, float py, float pz,
+                                          float &r, float &g, float &b)
+{
+    float dist = fminf(sb.w, __fsqrt_rn(sqr_dist(sa.x, sa.y, sa.z, px, py, pz)));
+    float add = __fsub_rn(1.0f, __fdiv_rn(dist, sb.w));
+    r = __fadd_rn(r, __fmul_rn(add, sb.x));
+    g = __fadd_rn(g, __fmul_rn(add, sb.y));
+    b = __fadd_rn(b, __fmul_rn(add, sb.z));
+}
+
+/* renderer.c:40-49 with lights.c:104-116 (vox_get_light) and
+ * mtree.c:463-493 (vox_mtree_spheres_containing_f): ambient light plus the
+ * spheres containing the hit, in the M-tree's depth-first order (a
+ * one-sphere leaf whose bounding sphere holds the hit counts its sphere
+ * without a second test), then min(light, 1) * texel per channel, truncated
+ * to 8 bits.  `overflow` is set if the search stack would overflow. */
+__device__ __forceinline__ uint32_t lit_color(const DevLights &L, uint32_t c, float px, float py, float pz,
+                                              bool &overflow)
+{
+    float r = L.ar, g = L.ag, b = L.ab;
+    if (L.nodes) {
+        uint32_t stack[LIGHT_STACK];
+        int sp = 0;
+        uint32_t cur = 0;
+        for (;;) {
+            float4 na = L.nodes[2 * cur];
+            float4 nb = L.nodes[2 * cur + 1];
+            uint32_t leaf = __float_as_uint(nb.x), num = __float_as_uint(nb.y), first = __float_as_uint(nb.z);
+            bool next_from_stack = true;
+            if (sqr_dist(na.x, na.y, na.z, px, py, pz) < na.w) {
+                if (leaf) {
+                    if (num == 1) {
+                        add_light(L.spheres[2 * first], L.spheres[2 * first + 1], px, py, pz, r, g, b);
+                    } else {
+                        for (uint32_t i = 0; i < num; i++) {
+                            float4 sa = L.spheres[2 * (first + i)];
+                            if (sqr_dist(sa.x, sa.y, sa.z, px, py, pz) < sa.w)
+                                add_light(sa, L.spheres[2 * (first + i) + 1], px, py, pz, r, g, b);
+                        }
+                    }
+                } else if (num > 0) {
+                    if (sp + (int)num - 1 > LIGHT_STACK) { overflow = true; break; }
+                    for (uint32_t i = num - 1; i >= 1; i--) stack[sp++] = first + i;
+                    cur = first;
+                    next_from_stack = false;
+                }
+            }
+            if (next_from_stack) {
+                if (sp == 0) break;
+                cur = stack[--sp];
+            }
+        }
+    }
+    uint32_t R = __float2uint_rz(__fmul_rn(fminf(r, 1.0f), (float)c));
+    uint32_t G = __float2uint_rz(__fmul_rn(fminf(g, 1.0f), (float)c));
+    uint32_t B = __float2uint_rz(__fmul_rn(fminf(b, 1.0f), (float)c));
+    return 0xFF000000u | ((R & 0xFFu) << 16) | ((G & 0xFFu) << 8) | (B & 0xFFu);
+}
+
+/* renderer.c:27-52 get_color: the texel of the hit point, grey without a
+ * light manager (SDL_MapRGB on ARGB8888), lit with one. */
+__device__ __forceinline__ uint32_t hit_color(const uint8_t *__restrict__ tex, const DevTree &t, const DevLights &L,
+                                              float x, float y, float z, bool &overflow)
+{
+    int ix = abs(__float2int_rz(__fdiv_rn(x, t.vx))) & 31;
+    int iy = abs(__float2int_rz(__fdiv_rn(y, t.vy))) & 31;
+    int iz = abs(__float2int_rz(__fdiv_rn(z, t.vz))) & 31;
+    uint32_t c = __ldg(tex + ix * 1024 + iy * 32 + iz);
+    if (!L.on) return 0xFF000000u | (c << 16) | (c << 8) | c;
+    return lit_color(L, c, x, y, z, overflow);
+}
+
 }  // namespace vox
 
 #endif

@@ -24,6 +24,7 @@
 #include <new>
 
 #include "flatten.h"
+#include "lights_internal.h"
 #include "internal.h"
 #include "pool_layout.h"
 #include "traverse.cuh"
@@ -133,12 +134,12 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-template <int CAP, bool COUNT, int MINB>
+template <int CAP, bool COUNT, int MINB, bool LIT>
 __global__ void __launch_bounds__(128, MINB) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
                                                      FramePlan p, const uint8_t *__restrict__ tex,
                                                      uint32_t *__restrict__ argb,
                                                      unsigned long long *__restrict__ counts,
-                                                     uint32_t *__restrict__ status)
+                                                     uint32_t *__restrict__ status, vox::DevLights lights)
 {
     pdl_launch_dependents();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -181,7 +182,12 @@ __global__ void __launch_bounds__(128, MINB) render_kernel(DevTree t, vox_cuda_c
     }
     pdl_wait();
     if (mine) {
-        if (!COUNT) argb[(size_t)py * w + px] = hit ? vox::texel_color(tex, t, hh.x, hh.y, hh.z) : 0u;
+        if (!COUNT) {
+            uint32_t colour = 0u;
+            if (hit) colour = LIT ? vox::hit_color(tex, t, lights, hh.x, hh.y, hh.z, overflow)
+                                  : vox::texel_color(tex, t, hh.x, hh.y, hh.z);
+            argb[(size_t)py * w + px] = colour;
+        }
         if (overflow) atomicOr(status, 1u);
     }
     if (COUNT) add_counts(counts, c);
@@ -203,7 +209,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
                                                              uint32_t h, unsigned int quality,
                                                              const uint8_t *__restrict__ tex,
                                                              uint32_t *__restrict__ argb,
-                                                             uint32_t *__restrict__ status)
+                                                             uint32_t *__restrict__ status, vox::DevLights lights)
 {
     const int order[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};   // renderer.c:23-25
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -241,13 +247,13 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
             leaf_rec = h1.rec;
             ix = h1.x; iy = h1.y; iz = h1.z;
             iend = 15;
-            out[0] = vox::texel_color(tex, t, h1.x, h1.y, h1.z);
+            out[0] = vox::hit_color(tex, t, lights, h1.x, h1.y, h1.z, overflow);
             float d2x, d2y, d2z;
             vox::screen2world(cam, xstart + 3, ystart + 3, d2x, d2y, d2z);
             RayHit h2;
             bool c2 = vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d2x, d2y, d2z, h2, c, overflow);
             if (c2) {
-                out[15] = vox::texel_color(tex, t, h2.x, h2.y, h2.z);
+                out[15] = vox::hit_color(tex, t, lights, h2.x, h2.y, h2.z, overflow);
                 float d1 = sqr3(h1.x, h1.y, h1.z, ox, oy, oz);
                 float d2 = sqr3(d1x, d1y, d1z, 0.f, 0.f, 0.f);
                 float criteria = __fmul_rn(__fdiv_rn(d1, d2), sqr3(d1x, d1y, d1z, d2x, d2y, d2z));
@@ -287,7 +293,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
                 ix = hh.x; iy = hh.y; iz = hh.z;
             }
         }
-        if (have_leaf) out[p] = merge ? out[prev_p] : vox::texel_color(tex, t, ix, iy, iz);
+        if (have_leaf) out[p] = merge ? out[prev_p] : vox::hit_color(tex, t, lights, ix, iy, iz, overflow);
         prev_p = p;
     }
 #pragma unroll
@@ -343,25 +349,32 @@ constexpr int MINB_ALONE = 8, MINB_PIPELINED = 12;
 template <bool COUNT>
 cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                           const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s,
-                          bool pipelined = false)
+                          bool pipelined = false, const vox::DevLights *lights = nullptr)
 {
     // the counting kernel counts the reference's work: every pixel traced
     FramePlan p;
     plan_frame(t, cam, w, h, !COUNT && g_render_cull.load(), p);
     void (*kern)(DevTree, vox_cuda_camera, uint32_t, uint32_t, FramePlan, const uint8_t *, uint32_t *,
-                 unsigned long long *, uint32_t *);
-    if (pipelined && !COUNT) {
-        switch (t->cap_class) {
-        case 0: kern = render_kernel<CAP0, COUNT, MINB_PIPELINED>; break;
-        case 1: kern = render_kernel<CAP1, COUNT, MINB_PIPELINED>; break;
-        default: kern = render_kernel<CAP2, COUNT, MINB_PIPELINED>; break;
-        }
+                 unsigned long long *, uint32_t *, vox::DevLights);
+    vox::DevLights L{};
+    if (lights) L = *lights;
+    const bool lit = !COUNT && L.on;
+    const int cap = t->cap_class;
+    if (lit) {
+        if (pipelined) kern = cap == 0 ? render_kernel<CAP0, COUNT, MINB_PIPELINED, true>
+                            : cap == 1 ? render_kernel<CAP1, COUNT, MINB_PIPELINED, true>
+                                       : render_kernel<CAP2, COUNT, MINB_PIPELINED, true>;
+        else kern = cap == 0 ? render_kernel<CAP0, COUNT, MINB_ALONE, true>
+                  : cap == 1 ? render_kernel<CAP1, COUNT, MINB_ALONE, true>
+                             : render_kernel<CAP2, COUNT, MINB_ALONE, true>;
+    } else if (pipelined && !COUNT) {
+        kern = cap == 0 ? render_kernel<CAP0, COUNT, MINB_PIPELINED, false>
+             : cap == 1 ? render_kernel<CAP1, COUNT, MINB_PIPELINED, false>
+                        : render_kernel<CAP2, COUNT, MINB_PIPELINED, false>;
     } else {
-        switch (t->cap_class) {
-        case 0: kern = render_kernel<CAP0, COUNT, MINB_ALONE>; break;
-        case 1: kern = render_kernel<CAP1, COUNT, MINB_ALONE>; break;
-        default: kern = render_kernel<CAP2, COUNT, MINB_ALONE>; break;
-        }
+        kern = cap == 0 ? render_kernel<CAP0, COUNT, MINB_ALONE, false>
+             : cap == 1 ? render_kernel<CAP1, COUNT, MINB_ALONE, false>
+                        : render_kernel<CAP2, COUNT, MINB_ALONE, false>;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.ntiles + p.nclear);
@@ -373,21 +386,24 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = g_render_overlap.load() ? 1 : 0;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, t->dev, cam, w, h, p, tex, argb, counts, t->d_status);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, t->dev, cam, w, h, p, tex, argb, counts, t->d_status, L);
     count_launch();
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
 cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
-                                  unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s)
+                                  unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s,
+                                  const vox::DevLights *lights = nullptr)
 {
     uint32_t ws = w / 4, hs = h / 4;
     dim3 block(128), grid((ws + 15) / 16, (hs + 7) / 8);
+    vox::DevLights L{};
+    if (lights) L = *lights;
     switch (t->cap_class) {
-    case 0: render_squares_kernel<CAP0><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
-    case 1: render_squares_kernel<CAP1><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
-    default: render_squares_kernel<CAP2><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status); break;
+    case 0: render_squares_kernel<CAP0><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L); break;
+    case 1: render_squares_kernel<CAP1><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L); break;
+    default: render_squares_kernel<CAP2><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L); break;
     }
     count_launch();
     return cudaGetLastError();
@@ -986,20 +1002,43 @@ static bool valid_quality(unsigned int q)
     return true;
 }
 
-EXPORT int vox_cuda_render_quality_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
-                                          uint32_t h, unsigned int quality, const uint8_t *tex, uint32_t *argb,
-                                          void *stream)
+// A light manager's snapshot on the device (vox_cuda_lights_upload).
+struct vox_cuda_lights {
+    float4 *d_nodes = nullptr;
+    float4 *d_spheres = nullptr;
+    vox::DevLights dev{};
+};
+
+static int render_any_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                             unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights,
+                             uint32_t *argb, void *stream)
 {
     int rc = check_render_args(t, cam, w, h, tex, argb);
     if (rc) return rc;
     if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
+    const vox::DevLights *L = lights ? &lights->dev : nullptr;
     if ((quality & VOX_CUDA_QUALITY_MODE_MASK) == VOX_CUDA_QUALITY_BEST)
-        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true));
-    return status_of(launch_render_squares(t, *cam, w, h, quality, tex, argb, as_stream(stream)));
+        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true, L));
+    return status_of(launch_render_squares(t, *cam, w, h, quality, tex, argb, as_stream(stream), L));
 }
 
-EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
-                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, void *stream)
+EXPORT int vox_cuda_render_quality_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
+                                          uint32_t h, unsigned int quality, const uint8_t *tex, uint32_t *argb,
+                                          void *stream)
+{
+    return render_any_device(t, cam, w, h, quality, tex, nullptr, argb, stream);
+}
+
+EXPORT int vox_cuda_render_lit_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                                      unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights,
+                                      uint32_t *argb, void *stream)
+{
+    return render_any_device(t, cam, w, h, quality, tex, lights, argb, stream);
+}
+
+static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                           unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights, uint32_t *argb,
+                           void *stream)
 {
     int rc = check_render_args(t, cam, w, h, tex, argb);
     if (rc) return rc;
@@ -1014,7 +1053,7 @@ EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera
     uint32_t *d_argb = in_place ? in_place : static_cast<uint32_t *>(sc.p);
     cudaError_t e = host_call_texture(hc, tex, s);
     if (e == cudaSuccess) {
-        rc = vox_cuda_render_quality_device(t, cam, w, h, quality, hc->d_tex, d_argb, stream);
+        rc = render_any_device(t, cam, w, h, quality, hc->d_tex, lights, d_argb, stream);
         if (rc) {
             host_call_finish(hc, t, s, cudaErrorUnknown);
             return rc;
@@ -1022,4 +1061,67 @@ EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera
         if (!in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
     }
     return host_call_finish(hc, t, s, e);
+}
+
+EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, void *stream)
+{
+    return render_any_host(t, cam, w, h, quality, tex, nullptr, argb, stream);
+}
+
+EXPORT int vox_cuda_render_lit(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                               unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights, uint32_t *argb,
+                               void *stream)
+{
+    return render_any_host(t, cam, w, h, quality, tex, lights, argb, stream);
+}
+
+// ------------------------------------------------------------------ lights
+
+EXPORT int vox_cuda_lights_upload(const struct vox_light_manager *lm, vox_cuda_lights **out)
+{
+    if (!lm || !out) return VOX_CUDA_EINVAL;
+    *out = nullptr;
+    lights_image img;
+    if (lights_flatten(lm, &img)) return VOX_CUDA_ENOMEM;
+    // (children - 1) pending records per level fit the search stack
+    if (img.depth > 1 + vox::LIGHT_STACK / (VOX_MTREE_MAX_CHILDREN - 1)) {
+        lights_image_free(&img);
+        return VOX_CUDA_EDEPTH;
+    }
+    vox_cuda_lights *l = new (std::nothrow) vox_cuda_lights();
+    if (!l) { lights_image_free(&img); return VOX_CUDA_ENOMEM; }
+    l->dev.ar = img.ambient[0];
+    l->dev.ag = img.ambient[1];
+    l->dev.ab = img.ambient[2];
+    l->dev.on = 1;
+    cudaError_t e = cudaSuccess;
+    if (img.n_nodes) {
+        size_t nb = img.n_nodes * 32, sb = (img.n_spheres ? img.n_spheres : 1) * 32;
+        e = cudaMalloc(&l->d_nodes, nb);
+        if (e == cudaSuccess) e = cudaMalloc(&l->d_spheres, sb);
+        if (e == cudaSuccess) e = cudaMemcpy(l->d_nodes, img.nodes, nb, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(l->d_spheres, img.spheres, sb, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
+        l->dev.nodes = l->d_nodes;
+        l->dev.spheres = l->d_spheres;
+    }
+    lights_image_free(&img);
+    if (e != cudaSuccess) {
+        cudaFree(l->d_nodes);
+        cudaFree(l->d_spheres);
+        delete l;
+        return e == cudaErrorMemoryAllocation ? VOX_CUDA_ENOMEM : VOX_CUDA_ECUDA;
+    }
+    *out = l;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_lights_free(vox_cuda_lights *l)
+{
+    if (!l) return VOX_CUDA_EINVAL;
+    cudaFree(l->d_nodes);
+    cudaFree(l->d_spheres);
+    delete l;
+    return VOX_CUDA_OK;
 }
