@@ -258,6 +258,43 @@ def measure_incoherent(torch, vg, dt, flush):
                       "r U[0.5,8] seed 4"}
 
 
+def measure_editing(vg, vox, edits=1000, seed=16):
+    """Live editing of the 256^3 tree: `edits` single-voxel insertions and
+    deletions through the library's vox_insert_voxel / vox_delete_voxel on
+    a separate host copy of the tree, then vox_cuda_tree_refresh of its
+    device copy (re-flatten and copy in place); a fresh upload for
+    comparison."""
+    import ctypes as C
+    L = vg.lib()
+    pts = np.ascontiguousarray(vox, dtype=np.float32).copy()
+    root = C.c_void_p(L.vox_make_tree(pts.ctypes.data_as(C.c_void_p), pts.shape[0]))
+    dt = vg.DeviceTree(root.value)
+    rng = np.random.default_rng(seed)
+    ops = []
+    for i in range(edits):
+        if i % 2 == 0:
+            ops.append((L.vox_insert_voxel, rng.integers(0, 256, 3).astype(np.float32)))
+        else:
+            ops.append((L.vox_delete_voxel, vox[int(rng.integers(len(vox)))].astype(np.float32).copy()))
+    t0 = time.perf_counter()
+    changed = sum(fn(C.byref(root), a.ctypes.data_as(C.c_void_p)) for fn, a in ops)
+    t_edit = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    vg.check(L.vox_cuda_tree_refresh(dt.h, root), "vox_cuda_tree_refresh")
+    t_refresh = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fresh = vg.DeviceTree(root.value)
+    t_upload = time.perf_counter() - t0
+    fresh.close()
+    dt.close()
+    L.vox_destroy_tree(root)
+    return {"edits": edits, "changed": int(changed), "edit_ms": t_edit * 1e3,
+            "edit_us_each": t_edit / edits * 1e6, "refresh_ms": t_refresh * 1e3,
+            "fresh_upload_ms": t_upload * 1e3,
+            "what": "alternating insertions (random voxels of the 256^3 box) and deletions (voxels of the "
+                    "volume) on the host tree, then vox_cuda_tree_refresh of its device copy"}
+
+
 def build_batch_trees(vg):
     from voxvision_gb300 import workloads as wl
     trees = []
@@ -573,6 +610,7 @@ def run_ours(args):
         btrees = build_batch_trees(vg)
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
         line["served"] = measure_served(vg, btrees, tex)
+        line["editing"] = measure_editing(vg, vox)
     if not args.no_cpu_baseline and world >= 1:
         line["cpu_baseline"] = cpu_baseline_sample(ht.ptr, states, tex)
     print(json.dumps(line), flush=True)

@@ -62,10 +62,24 @@ struct vox_node *vox_make_dense_leaf(const struct vox_box *box);
 /* tree.h:149 */
 void vox_set_voxel_size(float x, float y, float z);
 
+/* tree.h:88-122 -- editing.  The voxel is first snapped to the voxel grid
+ * in place; insertion returns 1 if the voxel was added (0: already there),
+ * deletion 1 if it was removed (0: not there).  *tree may change (a new root,
+ * or NULL when the last voxel goes).  Cached device copies of the edited
+ * tree (the single-query calls below) are dropped; a vox_cuda_tree of it
+ * must be refreshed with vox_cuda_tree_refresh. */
+int vox_insert_voxel(struct vox_node **tree, vox_dot voxel);
+int vox_insert_voxel_coord(struct vox_node **tree, float x, float y, float z);
+int vox_delete_voxel(struct vox_node **tree, vox_dot voxel);
+int vox_delete_voxel_coord(struct vox_node **tree, float x, float y, float z);
+/* tree.h:86 -- a new tree built by vox_make_tree from the voxels of `tree`. */
+struct vox_node *vox_rebuild_tree(const struct vox_node *tree);
+
 /* search.h:24-26 -- one ray, run on the GPU.  The tree (or the tree that
  * contains `tree`, which may be any of its nodes) is uploaded on first use and
- * kept until vox_cuda_forget_tree; after editing a tree, call that before the
- * next search.  Returns the leaf the reference returns, or NULL; `res` is
+ * kept until it is edited through this library or vox_cuda_forget_tree is
+ * called; after editing a tree with other code, call that before the next
+ * search.  Returns the leaf the reference returns, or NULL; `res` is
  * written on a hit only. */
 const struct vox_node *vox_ray_tree_intersection(const struct vox_node *tree, const vox_dot origin,
                                                  const vox_dot dir, vox_dot res);

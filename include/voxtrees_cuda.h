@@ -88,6 +88,13 @@ const char *vox_cuda_strerror(int code);
  * reference (the reference searches host memory directly). */
 int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out);
 int vox_cuda_tree_free(vox_cuda_tree *tree);
+/* Reload a device tree from `root` after the host tree was edited
+ * (vox_insert_voxel, vox_delete_voxel; no counterpart in the reference,
+ * whose trees live on the host).  Waits for all work on the device first
+ * (kernels in flight may read the old image), then flattens `root` again
+ * and copies it into the handle's device memory, growing it if needed.
+ * Pre-order leaf ids are those of the edited tree afterwards. */
+int vox_cuda_tree_refresh(vox_cuda_tree *tree, const struct vox_node *root);
 /* Flatten and check `root` on the host only (no device needed) and report
  * what vox_cuda_tree_upload would allocate: the basis of memory budgets.
  * VOX_CUDA_EDEPTH / ETOOBIG as the upload would return them. */

@@ -4,10 +4,11 @@ Run in a container that has the reference sources (default /root/reference):
 
     make -C oracle ref            # compiles the reference's own voxtrees and
                                   # camera sources into oracle/_ref/
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # everything
+    python tests/golden/make_golden.py edits    # the tree-editing fixtures only
 
 Every expected value here comes from the reference's compiled code:
-vox_make_tree, vox_insert_voxel, vox_ray_tree_intersection,
+vox_make_tree, vox_insert_voxel, vox_delete_voxel, vox_ray_tree_intersection,
 vox_tree_ball_collidep (src/voxtrees/tree.c, search.c, geom.c) and the
 simple-camera / doom-camera plugins (src/voxrnd/*-camera.c, vect-ops.c).
 The oracle library is used only to serialise the reference-built trees
@@ -38,6 +39,7 @@ ref.vox_destroy_tree.argtypes = [vp]
 ref.vox_ray_tree_intersection.argtypes = [vp, vp, vp, vp]; ref.vox_ray_tree_intersection.restype = vp
 ref.vox_tree_ball_collidep.argtypes = [vp, vp, C.c_float]; ref.vox_tree_ball_collidep.restype = C.c_int
 ref.vox_insert_voxel.argtypes = [C.POINTER(vp), vp]; ref.vox_insert_voxel.restype = C.c_int
+ref.vox_delete_voxel.argtypes = [C.POINTER(vp), vp]; ref.vox_delete_voxel.restype = C.c_int
 ref.vox_set_voxel_size.argtypes = [C.c_float] * 3
 
 
@@ -318,6 +320,103 @@ def render_case():
     ref.vox_destroy_tree(tree)
 
 
+def edit_ops(rng, n, lo, hi, voxel, start, p_insert=0.55, p_fraction=0.15):
+    """A seeded sequence of (kind, x, y, z): kind 0 insert, 1 delete; deletions
+    mostly of voxels present (tracked on the grid), some of random places;
+    some coordinates off the grid (the call snaps them)."""
+    v = np.asarray(voxel, np.float64)
+    present = {tuple(p) for p in np.round(np.asarray(start, np.float64) / v).astype(np.int64)}
+    ops = []
+    for _ in range(n):
+        if rng.random() < p_insert or not present:
+            g = rng.integers(lo, hi, 3)
+            off = rng.random(3) * 0.9 if rng.random() < p_fraction else np.zeros(3)
+            ops.append((0, *((g + off) * v)))
+            present.add(tuple(g))
+        else:
+            if rng.random() < 0.75:
+                keys = list(present)
+                g = np.asarray(keys[int(rng.integers(len(keys)))])
+                present.discard(tuple(g))
+            else:
+                g = rng.integers(lo, hi, 3)
+                present.discard(tuple(g))
+            ops.append((1, *(g * v)))
+    return np.asarray(ops, np.float64)
+
+
+def edit_case(name, voxel, start, ops, every=50):
+    """Replays `ops` on the reference's tree built from `start` with its
+    vox_insert_voxel / vox_delete_voxel; stores the return values and the
+    tree's dump every `every` operations and at the end."""
+    set_voxel(voxel)
+    t = vp(ref_tree_from_voxels(start) if len(start) else None)
+    rets = np.zeros(len(ops), np.int32)
+    out = dict(voxel=np.asarray(voxel, np.float32), start=np.asarray(start, np.float32).reshape(-1, 3),
+               ops=ops.astype(np.float32))
+    snaps = []
+    for i, (k, x, y, z) in enumerate(ops):
+        a = np.asarray([x, y, z], np.float32)
+        rets[i] = (ref.vox_insert_voxel if k == 0 else ref.vox_delete_voxel)(C.byref(t), P(a))
+        if (i + 1) % every == 0 or i + 1 == len(ops):
+            d = orc.dump_tree(t.value) if t.value else None
+            snaps.append(i)
+            pre = f"s{len(snaps) - 1}_"
+            if d is None:
+                out[pre + "empty"] = np.ones(1, np.uint8)
+            else:
+                for key in ("flags", "dots_num", "boxes", "centers", "child_mask", "dots"):
+                    out[pre + key] = d[key]
+    out["returns"] = rets
+    out["snap_after"] = np.asarray(snaps, np.int32)
+    path = os.path.join(OUT, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: ops={len(ops)} inserted={int(rets[ops[:, 0] == 0].sum())} "
+          f"deleted={int(rets[ops[:, 0] == 1].sum())} size={os.path.getsize(path)}")
+    if t.value:
+        ref.vox_destroy_tree(t.value)
+    set_voxel((1.0, 1.0, 1.0))
+
+
+def edit_cases():
+    """Tree editing (tree.c:425-866) by the reference's own code."""
+    # A: a blob volume, random insertions and deletions around it
+    rng = np.random.default_rng(80)
+    vol = wl.blobs_volume(20, 6, 80, 0.30)
+    start = wl.voxels_from_mask(vol)
+    edit_case("edit_blobs", (1, 1, 1), start, edit_ops(rng, 700, -3, 23, (1, 1, 1), start))
+    # B: dense leaves: a cube and a stripe, edited around their voxels
+    rng = np.random.default_rng(81)
+    cube = np.mgrid[0:6, 0:6, 0:6].reshape(3, -1).T
+    stripe = np.stack([np.arange(10, 19), np.full(9, 2), np.full(9, 3)], 1)
+    start = np.concatenate([cube, stripe]).astype(np.float32)
+    ops = []
+    present = [tuple(p) for p in start.astype(np.int64)]
+    for _ in range(500):
+        if rng.random() < 0.6 and present:
+            ops.append((1, *present.pop(int(rng.integers(len(present))))))
+        else:
+            g = tuple(int(x) for x in rng.integers(-1, 20, 3)) if rng.random() < 0.3 else \
+                tuple(int(x) for x in rng.integers(0, 7, 3))
+            ops.append((0, *g))
+            present.append(g)
+    edit_case("edit_dense", (1, 1, 1), start, np.asarray(ops, np.float64), every=25)
+    # C: from an empty tree: insert 300 voxels, then delete them all
+    rng = np.random.default_rng(82)
+    pts = np.unique(rng.integers(0, 12, (300, 3)), axis=0)
+    rng.shuffle(pts)
+    order = rng.permutation(len(pts))
+    ops = [(0, *p) for p in pts] + [(1, *pts[i]) for i in order]
+    edit_case("edit_empty", (1, 1, 1), np.zeros((0, 3), np.float32), np.asarray(ops, np.float64))
+    # D: non-unit voxels
+    rng = np.random.default_rng(83)
+    v = (0.5, 1.0, 2.0)
+    g = np.mgrid[0:10, 0:10, 0:10].reshape(3, -1).T
+    sel = g[((g - 5) ** 2).sum(1) < 20]
+    start = (sel * np.asarray(v)).astype(np.float32)
+    edit_case("edit_voxsize", v, start, edit_ops(rng, 500, -2, 12, v, start))
+
+
 def main():
     # 1. ball of radius 12 (the reference's own tree fixture, tests.c:214-237, scaled down)
     set_voxel((1.0, 1.0, 1.0))
@@ -383,4 +482,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["edits"]:
+        edit_cases()
+    else:
+        main()
+        edit_cases()

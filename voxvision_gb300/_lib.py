@@ -97,6 +97,7 @@ SIGNATURES = {
     "vox_cuda_launch_count": (C.c_uint64, []),
     "vox_cuda_tree_upload": (C.c_int, [_vp, C.POINTER(_vp)]),
     "vox_cuda_tree_free": (C.c_int, [_vp]),
+    "vox_cuda_tree_refresh": (C.c_int, [_vp, _vp]),
     "vox_cuda_tree_measure": (C.c_int, [_vp, C.POINTER(TreeInfo)]),
     "vox_cuda_tree_get_info": (C.c_int, [_vp, C.POINTER(TreeInfo)]),
     "vox_cuda_tree_node": (_vp, [_vp, _u32]),
@@ -143,6 +144,11 @@ SIGNATURES = {
     "vox_cuda_ball_counts_device": (C.c_int, [_vp, _vp, _vp, _sz, _vp, _vp]),
     # voxtrees.h
     "vox_make_tree": (_vp, [_vp, _sz]),
+    "vox_insert_voxel": (C.c_int, [C.POINTER(_vp), _vp]),
+    "vox_insert_voxel_coord": (C.c_int, [C.POINTER(_vp), _f, _f, _f]),
+    "vox_delete_voxel": (C.c_int, [C.POINTER(_vp), _vp]),
+    "vox_delete_voxel_coord": (C.c_int, [C.POINTER(_vp), _f, _f, _f]),
+    "vox_rebuild_tree": (_vp, [_vp]),
     "vox_destroy_tree": (None, [_vp]),
     "vox_voxels_in_tree": (_sz, [_vp]),
     "vox_bounding_box": (None, [_vp, _vp]),

@@ -6,8 +6,10 @@
  * The reference accepts any node as the search root (renderer.c:297 passes a
  * leaf).  A registry of uploaded trees maps a node pointer to (device tree,
  * pre-order id); a pointer found in no registered tree is taken as the root
- * of a new tree and uploaded.  Edited trees must be dropped with
- * vox_cuda_forget_tree before the next search.  These single-query calls
+ * of a new tree and uploaded.  The library's vox_insert_voxel and
+ * vox_delete_voxel drop the copies of the trees they edit; trees edited by
+ * other code must be dropped with vox_cuda_forget_tree before the next
+ * search.  These single-query calls
  * cost a round trip each; batches belong in vox_cuda_ray_batch.
  */
 #include <cstring>
@@ -92,6 +94,23 @@ EXPORT void vox_cuda_forget_tree(const struct vox_node *root)
             vox_cuda_tree_free(g_trees[i].tree);
             g_trees.erase(g_trees.begin() + (long)i);
             return;
+        }
+    }
+}
+
+// Called by the tree-editing functions before they change a tree: a cached
+// device copy of any tree that contains `node` is dropped.
+extern "C" void vox_dropin_forget_containing(const struct vox_node *node)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (size_t i = 0; i < g_trees.size();) {
+        uint32_t id;
+        if (vox_cuda_tree_node_id(g_trees[i].tree, node, &id) == VOX_CUDA_OK) {
+            vox_cuda_tree_free(g_trees[i].tree);
+            g_trees[i] = g_trees.back();
+            g_trees.pop_back();
+        } else {
+            i++;
         }
     }
 }

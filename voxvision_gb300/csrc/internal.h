@@ -17,15 +17,16 @@
 using vox::DevTree;
 
 struct vox_cuda_tree {
-    int device;
-    float bbox[6];           // root bounding box (for scheduling only)
-    uint4 *d_pool;
-    uint32_t *d_rec_of_id;
-    uint32_t *d_status;      // bit 0: a traversal stack overflowed
-    DevTree dev;
-    int cap_class;           // 0: 28 stack entries, 1: 64, 2: 256
-    FlatTree flat;           // host copy: pre-order table and maps
-    size_t pool_bytes;
+    int device = 0;
+    float bbox[6] = {0, 0, 0, 0, 0, 0};   // root bounding box (for scheduling only)
+    uint4 *d_pool = nullptr;
+    uint32_t *d_rec_of_id = nullptr;
+    uint32_t *d_status = nullptr;          // bit 0: a traversal stack overflowed
+    DevTree dev{};
+    int cap_class = 0;                     // 0: 28 stack entries, 1: 64, 2: 256
+    FlatTree flat;                         // host copy: pre-order table and maps
+    size_t pool_bytes = 0;                 // device pool allocation
+    size_t map_bytes = 0;                  // device pre-order map allocation
 };
 
 

@@ -628,45 +628,57 @@ EXPORT const char *vox_cuda_version(void) { return "voxtrees_cuda 0.1 (sm_103a)"
 
 EXPORT uint64_t vox_cuda_launch_count(void) { return g_launches.load(); }
 
-EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out)
+// Flattens `root` into t (host maps) and copies the image to the device,
+// reusing t's device buffers when they are large enough.  On failure t keeps
+// its previous contents when `keep` is set (a refresh), else is left empty.
+static int load_tree(vox_cuda_tree *t, const struct vox_node *root)
 {
-    if (!out) return VOX_CUDA_EINVAL;
-    *out = nullptr;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return VOX_CUDA_ENODEV;
-    vox_cuda_tree *t = new (std::nothrow) vox_cuda_tree();
-    if (!t) return VOX_CUDA_ENOMEM;
-    t->device = dev;
-    int rc = vox_flatten(root, vox_voxel, &t->flat);
-    if (rc == -2 || rc == -1) { delete t; return VOX_CUDA_ETOOBIG; }
-    if (vox_flatten_validate(t->flat) != 0) { delete t; return VOX_CUDA_EINVAL; }
-    int cls = cap_class_for_depth(t->flat.depth);
-    if (cls < 0) { delete t; return VOX_CUDA_EDEPTH; }
-    t->cap_class = cls;
-    size_t units = t->flat.units.size() ? t->flat.units.size() : VOXP_REC_UNITS;
-    size_t nodes = t->flat.preorder.size();
-    t->pool_bytes = units * 16;
-    if (cudaMalloc(&t->d_pool, t->pool_bytes) != cudaSuccess) { delete t; return VOX_CUDA_ENOMEM; }
-    if (cudaMalloc(&t->d_rec_of_id, (nodes ? nodes : 1) * 4) != cudaSuccess ||
-        cudaMalloc(&t->d_status, 4) != cudaSuccess) {
-        cudaFree(t->d_pool); cudaFree(t->d_rec_of_id);
-        delete t;
+    FlatTree flat;
+    int rc = vox_flatten(root, vox_voxel, &flat);
+    if (rc == -2 || rc == -1) return VOX_CUDA_ETOOBIG;
+    if (vox_flatten_validate(flat) != 0) return VOX_CUDA_EINVAL;
+    int cls = cap_class_for_depth(flat.depth);
+    if (cls < 0) return VOX_CUDA_EDEPTH;
+    size_t units = flat.units.size() ? flat.units.size() : VOXP_REC_UNITS;
+    size_t nodes = flat.preorder.size();
+    size_t pool_bytes = units * 16, map_bytes = (nodes ? nodes : 1) * 4;
+    uint4 *pool = t->d_pool;
+    uint32_t *map = t->d_rec_of_id;
+    bool new_pool = !pool || t->pool_bytes < pool_bytes, new_map = !map || t->map_bytes < map_bytes;
+    if (new_pool && cudaMalloc(&pool, pool_bytes) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    if (new_map && cudaMalloc(&map, map_bytes) != cudaSuccess) {
+        if (new_pool) cudaFree(pool);
+        return VOX_CUDA_ENOMEM;
+    }
+    if (!t->d_status && cudaMalloc(&t->d_status, 4) != cudaSuccess) {
+        if (new_pool) cudaFree(pool);
+        if (new_map) cudaFree(map);
         return VOX_CUDA_ENOMEM;
     }
     cudaError_t e = cudaMemset(t->d_status, 0, 4);
-    if (e == cudaSuccess && t->flat.units.size())
-        e = cudaMemcpy(t->d_pool, t->flat.units.data(), t->pool_bytes, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && nodes)
-        e = cudaMemcpy(t->d_rec_of_id, t->flat.rec_of_id.data(), nodes * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && flat.units.size())
+        e = cudaMemcpy(pool, flat.units.data(), flat.units.size() * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nodes) e = cudaMemcpy(map, flat.rec_of_id.data(), nodes * 4, cudaMemcpyHostToDevice);
     // A copy from pageable memory may still be in flight when cudaMemcpy
     // returns; the pool must be complete before any kernel on any stream
     // reads it (the frame kernel reads it ahead of its stream dependency).
     if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
     if (e != cudaSuccess) {
-        cudaFree(t->d_pool); cudaFree(t->d_rec_of_id); cudaFree(t->d_status);
-        delete t;
+        if (new_pool) cudaFree(pool);
+        if (new_map) cudaFree(map);
         return VOX_CUDA_ECUDA;
     }
+    if (new_pool) {
+        if (t->d_pool) cudaFree(t->d_pool);
+        t->d_pool = pool;
+        t->pool_bytes = pool_bytes;
+    }
+    if (new_map) {
+        if (t->d_rec_of_id) cudaFree(t->d_rec_of_id);
+        t->d_rec_of_id = map;
+        t->map_bytes = map_bytes;
+    }
+    t->cap_class = cls;
     if (root) {
         for (int i = 0; i < 3; i++) {
             t->bbox[i] = root->bounding_box.min[i];
@@ -679,15 +691,44 @@ EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out
     t->dev.rec_of_id = t->d_rec_of_id;
     t->dev.root = root ? 0u : VOXP_EMPTY;
     t->dev.n_nodes = (uint32_t)nodes;
-    t->dev.vx = t->flat.voxel[0];
-    t->dev.vy = t->flat.voxel[1];
-    t->dev.vz = t->flat.voxel[2];
-    uint64_t steps = (uint64_t)nodes + t->flat.n_dots + 2;
+    t->dev.vx = flat.voxel[0];
+    t->dev.vy = flat.voxel[1];
+    t->dev.vz = flat.voxel[2];
+    uint64_t steps = (uint64_t)nodes + flat.n_dots + 2;
     t->dev.max_steps = steps > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)steps;
     // The flattened image is on the device now; keep only the maps.
-    std::vector<uint4_host>().swap(t->flat.units);
+    std::vector<uint4_host>().swap(flat.units);
+    t->flat = std::move(flat);
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out)
+{
+    if (!out) return VOX_CUDA_EINVAL;
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return VOX_CUDA_ENODEV;
+    vox_cuda_tree *t = new (std::nothrow) vox_cuda_tree();
+    if (!t) return VOX_CUDA_ENOMEM;
+    t->device = dev;
+    int rc = load_tree(t, root);
+    if (rc) {
+        cudaFree(t->d_pool);
+        cudaFree(t->d_rec_of_id);
+        cudaFree(t->d_status);
+        delete t;
+        return rc;
+    }
     *out = t;
     return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_tree_refresh(vox_cuda_tree *t, const struct vox_node *root)
+{
+    if (!t) return VOX_CUDA_EINVAL;
+    // kernels in flight on any stream may still read the old image
+    if (cudaDeviceSynchronize() != cudaSuccess) return VOX_CUDA_ECUDA;
+    return load_tree(t, root);
 }
 
 EXPORT int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info *info)
