@@ -3,7 +3,6 @@
 #define VOX_FLATTEN_H
 
 #include <cstdint>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/voxtrees.h"
@@ -16,7 +15,6 @@ struct FlatTree {
     std::vector<uint4_host> units;                     // the pool image
     std::vector<const vox_node *> preorder;            // pre-order id -> host node
     std::vector<uint32_t> rec_of_id;                   // pre-order id -> record offset
-    std::unordered_map<const vox_node *, uint32_t> index;  // host node -> pre-order id
     uint64_t n_inner, n_leaf, n_dense, n_dots, depth;
     float voxel[3];
 };

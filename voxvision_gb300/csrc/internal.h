@@ -8,6 +8,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "flatten.h"
 #include "pool_layout.h"
@@ -27,6 +30,10 @@ struct vox_cuda_tree {
     FlatTree flat;                         // host copy: pre-order table and maps
     size_t pool_bytes = 0;                 // device pool allocation
     size_t map_bytes = 0;                  // device pre-order map allocation
+    // host node -> pre-order id, sorted by node; built on the first lookup
+    std::mutex index_mu;
+    bool index_built = false;
+    std::vector<std::pair<const vox_node *, uint32_t>> index;
 };
 
 

@@ -699,6 +699,9 @@ static int load_tree(vox_cuda_tree *t, const struct vox_node *root)
     // The flattened image is on the device now; keep only the maps.
     std::vector<uint4_host>().swap(flat.units);
     t->flat = std::move(flat);
+    std::lock_guard<std::mutex> lock(t->index_mu);
+    t->index.clear();
+    t->index_built = false;
     return VOX_CUDA_OK;
 }
 
@@ -785,8 +788,16 @@ EXPORT const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *t, uint32_
 EXPORT int vox_cuda_tree_node_id(const vox_cuda_tree *t, const struct vox_node *node, uint32_t *id)
 {
     if (!t || !id) return VOX_CUDA_EINVAL;
-    auto it = t->flat.index.find(node);
-    if (it == t->flat.index.end()) return VOX_CUDA_EINVAL;
+    vox_cuda_tree *m = const_cast<vox_cuda_tree *>(t);
+    std::lock_guard<std::mutex> lock(m->index_mu);
+    if (!m->index_built) {
+        m->index.resize(t->flat.preorder.size());
+        for (size_t i = 0; i < m->index.size(); i++) m->index[i] = {t->flat.preorder[i], (uint32_t)i};
+        std::sort(m->index.begin(), m->index.end());
+        m->index_built = true;
+    }
+    auto it = std::lower_bound(m->index.begin(), m->index.end(), std::make_pair(node, (uint32_t)0));
+    if (it == m->index.end() || it->first != node) return VOX_CUDA_EINVAL;
     *id = it->second;
     return VOX_CUDA_OK;
 }
