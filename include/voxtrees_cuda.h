@@ -100,6 +100,54 @@ int vox_cuda_tree_refresh(vox_cuda_tree *tree, const struct vox_node *root);
  * VOX_CUDA_EDEPTH / ETOOBIG as the upload would return them. */
 int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info *info);
 int vox_cuda_tree_get_info(const vox_cuda_tree *tree, vox_cuda_tree_info *info);
+
+/* ---- trees built on the device (tree.c:249-338, datareader.c:11-85) ----
+ *
+ * The tree vox_make_tree(set, n) would build, node for node and voxel for
+ * voxel, built on the GPU straight into a device tree: the image equals
+ * vox_make_tree followed by vox_cuda_tree_upload byte for byte, pre-order
+ * leaf ids included.  No host tree exists, so vox_cuda_tree_node returns NULL
+ * and vox_cuda_tree_node_id fails for these handles; everything else (rays,
+ * balls, frames, batches, servers, refresh from a host tree) works as for an
+ * uploaded tree.  The voxel size is read from vox_voxel, as by vox_make_tree.
+ * Synchronous; n = 0 gives the empty tree.  Sets of 2^31 voxels or more:
+ * VOX_CUDA_ETOOBIG. */
+/* `set`: n voxels (a vox_dot array, 3n floats) in host memory, left
+ * unmodified (vox_make_tree reorders its set). */
+int vox_cuda_tree_build(const float *set, size_t n, vox_cuda_tree **out);
+/* `d_set`: n voxels (3n floats) in device memory of the current device. */
+int vox_cuda_tree_build_device(const float *d_set, size_t n, vox_cuda_tree **out);
+
+/* Which samples are solid.  With mask == NULL: lo <= sample <= hi (the
+ * demo's "sample > threshold" is lo = threshold + 1, hi = 0xFFFFFFFF; the
+ * engine's ranged reader [min, max) is lo = min, hi = max - 1).  Otherwise
+ * bit (sample & 7) of mask[sample >> 3] for samplesize 1 or 2: any predicate
+ * of the reference's test block (datareader.h:34), tabulated. */
+typedef struct {
+    uint32_t lo, hi;
+    const uint8_t *mask;
+} vox_cuda_raw_test;
+
+/* datareader.c:11-85 with the test on the GPU: `samples` (host memory) holds
+ * dim[0] x dim[1] x dim[2] samples of `samplesize` (1..4) little-endian
+ * bytes, the last index fastest; the voxel of sample (i, j, k) has its
+ * minimum corner at (i, j, k) * vox_voxel, and the set is in that order.
+ * Returns the tree of the solid voxels (empty if none, where the reference
+ * returns NULL).  Volumes of 2^32 samples or more: VOX_CUDA_ETOOBIG. */
+int vox_cuda_tree_build_raw(const void *samples, const unsigned dim[3], unsigned samplesize,
+                            const vox_cuda_raw_test *test, vox_cuda_tree **out);
+/* vox_read_raw_data (datareader.h:34-37): the file must hold exactly
+ * dim[0]*dim[1]*dim[2]*samplesize bytes ("Wrong size of dataset" otherwise);
+ * on failure *error (if error is not NULL) is set to a static string. */
+int vox_cuda_read_raw_data(const char *filename, const unsigned dim[3], unsigned samplesize,
+                           const vox_cuda_raw_test *test, vox_cuda_tree **out, const char **error);
+
+/* The device image of a tree copied to host memory: *n_units 16-byte units
+ * (pool_layout.h) and *n_ids pre-order id -> record offset entries.  With
+ * NULL buffers only the sizes are reported; buffers smaller than the sizes:
+ * VOX_CUDA_EINVAL.  For tests, tools and serialisation. */
+int vox_cuda_tree_image(const vox_cuda_tree *tree, void *units, size_t units_cap, uint32_t *rec_of_id,
+                        size_t ids_cap, size_t *n_units, size_t *n_ids);
 /* Pre-order index -> host node (NULL when out of range). */
 const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *tree, uint32_t id);
 /* Host node -> pre-order index; VOX_CUDA_EINVAL when the node is not in the tree. */

@@ -43,3 +43,49 @@ def dumps_equal(d1, d2):
                               np.asarray(d2[k], np.float32).view(np.uint32)):
             return False, k
     return True, None
+
+
+def image_dump(units, rec_of_id, voxel):
+    """The device image of a tree (pool_layout.h) decoded into the pre-order
+    dump format of the oracle (flags with the overflow bit for leaves of more
+    than VOX_MAX_DOTS voxels, dots_num, boxes, centers, child_mask, dot_offset,
+    dots): device-built trees compare directly with the reference's dumps."""
+    n = len(rec_of_id)
+    recs = rec_of_id.astype(np.int64)
+    r0, r1, r2 = units[recs], units[recs + 1], units[recs + 2]
+    boxes = np.concatenate([r0, r1[:, :2]], axis=1).astype(np.uint32).view(np.float32)
+    meta, link = r1[:, 2], r1[:, 3]
+    kind = meta & 3
+    flags = np.zeros(n, np.uint32)
+    dots_num = np.zeros(n, np.uint64)
+    centers = np.zeros((n, 3), np.float32)
+    mask = np.zeros(n, np.uint8)
+    doff = np.zeros(n, np.uint64)
+    dots = []
+    nd = 0
+    id_of_rec = {int(r): i for i, r in enumerate(recs)}
+    children = {}
+    v = np.asarray(voxel, np.float64)
+    for i in range(n):
+        doff[i] = nd
+        if kind[i] == 2:
+            flags[i] = 2
+            ext = (boxes[i, 3:].astype(np.float64) - boxes[i, :3]) / v
+            dots_num[i] = int(np.prod(np.rint(ext)))
+        elif kind[i] == 1:
+            cnt = int(meta[i] >> 2)
+            flags[i] = 1 | (4 if cnt > 7 else 0)
+            dots_num[i] = cnt
+            dots.append(units[link[i]:link[i] + cnt, :3])
+            nd += cnt
+        else:
+            m = int((meta[i] >> 8) & 0xFF)
+            mask[i] = m
+            centers[i] = r2[i, :3].astype(np.uint32).view(np.float32)
+            children[i] = [id_of_rec[int(link[i]) + 3 * j] for j in range(bin(m).count("1"))]
+    for i in range(n - 1, -1, -1):
+        if i in children:
+            dots_num[i] = sum(int(dots_num[c]) for c in children[i])
+    d = np.concatenate(dots).astype(np.uint32).view(np.float32) if dots else np.zeros((0, 3), np.float32)
+    return dict(flags=flags, dots_num=dots_num.astype(np.uint32), boxes=boxes, centers=centers,
+                child_mask=mask, dot_offset=doff, dots=d)

@@ -14,8 +14,8 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (CAMERA_DOOM, CAMERA_SIMPLE, VOX_CUDA_MISS, VOX_CUDA_SLOT_DENSE, BatchConfig, CameraStruct,
-                   FrameJob, RenderConfig, ReplayRequest, ReplayResult, ServerConfig, ServerStats, TreeInfo,
-                   VoxCudaError, available, check, lib)
+                   FrameJob, RawTest, RenderConfig, ReplayRequest, ReplayResult, ServerConfig, ServerStats,
+                   TreeInfo, VoxCudaError, available, check, lib)
 
 __all__ = ["HostTree", "DeviceTree", "FrameBatch", "BatchConfig", "Server", "ServerConfig", "Camera", "camera_struct", "VoxCudaError", "available", "lib",
            "VOX_CUDA_MISS", "VOX_CUDA_SLOT_DENSE", "CAMERA_SIMPLE", "CAMERA_DOOM", "set_voxel_size",
@@ -75,13 +75,95 @@ def measure_tree(host_ptr) -> dict:
     return {k: int(getattr(i, k)) for k, _ in TreeInfo._fields_}
 
 
-class DeviceTree:
-    """A tree uploaded with vox_cuda_tree_upload."""
+def _raw_test(samplesize: int, lo: int | None, hi: int | None, test=None):
+    """A vox_cuda_raw_test: the range [lo, hi] of solid samples, or a
+    predicate tabulated over every sample value (samplesize 1 or 2)."""
+    if test is not None:
+        if samplesize > 2:
+            raise ValueError("a predicate is tabulated only for 1- and 2-byte samples")
+        vals = np.arange(1 << (8 * samplesize), dtype=np.uint64)
+        bits = np.fromiter((1 if test(int(v)) else 0 for v in vals), np.uint8, vals.size)
+        mask = np.packbits(bits, bitorder="little")
+        return RawTest(0, 0, mask.ctypes.data), mask
+    lo = 0 if lo is None else int(lo)
+    hi = (1 << (8 * samplesize)) - 1 if hi is None else int(hi)
+    return RawTest(lo, hi, None), None
 
-    def __init__(self, host_ptr):
+
+class DeviceTree:
+    """A device tree: uploaded from a host tree (vox_cuda_tree_upload), or built
+    on the GPU from voxels or a raw volume (DeviceTree.build*, from_raw)."""
+
+    def __init__(self, host_ptr=None, *, handle=None):
+        if handle is not None:
+            self.h = handle
+            return
         h = C.c_void_p()
         check(lib().vox_cuda_tree_upload(host_ptr, C.byref(h)), "vox_cuda_tree_upload")
         self.h = h
+
+    @classmethod
+    def build(cls, voxels: np.ndarray) -> "DeviceTree":
+        """vox_cuda_tree_build: vox_make_tree's tree of `voxels` ((n, 3) float32,
+        host), built on the GPU."""
+        s = np.ascontiguousarray(voxels, dtype=np.float32)
+        if s.ndim != 2 or s.shape[1] != 3:
+            raise ValueError("voxels must be (n, 3)")
+        h = C.c_void_p()
+        check(lib().vox_cuda_tree_build(_p(s), s.shape[0], C.byref(h)), "vox_cuda_tree_build")
+        return cls(handle=h)
+
+    @classmethod
+    def build_device(cls, voxels, n: int | None = None) -> "DeviceTree":
+        """vox_cuda_tree_build_device: voxels already on the device (a torch
+        tensor of (n, 3) float32 or a device pointer with n)."""
+        if n is None:
+            n = int(voxels.shape[0])
+        h = C.c_void_p()
+        check(lib().vox_cuda_tree_build_device(_dptr(voxels), n, C.byref(h)), "vox_cuda_tree_build_device")
+        return cls(handle=h)
+
+    @classmethod
+    def from_raw(cls, samples, dim, samplesize: int = 1, lo: int | None = None, hi: int | None = None,
+                 test=None) -> "DeviceTree":
+        """vox_cuda_tree_build_raw: a dim[0] x dim[1] x dim[2] volume of
+        little-endian samples (bytes or a numpy array), solid where
+        lo <= sample <= hi or where test(sample) is true."""
+        buf = np.ascontiguousarray(np.frombuffer(samples, np.uint8) if isinstance(samples, (bytes, bytearray))
+                                   else np.asarray(samples)).view(np.uint8)
+        d = (C.c_uint * 3)(*[int(x) for x in dim])
+        rt, keep = _raw_test(samplesize, lo, hi, test)
+        h = C.c_void_p()
+        check(lib().vox_cuda_tree_build_raw(_p(buf), C.byref(d), samplesize, C.byref(rt), C.byref(h)),
+              "vox_cuda_tree_build_raw")
+        del keep
+        return cls(handle=h)
+
+    @classmethod
+    def read_raw(cls, path: str, dim, samplesize: int = 1, lo: int | None = None, hi: int | None = None,
+                 test=None) -> "DeviceTree":
+        """vox_cuda_read_raw_data (vox_read_raw_data with the test on the GPU)."""
+        d = (C.c_uint * 3)(*[int(x) for x in dim])
+        rt, keep = _raw_test(samplesize, lo, hi, test)
+        h = C.c_void_p()
+        err = C.c_char_p()
+        rc = lib().vox_cuda_read_raw_data(path.encode(), C.byref(d), samplesize, C.byref(rt), C.byref(h),
+                                         C.byref(err))
+        del keep
+        if rc:
+            raise VoxCudaError(rc, f"vox_cuda_read_raw_data: {err.value.decode() if err.value else rc}")
+        return cls(handle=h)
+
+    def image(self):
+        """The device image: (units as an (n, 4) uint32 array, pre-order id ->
+        record offset)."""
+        nu, ni = C.c_size_t(), C.c_size_t()
+        check(lib().vox_cuda_tree_image(self.h, None, 0, None, 0, C.byref(nu), C.byref(ni)), "vox_cuda_tree_image")
+        units = np.zeros((nu.value, 4), np.uint32)
+        ids = np.zeros(ni.value, np.uint32)
+        check(lib().vox_cuda_tree_image(self.h, _p(units), nu.value, _p(ids), ni.value, None, None),
+              "vox_cuda_tree_image")
+        return units, ids
 
     def info(self) -> dict:
         i = TreeInfo()

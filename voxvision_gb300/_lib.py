@@ -41,6 +41,11 @@ class TreeInfo(C.Structure):
                 ("nodes", "inner", "leaves", "dense_leaves", "dots", "depth", "device_bytes")]
 
 
+class RawTest(C.Structure):
+    """vox_cuda_raw_test (include/voxtrees_cuda.h)."""
+    _fields_ = [("lo", C.c_uint32), ("hi", C.c_uint32), ("mask", C.c_void_p)]
+
+
 class FrameJob(C.Structure):
     """vox_cuda_frame_job (include/voxtrees_cuda.h)."""
     _fields_ = [("tree", C.c_void_p), ("camera", CameraStruct), ("w", C.c_uint32), ("h", C.c_uint32),
@@ -98,6 +103,13 @@ SIGNATURES = {
     "vox_cuda_tree_upload": (C.c_int, [_vp, C.POINTER(_vp)]),
     "vox_cuda_tree_free": (C.c_int, [_vp]),
     "vox_cuda_tree_refresh": (C.c_int, [_vp, _vp]),
+    "vox_cuda_tree_build": (C.c_int, [_vp, _sz, C.POINTER(_vp)]),
+    "vox_cuda_tree_build_device": (C.c_int, [_vp, _sz, C.POINTER(_vp)]),
+    "vox_cuda_tree_build_raw": (C.c_int, [_vp, C.POINTER(C.c_uint * 3), C.c_uint, C.POINTER(RawTest),
+                                          C.POINTER(_vp)]),
+    "vox_cuda_read_raw_data": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint * 3), C.c_uint, C.POINTER(RawTest),
+                                         C.POINTER(_vp), C.POINTER(C.c_char_p)]),
+    "vox_cuda_tree_image": (C.c_int, [_vp, _vp, _sz, _vp, _sz, C.POINTER(_sz), C.POINTER(_sz)]),
     "vox_cuda_tree_measure": (C.c_int, [_vp, C.POINTER(TreeInfo)]),
     "vox_cuda_tree_get_info": (C.c_int, [_vp, C.POINTER(TreeInfo)]),
     "vox_cuda_tree_node": (_vp, [_vp, _u32]),

@@ -30,12 +30,29 @@ struct vox_cuda_tree {
     FlatTree flat;                         // host copy: pre-order table and maps
     size_t pool_bytes = 0;                 // device pool allocation
     size_t map_bytes = 0;                  // device pre-order map allocation
+    uint64_t n_nodes = 0, n_units = 0;     // nodes, image units (3 for the empty tree)
     // host node -> pre-order id, sorted by node; built on the first lookup
     std::mutex index_mu;
     bool index_built = false;
     std::vector<std::pair<const vox_node *, uint32_t>> index;
 };
 
+
+// What a device-built image holds (build.cu).
+struct ImageStats {
+    uint64_t nodes, units, inner, leaf, dense, dots, depth;
+    float bbox[6];
+    float voxel[3];
+};
+
+/* Makes t serve a device image built in place: `pool` (st.units 16-byte
+ * units) and `map` (st.nodes pre-order id -> record entries), both
+ * cudaMalloc'ed and owned by t from then on; t's previous buffers are freed.
+ * st.nodes == 0 (pool and map NULL) is the empty tree.  VOX_CUDA_EDEPTH when
+ * the tree is too deep for the traversal stack (the buffers stay the
+ * caller's). */
+int adopt_image(vox_cuda_tree *t, uint4 *pool, size_t pool_bytes, uint32_t *map, size_t map_bytes,
+                const ImageStats &st);
 
 // Ray stacks hold at most 3 pending children per inner level on the path.
 constexpr int CAP0 = 28, CAP1 = 64, CAP2 = 256;

@@ -696,9 +696,68 @@ static int load_tree(vox_cuda_tree *t, const struct vox_node *root)
     t->dev.vz = flat.voxel[2];
     uint64_t steps = (uint64_t)nodes + flat.n_dots + 2;
     t->dev.max_steps = steps > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)steps;
+    t->n_nodes = nodes;
+    t->n_units = flat.units.size();
     // The flattened image is on the device now; keep only the maps.
     std::vector<uint4_host>().swap(flat.units);
     t->flat = std::move(flat);
+    std::lock_guard<std::mutex> lock(t->index_mu);
+    t->index.clear();
+    t->index_built = false;
+    return VOX_CUDA_OK;
+}
+
+int adopt_image(vox_cuda_tree *t, uint4 *pool, size_t pool_bytes, uint32_t *map, size_t map_bytes,
+                const ImageStats &st)
+{
+    int cls = cap_class_for_depth(st.depth);
+    if (cls < 0) return VOX_CUDA_EDEPTH;
+    bool empty = st.nodes == 0;
+    uint4 *own_pool = nullptr;
+    uint32_t *own_map = nullptr;
+    if (empty) {   // as the upload of a NULL tree: one record's worth of pool, a one-entry map
+        pool_bytes = VOXP_REC_UNITS * 16;
+        map_bytes = 4;
+        if (cudaMalloc(&own_pool, pool_bytes) != cudaSuccess) return VOX_CUDA_ENOMEM;
+        if (cudaMalloc(&own_map, map_bytes) != cudaSuccess) {
+            cudaFree(own_pool);
+            return VOX_CUDA_ENOMEM;
+        }
+        pool = own_pool;
+        map = own_map;
+    }
+    if ((!t->d_status && cudaMalloc(&t->d_status, 4) != cudaSuccess) || cudaMemset(t->d_status, 0, 4) != cudaSuccess) {
+        cudaFree(own_pool);
+        cudaFree(own_map);
+        return VOX_CUDA_ENOMEM;
+    }
+    if (t->d_pool) cudaFree(t->d_pool);
+    if (t->d_rec_of_id) cudaFree(t->d_rec_of_id);
+    t->d_pool = pool;
+    t->pool_bytes = pool_bytes;
+    t->d_rec_of_id = map;
+    t->map_bytes = map_bytes;
+    t->cap_class = cls;
+    for (int i = 0; i < 6; i++) t->bbox[i] = empty ? 0.0f : st.bbox[i];
+    t->dev.pool = pool;
+    t->dev.rec_of_id = map;
+    t->dev.root = empty ? VOXP_EMPTY : 0u;
+    t->dev.n_nodes = (uint32_t)st.nodes;
+    t->dev.vx = st.voxel[0];
+    t->dev.vy = st.voxel[1];
+    t->dev.vz = st.voxel[2];
+    uint64_t steps = st.nodes + st.dots + 2;
+    t->dev.max_steps = steps > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)steps;
+    t->n_nodes = st.nodes;
+    t->n_units = empty ? 0 : st.units;
+    FlatTree f;
+    f.n_inner = st.inner;
+    f.n_leaf = st.leaf;
+    f.n_dense = st.dense;
+    f.n_dots = st.dots;
+    f.depth = st.depth;
+    for (int i = 0; i < 3; i++) f.voxel[i] = st.voxel[i];
+    t->flat = std::move(f);
     std::lock_guard<std::mutex> lock(t->index_mu);
     t->index.clear();
     t->index_built = false;
@@ -769,13 +828,30 @@ EXPORT int vox_cuda_tree_free(vox_cuda_tree *t)
 EXPORT int vox_cuda_tree_get_info(const vox_cuda_tree *t, vox_cuda_tree_info *info)
 {
     if (!t || !info) return VOX_CUDA_EINVAL;
-    info->nodes = t->flat.preorder.size();
+    info->nodes = t->n_nodes;
     info->inner = t->flat.n_inner;
     info->leaves = t->flat.n_leaf;
     info->dense_leaves = t->flat.n_dense;
     info->dots = t->flat.n_dots;
     info->depth = t->flat.depth;
-    info->device_bytes = t->pool_bytes + 4 * t->flat.preorder.size() + 4;
+    info->device_bytes = t->pool_bytes + 4 * t->n_nodes + 4;
+    return VOX_CUDA_OK;
+}
+
+EXPORT int vox_cuda_tree_image(const vox_cuda_tree *t, void *units, size_t units_cap, uint32_t *rec_of_id,
+                               size_t ids_cap, size_t *n_units, size_t *n_ids)
+{
+    if (!t) return VOX_CUDA_EINVAL;
+    if (n_units) *n_units = t->n_units;
+    if (n_ids) *n_ids = t->n_nodes;
+    if ((units && units_cap < t->n_units) || (rec_of_id && ids_cap < t->n_nodes)) return VOX_CUDA_EINVAL;
+    // kernels in flight on other streams may still write the status word only
+    if (units && t->n_units &&
+        cudaMemcpy(units, t->d_pool, t->n_units * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return VOX_CUDA_ECUDA;
+    if (rec_of_id && t->n_nodes &&
+        cudaMemcpy(rec_of_id, t->d_rec_of_id, t->n_nodes * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return VOX_CUDA_ECUDA;
     return VOX_CUDA_OK;
 }
 
