@@ -73,9 +73,11 @@ constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
 constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr uint32_t BIG = 4096;       // nodes with more voxels sum their coordinates by chunks
+constexpr uint32_t SMALL = 512;      // nodes with at most this many voxels are split by one warp
+constexpr uint32_t TINY = 32;        // nodes with at most this many voxels get their box from one thread
 constexpr uint32_t CHUNK = 1024;     // voxels per chunk
 constexpr int CHUNK_THREADS = 128;   // 8 consecutive voxels per thread
-constexpr int NBIN = 12;             // binades with a precomputed map per chunk
+constexpr int NBIN = 16;             // binades with a precomputed map per chunk
 constexpr uint32_t SAT = 1u << 25;   // map increments saturate here (any >= 2^24 is unusable)
 constexpr int MAX_LEVELS = 90;       // deeper trees exceed the traversal stack anyway
 constexpr uint64_t MAX_VOXELS = 0x7FFFFFFFull;
@@ -358,16 +360,58 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_chunk_box(const float *P, Lev
     }
 }
 
-// Bounding box of every node (calc_bounding_box, tree.c:138-155): a warp per
-// node over its voxels, or over its chunks' partial extremes for a big node.
-// Also the top binade a big node's coordinate sums can reach.
-__global__ void k_node_box(const float *P, Level L, const float *cv, const uint32_t *ci, float vx, float vy,
-                           float vz)
+// The box of node k and the top binade its coordinate sums can reach.
+__device__ void write_box(const Level &L, uint32_t k, const float *mn, const float *mx, const float *v)
+{
+    uint32_t nk = L.n[k];
+    for (int a = 0; a < 3; a++) {
+        L.box[6 * k + a] = mn[a];
+        float hi = __fadd_rn(mx[a], v[a]);
+        L.box[6 * k + 3 + a] = hi;
+        // The float sum of nk values in [0, extent] stays below 2 * nk * extent
+        // for any nk this builder accepts (each addition rounds up by at most
+        // 2^-24 relative); were it ever higher, its chunks would just be added
+        // one voxel at a time.
+        double bound = 2.0 * (double)nk * (double)__fsub_rn(hi, mn[a]);
+        int ehi = -100000;
+        if (bound > 0.0 && bound < 1e38) {
+            int ex;
+            frexp(bound, &ex);
+            ehi = ex - 24;           // bound in [2^(ex-1), 2^ex): its ulp exponent
+            if (ehi < -149) ehi = -149;
+        }
+        L.ehi[3 * k + a] = ehi;
+    }
+}
+
+// Bounding boxes (calc_bounding_box, tree.c:138-155) of nodes of at most TINY
+// voxels: the serial scan itself, one thread per node.
+__global__ void k_box_thread(const float *P, Level L, float vx, float vy, float vz)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L.m || L.n[k] > TINY) return;
+    const float *p = P + 3 * (uint64_t)L.start[k];
+    float mn[3] = {p[0], p[1], p[2]}, mx[3] = {p[0], p[1], p[2]};
+    for (uint32_t i = 1; i < L.n[k]; i++)
+        for (int a = 0; a < 3; a++) {
+            float x = p[3 * i + a];
+            if (x < mn[a]) mn[a] = x;
+            else if (x > mx[a]) mx[a] = x;
+        }
+    float v[3] = {vx, vy, vz};
+    write_box(L, k, mn, mx, v);
+}
+
+// The other nodes: a warp per node over its voxels, or over its chunks'
+// partial extremes for a big node (listed for the centre kernel).
+__global__ void k_box_warp(const float *P, Level L, const float *cv, const uint32_t *ci, float vx, float vy,
+                           float vz, uint32_t *big, uint32_t *nbig)
 {
     uint32_t k = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     int lane = threadIdx.x & 31;
     if (k >= L.m) return;
     uint32_t nk = L.n[k];
+    if (nk <= TINY) return;
     Extremes x;
     x.init();
     if (nk > BIG) {
@@ -388,22 +432,8 @@ __global__ void k_node_box(const float *P, Level L, const float *cv, const uint3
     x.warp_merge();
     if (lane) return;
     float v[3] = {vx, vy, vz};
-    for (int a = 0; a < 3; a++) {
-        L.box[6 * k + a] = x.mn[a];
-        L.box[6 * k + 3 + a] = __fadd_rn(x.mx[a], v[a]);
-        // A float sum of nk values in [0, extent] stays below 4 * nk * extent
-        // (each addition rounds up by at most 2^-24 relative).
-        double ext = (double)__fsub_rn(__fadd_rn(x.mx[a], v[a]), x.mn[a]);
-        double bound = 4.0 * (double)nk * ext;
-        int ehi = -100000;
-        if (bound > 0.0 && bound < 1e38) {
-            int ex;
-            frexp(bound, &ex);
-            ehi = ex - 24;           // bound in [2^(ex-1), 2^ex): its ulp exponent
-            if (ehi < -149) ehi = -149;
-        }
-        L.ehi[3 * k + a] = ehi;
-    }
+    write_box(L, k, x.mn, x.mx, v);
+    if (nk > BIG) big[atomicAdd(nbig, 1u)] = k;
 }
 
 // ---- the two-state machine of a float sum within one binade
@@ -427,7 +457,11 @@ __device__ __forceinline__ Tr tr_cat(Tr f, Tr g)   // f, then g
 // Adding d >= 0 to A * 2^e, A in [2^23, 2^24), with round to nearest even.
 __device__ __forceinline__ Tr tr_elem(float d, int e)
 {
-    float x = ldexpf(d, -e);   // exact scaling (a tiny x that rounds stays far below one half)
+    // d / 2^e by a power-of-two multiply: exact, except that an x below the
+    // normal range may round, which leaves it far below one half all the same.
+    // Binades whose 2^-e is not a normal float never get a usable map.
+    if (e < -126 || e > 126) return {SAT, SAT | 0x80000000u};
+    float x = __fmul_rn(d, __int_as_float((127 - e) << 23));
     if (!(x < 33554432.0f)) return {SAT, SAT | 0x80000000u};
     float qf = floorf(x);
     float f = __fsub_rn(x, qf);
@@ -445,8 +479,13 @@ __device__ __forceinline__ Tr tr_shfl_down(Tr t, int off)
 
 // Maps of one chunk of a big node, for the NBIN binades ending at the node's
 // top binade, per axis; and whether any of its d is non-zero.
+__device__ __forceinline__ size_t map_index(uint64_t maxc, int a, uint32_t c, int bi)
+{
+    return (((size_t)a * maxc + c) * NBIN + bi) * 2;
+}
+
 __global__ void __launch_bounds__(CHUNK_THREADS) k_chunk_maps(const float *P, Level L, const uint32_t *total,
-                                                             uint32_t *maps, uint8_t *nz)
+                                                             uint32_t *maps, uint8_t *nz, uint64_t maxc)
 {
     __shared__ Tr part[NBIN][3][CHUNK_THREADS / 32];
     __shared__ uint32_t any[3];
@@ -485,70 +524,214 @@ __global__ void __launch_bounds__(CHUNK_THREADS) k_chunk_maps(const float *P, Le
         int bi = threadIdx.x / 3, a = threadIdx.x % 3;
         Tr t = part[bi][a][0];
         for (int w = 1; w < CHUNK_THREADS / 32; w++) t = tr_cat(t, part[bi][a][w]);
-        size_t o = (((size_t)c * NBIN + bi) * 3 + a) * 2;
+        size_t o = map_index(maxc, a, c, bi);
         maps[o] = t.w0;
         maps[o + 1] = t.w1;
     }
     if (threadIdx.x < 3) nz[3 * c + threadIdx.x] = (uint8_t)any[threadIdx.x];
 }
 
-__device__ __forceinline__ float add_serial(const float *P, uint64_t b, uint64_t e, int a, float mn, float acc)
+// acc plus the d of positions [b, e) in order, by one warp (every lane returns
+// the same sum): 128 voxels a step, 4 consecutive ones per lane, added by the
+// composed map of the binade acc is in, or one at a time when acc is not a
+// normal float or the step would leave its binade.
+__device__ float warp_sum(const float *P, uint64_t b, uint64_t e, int a, float mn, float acc)
 {
-    for (uint64_t t = b; t < e; t++) acc = __fadd_rn(__fsub_rn(P[3 * t + a], mn), acc);
+    int lane = threadIdx.x & 31;
+    float nx[4];
+    for (int j = 0; j < 4; j++) {
+        uint64_t t = b + 4 * (uint64_t)lane + j;
+        nx[j] = t < e ? P[3 * t + a] : mn;
+    }
+    for (uint64_t s = b; s < e; s += 128) {
+        float d[4];
+        for (int j = 0; j < 4; j++) d[j] = __fsub_rn(nx[j], mn);   // past e: +0, which changes no sum
+        for (int j = 0; j < 4; j++) {                              // the next step's voxels, in flight meanwhile
+            uint64_t t = s + 128 + 4 * (uint64_t)lane + j;
+            nx[j] = t < e ? P[3 * t + a] : mn;
+        }
+        uint32_t bits = __float_as_uint(acc), E = bits >> 23;
+        if (E >= 1u && E < 255u) {
+            int ee = (int)E - 150;
+            Tr t = tr_cat(tr_cat(tr_elem(d[0], ee), tr_elem(d[1], ee)), tr_cat(tr_elem(d[2], ee), tr_elem(d[3], ee)));
+            for (int off = 1; off < 32; off <<= 1) {
+                Tr u = tr_shfl_down(t, off);
+                if ((lane & (2 * off - 1)) == 0) t = tr_cat(t, u);
+            }
+            uint32_t A = (bits & 0x7FFFFFu) | 0x800000u;
+            uint32_t w = __shfl_sync(0xffffffffu, (A & 1u) ? t.w1 : t.w0, 0);
+            uint32_t An = A + (w & 0x7FFFFFFFu);
+            if (An < (1u << 24)) {
+                acc = __uint_as_float((E << 23) | (An & 0x7FFFFFu));
+                continue;
+            }
+        }
+        for (int l = 0; l < 32; l++)
+            for (int j = 0; j < 4; j++) acc = __fadd_rn(__shfl_sync(0xffffffffu, d[j], l), acc);
+    }
     return acc;
 }
 
-// Node kinds and subdivision centres (tree.c:249-275 and find_center,
-// tree.c:125-136; density test geom.c:157-167).
-__global__ void k_classify(const float *P, Level L, const uint32_t *maps, const uint8_t *nz, float vx, float vy,
-                           float vz)
+__device__ __forceinline__ float centre_of(float acc, uint32_t nk, float mn, float v)
 {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    float mean = __fadd_rn(__fdiv_rn(acc, __uint2float_rn(nk)), mn);
+    return __fmul_rn(ceilf(__fdiv_rn(mean, v)), v);
+}
+
+// Node kinds and, for nodes of at most BIG voxels, subdivision centres
+// (tree.c:249-275, find_center tree.c:125-136, density test geom.c:157-167);
+// a warp per node.
+__global__ void k_classify(const float *P, Level L, float vx, float vy, float vz)
+{
+    uint32_t k = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    int lane = threadIdx.x & 31;
     if (k >= L.m) return;
     uint32_t nk = L.n[k];
     const float *bx = L.box + 6 * k;
-    float v[3] = {vx, vy, vz};
     float s0 = __fsub_rn(bx[3], bx[0]), s1 = __fsub_rn(bx[4], bx[1]), s2 = __fsub_rn(bx[5], bx[2]);
     float bbv = __fmul_rn(__fmul_rn(s0, s1), s2);
     float vv = __fmul_rn(__fmul_rn(vx, vy), vz);
-    float nf = __uint2float_rn(nk);
-    if (fabsf(__fsub_rn(__fmul_rn(nf, vv), bbv)) < vv) {
-        L.kind[k] = K_DENSE;
-        return;
-    }
-    if (nk <= VOX_MAX_DOTS) {
-        L.kind[k] = K_LEAF;
-        return;
-    }
-    L.kind[k] = K_INNER;
-    uint64_t s = L.start[k], end = s + nk;
+    uint8_t kind = fabsf(__fsub_rn(__fmul_rn(__uint2float_rn(nk), vv), bbv)) < vv ? K_DENSE
+                 : (nk <= VOX_MAX_DOTS ? K_LEAF : K_INNER);
+    if (lane == 0) L.kind[k] = kind;
+    if (kind != K_INNER || nk > BIG) return;
+    float v[3] = {vx, vy, vz};
+    uint64_t s = L.start[k];
     for (int a = 0; a < 3; a++) {
-        float mn = bx[a], acc = 0.0f;
-        if (nk <= BIG) {
-            acc = add_serial(P, s, end, a, mn, acc);
-        } else {
-            uint32_t nch = (nk + CHUNK - 1) / CHUNK, c0 = L.chunk_base[k];
-            int elo = L.ehi[3 * k + a] - (NBIN - 1);
-            for (uint32_t j = 0; j < nch; j++) {
-                uint32_t c = c0 + j;
-                uint64_t b = s + (uint64_t)j * CHUNK, e = min(b + CHUNK, end);
-                if (acc == 0.0f && !nz[3 * c + a]) continue;   // all of its d are zero
-                uint32_t bits = __float_as_uint(acc), E = bits >> 23;
-                int bi = (int)E - 150 - elo;
-                if (E >= 1u && E < 255u && bi >= 0 && bi < NBIN) {
-                    uint32_t A = (bits & 0x7FFFFFu) | 0x800000u;
-                    uint32_t w = maps[(((size_t)c * NBIN + bi) * 3 + a) * 2 + (A & 1u)];
-                    uint32_t An = A + (w & 0x7FFFFFFFu);
-                    if (An < (1u << 24)) {
-                        acc = __uint_as_float((E << 23) | (An & 0x7FFFFFu));
-                        continue;
-                    }
+        float acc = warp_sum(P, s, s + nk, a, bx[a], 0.0f);
+        if (lane == 0) L.centre[3 * k + a] = centre_of(acc, nk, bx[a], v[a]);
+    }
+}
+
+// Centres of big nodes: a warp per (node, axis) walks the node's chunks,
+// taking each chunk's map of the binade the sum is in from shared memory.
+constexpr int CENTRE_WARPS = 4;
+__global__ void __launch_bounds__(CENTRE_WARPS * 32) k_centre_big(const float *P, Level L, const uint32_t *big,
+                                                                  const uint32_t *nbig, const uint32_t *maps,
+                                                                  const uint8_t *nz, uint64_t maxc, float vx,
+                                                                  float vy, float vz)
+{
+    __shared__ uint32_t sm[CENTRE_WARPS][32 * NBIN * 2];
+    __shared__ uint8_t snz[CENTRE_WARPS][32];
+    uint32_t w = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+    uint32_t j = w / 3;
+    int a = (int)(w % 3);
+    if (j >= *nbig) return;
+    uint32_t k = big[j];
+    if (L.kind[k] != K_INNER) return;
+    uint32_t nk = L.n[k], nch = (nk + CHUNK - 1) / CHUNK, c0 = L.chunk_base[k];
+    uint64_t s = L.start[k], end = s + nk;
+    float mn = L.box[6 * k + a], acc = 0.0f;
+    int elo = L.ehi[3 * k + a] - (NBIN - 1);
+    for (uint32_t g = 0; g < nch; g += 32) {
+        uint32_t cnt = min(32u, nch - g);
+        const uint32_t *src = maps + map_index(maxc, a, c0 + g, 0);
+        __syncwarp();
+        for (uint32_t i = lane; i < cnt * NBIN * 2; i += 32) sm[wb][i] = src[i];
+        if ((uint32_t)lane < cnt) snz[wb][lane] = nz[3 * (c0 + g + lane) + a];
+        __syncwarp();
+        for (uint32_t i = 0; i < cnt; i++) {
+            if (acc == 0.0f && !snz[wb][i]) continue;   // all of its d are zero
+            uint32_t bits = __float_as_uint(acc), E = bits >> 23;
+            int bi = (int)E - 150 - elo;
+            if (E >= 1u && E < 255u && bi >= 0 && bi < NBIN) {
+                uint32_t A = (bits & 0x7FFFFFu) | 0x800000u;
+                uint32_t An = A + (sm[wb][(i * NBIN + bi) * 2 + (A & 1u)] & 0x7FFFFFFFu);
+                if (An < (1u << 24)) {
+                    acc = __uint_as_float((E << 23) | (An & 0x7FFFFFu));
+                    continue;
                 }
-                acc = add_serial(P, b, e, a, mn, acc);
             }
+            uint64_t b = s + (uint64_t)(g + i) * CHUNK;
+            acc = warp_sum(P, b, min(b + CHUNK, end), a, mn, acc);
         }
-        float mean = __fadd_rn(__fdiv_rn(acc, nf), mn);
-        L.centre[3 * k + a] = __fmul_rn(ceilf(__fdiv_rn(mean, v[a])), v[a]);
+    }
+    float v[3] = {vx, vy, vz};
+    if (lane == 0) L.centre[3 * k + a] = centre_of(acc, nk, mn, v[a]);
+}
+
+// The eight swapping passes (sort_set, tree.c:166-183) of nodes of at most
+// SMALL voxels: a warp per node in shared memory, each pass in the parallel
+// form of the file's header (ballot prefix counts, the walk back for the rest).
+constexpr int PART_WARPS = 4;
+__global__ void __launch_bounds__(PART_WARPS * 32) k_partition_warp(Level L, uint32_t *idx, uint8_t *oct,
+                                                                     uint32_t *err)
+{
+    __shared__ uint32_t sidx[PART_WARPS][2][SMALL];
+    __shared__ uint8_t soct[PART_WARPS][2][SMALL];
+    __shared__ uint16_t sc[PART_WARPS][SMALL], su[PART_WARPS][SMALL];
+    uint32_t k = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    uint32_t lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+    if (k >= L.m) return;
+    uint32_t nk = L.n[k];
+    if (L.kind[k] != K_INNER || nk > SMALL) return;
+    uint32_t s0 = L.start[k];
+    for (uint32_t i = lane; i < nk; i += 32) {
+        sidx[wb][0][i] = idx[s0 + i];
+        soct[wb][0][i] = oct[s0 + i];
+    }
+    __syncwarp();
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t from = 0;
+    int cur = 0;
+    for (uint32_t o = 0; o < 8; o++) {
+        const uint32_t *in_i = sidx[wb][cur];
+        const uint8_t *in_o = soct[wb][cur];
+        uint32_t *out_i = sidx[wb][cur ^ 1];
+        uint8_t *out_o = soct[wb][cur ^ 1];
+        for (uint32_t i = lane; i < from; i += 32) {   // claimed by earlier passes
+            out_i[i] = in_i[i];
+            out_o[i] = in_o[i];
+        }
+        uint32_t run = 0, urun = 0;
+        for (uint32_t base = from; base < nk; base += 32) {
+            uint32_t t = base + lane;
+            bool in = t < nk;
+            uint8_t q = in ? in_o[t] : (uint8_t)0xFF;
+            bool cl = in && q == o;
+            uint32_t bm = __ballot_sync(0xffffffffu, cl), um = __ballot_sync(0xffffffffu, in && !cl);
+            uint32_t crel = run + __popc(bm & lt), urel = urun + __popc(um & lt);
+            if (in) {
+                sc[wb][t] = (uint16_t)crel;
+                if (cl) {
+                    out_i[from + crel] = in_i[t];
+                    out_o[from + crel] = q;
+                } else {
+                    su[wb][from + urel] = (uint16_t)t;
+                }
+            }
+            run += __popc(bm);
+            urun += __popc(um);
+        }
+        __syncwarp();
+        for (uint32_t t = from + run + lane; t < nk; t += 32) {
+            uint32_t s = t;
+            for (uint32_t steps = 0; in_o[s] == o; steps++) {
+                uint32_t u = (s - from) - sc[wb][s];
+                if (u == 0 || steps > SMALL) {
+                    atomicOr(err, ERR_WALK);
+                    break;
+                }
+                uint32_t a = su[wb][from + u - 1] + 1u;
+                uint32_t back = ((s - a) / u + 1) * u;
+                if (a > s || back > s - from) {
+                    atomicOr(err, ERR_WALK);
+                    break;
+                }
+                s -= back;
+            }
+            out_i[t] = in_i[s];
+            out_o[t] = in_o[s];
+        }
+        if (lane == 0) L.cnt[8 * k + o] = run;
+        from += run;
+        cur ^= 1;
+        __syncwarp();
+    }
+    for (uint32_t i = lane; i < nk; i += 32) {   // eight passes: back in buffer 0
+        idx[s0 + i] = sidx[wb][0][i];
+        oct[s0 + i] = soct[wb][0][i];
     }
 }
 
@@ -568,19 +751,25 @@ __global__ void k_oct_init(const float *P, Level L, const uint32_t *seg_of, uint
     oct[t] = (uint8_t)((c[0] > p[0]) | ((c[1] > p[1]) << 1) | ((c[2] > p[2]) << 2));
 }
 
-// ---- one swapping pass (sort_set, tree.c:166-183) over every node to split
+// ---- one swapping pass (sort_set, tree.c:166-183) over every node above SMALL
+//
+// Four kernels a pass: claimed counts per tile of SCAN_TILE positions (and,
+// for every range starting in a tile, the count before its start), a scan of
+// the tile counts, the claimed voxels to the front (with each position's
+// claimed count since its range start and the unclaimed positions listed),
+// then the walk back for the rest of each range.
 
 struct Pass {
     const uint32_t *seg_of, *start, *n, *cnt;
-    const uint8_t *kind, *oct;   // octants in the pass's input order
+    const uint8_t *kind;
     uint32_t o;
     // The node of position t and where its pass range starts; false when t
     // is outside every pass range (voxels of other octants already claimed,
-    // nodes not split, voxels already in leaves).
+    // nodes not split here, voxels already in leaves).
     __device__ __forceinline__ bool range(uint64_t t, uint32_t &k, uint32_t &from) const
     {
         k = seg_of[t];
-        if (k == NONE || kind[k] != K_INNER) return false;
+        if (k == NONE || kind[k] != K_INNER || n[k] <= SMALL) return false;
         uint32_t f = start[k];
         for (uint32_t q = 0; q < o; q++) f += cnt[8 * k + q];
         from = f;
@@ -588,53 +777,103 @@ struct Pass {
     }
 };
 
-struct Claimed {
-    Pass p;
-    __device__ uint32_t operator()(uint64_t t) const
-    {
-        uint32_t k, f;
-        return p.range(t, k, f) && p.oct[t] == p.o;
-    }
-};
-
-// Claimed voxels to the front of their range, in order; unclaimed positions
-// listed; the claimed count of each node.  Positions outside the ranges are
-// carried over unchanged.
-__global__ void k_pass_front(Pass p, uint64_t N, const uint32_t *C, const uint32_t *in_idx, uint32_t *out_idx,
-                             uint8_t *out_oct, uint32_t *upos, uint32_t *cnt)
+// Block-wide exclusive scan of one flag per thread; *total gets the block's sum.
+__device__ __forceinline__ uint32_t block_excl(uint32_t x, uint32_t *ws, uint32_t &total)
 {
-    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N) return;
-    uint32_t k, from;
-    if (!p.range(t, k, from)) {
-        out_idx[t] = in_idx[t];
-        out_oct[t] = p.oct[t];
-        return;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = warp_incl_scan(x);
+    if (lane == 31) ws[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, tot = 0;
+    for (int q = 0; q < SCAN_THREADS / 32; q++) {
+        uint32_t t = ws[q];
+        before += q < warp ? t : 0u;
+        tot += t;
     }
-    uint32_t crel = C[t] - C[from];
-    bool cl = p.oct[t] == p.o;
-    if (cl) {
-        out_idx[from + crel] = in_idx[t];
-        out_oct[from + crel] = (uint8_t)p.o;
-    } else {
-        upos[from + ((uint32_t)t - from) - crel] = (uint32_t)t;
+    __syncthreads();
+    total = tot;
+    return before + incl - x;
+}
+
+// Claimed count of each tile, and for every range starting in the tile the
+// count before its start within the tile.
+__device__ __forceinline__ void tile_count(const Pass &p, uint64_t t, bool cl, bool head, uint32_t k,
+                                           uint32_t &run, uint32_t *ws, uint32_t *head_before)
+{
+    uint32_t tot;
+    uint32_t ex = block_excl(cl ? 1u : 0u, ws, tot);
+    if (head) head_before[k] = run + ex;
+    run += tot;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_pass_count(Pass p, const uint8_t *oct, uint64_t N,
+                                                             uint32_t *tile, uint32_t *head_before)
+{
+    __shared__ uint32_t ws[SCAN_THREADS / 32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    uint32_t run = 0;
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        uint64_t t = base + (uint64_t)j * SCAN_THREADS + threadIdx.x;
+        uint32_t k = 0, from = 0;
+        bool in = t < N && p.range(t, k, from);
+        tile_count(p, t, in && oct[t] == p.o, in && t == from, k, run, ws, head_before);
     }
-    if (t + 1 == (uint64_t)p.start[k] + p.n[k]) cnt[8 * k + p.o] = crel + (cl ? 1u : 0u);
+    if (threadIdx.x == 0) tile[blockIdx.x] = run;
+}
+
+// Claimed voxels to the front of their range, in order; each position's
+// claimed count since its range start (C); unclaimed positions listed; each
+// node's claimed count.  Positions outside the ranges are carried over.
+__global__ void __launch_bounds__(SCAN_THREADS) k_pass_front(Pass p, uint64_t N, const uint32_t *tile,
+                                                             const uint32_t *head_before, const uint8_t *in_oct,
+                                                             const uint32_t *in_idx, uint8_t *out_oct,
+                                                             uint32_t *out_idx, uint32_t *C, uint32_t *upos,
+                                                             uint32_t *cnt)
+{
+    __shared__ uint32_t ws[SCAN_THREADS / 32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
+    uint32_t run = tile[blockIdx.x];   // claimed positions before this tile
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        uint64_t t = base + (uint64_t)j * SCAN_THREADS + threadIdx.x;
+        uint32_t k = 0, from = 0;
+        bool in = t < N && p.range(t, k, from);
+        uint8_t q = t < N ? in_oct[t] : (uint8_t)0xFF;
+        bool cl = in && q == p.o;
+        uint32_t tot;
+        uint32_t ex = block_excl(cl ? 1u : 0u, ws, tot);
+        if (t < N) {
+            if (!in) {
+                out_idx[t] = in_idx[t];
+                out_oct[t] = q;
+            } else {
+                uint32_t cf = tile[from / SCAN_TILE] + head_before[k];   // claimed positions before the range
+                uint32_t crel = run + ex - cf;
+                C[t] = crel;
+                if (cl) {
+                    out_idx[from + crel] = in_idx[t];
+                    out_oct[from + crel] = q;
+                } else {
+                    upos[from + ((uint32_t)t - from) - crel] = (uint32_t)t;
+                }
+                if (t + 1 == (uint64_t)p.start[k] + p.n[k]) cnt[8 * k + p.o] = crel + (cl ? 1u : 0u);
+            }
+        }
+        run += tot;
+    }
 }
 
 // The rest of each range: the walk back described at the top of the file.
-__global__ void k_pass_back(Pass p, uint64_t N, const uint32_t *C, const uint32_t *upos, const uint32_t *in_idx,
-                            uint32_t *out_idx, uint8_t *out_oct, uint32_t *err)
+__global__ void k_pass_back(Pass p, uint64_t N, const uint32_t *C, const uint32_t *upos, const uint8_t *in_oct,
+                            const uint32_t *in_idx, uint8_t *out_oct, uint32_t *out_idx, uint32_t *err)
 {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     uint32_t k, from;
-    if (!p.range(t, k, from)) return;
-    if ((uint32_t)t - from < p.cnt[8 * k + p.o]) return;
-    uint32_t cf = C[from], s = (uint32_t)t;
-    for (uint32_t steps = 0; p.oct[s] == p.o; steps++) {
-        uint32_t u = (s - from) - (C[s] - cf);   // unclaimed positions before s
-        if (u == 0 || steps > (1u << 22)) {      // impossible for a consistent pass
+    if (!p.range(t, k, from) || (uint32_t)t - from < p.cnt[8 * k + p.o]) return;
+    uint32_t s = (uint32_t)t;
+    for (uint32_t steps = 0; in_oct[s] == p.o; steps++) {
+        uint32_t u = (s - from) - C[s];           // unclaimed positions before s
+        if (u == 0 || steps > (1u << 22)) {        // impossible for a consistent pass
             atomicOr(err, ERR_WALK);
             break;
         }
@@ -647,7 +886,7 @@ __global__ void k_pass_back(Pass p, uint64_t N, const uint32_t *C, const uint32_
         s -= back;
     }
     out_idx[t] = in_idx[s];
-    out_oct[t] = p.oct[s];
+    out_oct[t] = in_oct[s];
 }
 
 __global__ void k_gather(uint64_t N, const uint32_t *idx, const float *P, float *Pn)
@@ -661,24 +900,28 @@ __global__ void k_gather(uint64_t N, const uint32_t *idx, const float *P, float 
 }
 
 // Overflowed leaves (one octant took the whole set, tree.c:281-305), child
-// masks and per-level counts (inner, leaves, dense leaves, leaf voxels).
-__global__ void k_finish(Level L, unsigned long long *stats, uint32_t *err)
+// masks, per-level counts (inner, leaves, dense leaves, leaf voxels) and the
+// largest child.
+__global__ void k_finish(Level L, unsigned long long *stats, uint32_t *largest, uint32_t *err)
 {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= L.m) return;
     uint8_t kind = L.kind[k];
-    uint32_t mask = 0;
+    uint32_t mask = 0, top = 0;
     if (kind == K_INNER) {
         bool over = false;
         for (int o = 0; o < 8; o++) {
             uint32_t c = L.cnt[8 * k + o];
             over |= c == L.n[k];
             mask |= (c ? 1u : 0u) << o;
+            top = max(top, c);
         }
         if (over) {
             kind = K_OVER;
             mask = 0;
             L.kind[k] = K_OVER;
+        } else {
+            atomicMax(largest, top);
         }
     }
     L.mask[k] = (uint8_t)mask;
@@ -898,11 +1141,12 @@ int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s)
     } level_free{levels, s};
 
     float *P[2];
-    uint32_t *idx[2], *C, *upos, *seg_of, *tile, *scal, *maps, *cidx;
+    uint32_t *idx[2], *C, *upos, *seg_of, *tile, *scal, *maps, *cidx, *big;
     uint8_t *oct[2], *nz;
     float *cv;
     unsigned long long *stats;
     uint64_t max_chunks = N / CHUNK + N / BIG + 2;
+    uint64_t max_big = N / BIG + 1;
     uint64_t max_tiles = N / SCAN_TILE + 2;
     TRY(d.get(&P[0], 3 * N));
     TRY(d.get(&P[1], 3 * N));
@@ -914,11 +1158,21 @@ int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s)
     TRY(d.get(&upos, N));
     TRY(d.get(&seg_of, N));
     TRY(d.get(&tile, max_tiles));
-    TRY(d.get(&scal, 8));      // scan totals and the error word (scal[7])
-    TRY(d.get(&cv, 6 * max_chunks));
-    TRY(d.get(&cidx, 6 * max_chunks));
-    TRY(d.get(&maps, max_chunks * NBIN * 3 * 2));
-    TRY(d.get(&nz, 3 * max_chunks));
+    uint32_t *hbefore;   // per node: claimed count before its range start within its tile
+    TRY(d.get(&hbefore, N));
+    // scal: 0 chunks, 1 claimed, 2 children, 3 big nodes, 4 largest child, 7 error bits
+    TRY(d.get(&scal, 8));
+    TRY(d.get(&big, max_big));
+    if (N > BIG) {
+        TRY(d.get(&cv, 6 * max_chunks));
+        TRY(d.get(&cidx, 6 * max_chunks));
+        TRY(d.get(&maps, max_chunks * NBIN * 3 * 2));
+        TRY(d.get(&nz, 3 * max_chunks));
+    } else {
+        cv = nullptr;
+        cidx = maps = nullptr;
+        nz = nullptr;
+    }
     TRY(d.get(&stats, 4 * MAX_LEVELS));
     uint32_t *err = scal + 7;
     TRY(cudaMemsetAsync(scal, 0, 8 * 4, s));
@@ -941,40 +1195,67 @@ int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s)
         ~HostFree() { cudaFreeHost(p); }
     } host_free{h_next};
 
+    uint32_t largest = (uint32_t)N;   // the largest node of the level
     for (int lv = 0;; lv++) {
         if (lv >= MAX_LEVELS) return VOX_CUDA_EDEPTH;
         Level L = levels[lv];
         uint32_t m = L.m;
+        TRY(cudaMemsetAsync(scal, 0, 5 * 4, s));
         k_seg_of<<<grid_for(N, TB), TB, 0, s>>>(L.start, L.n, m, N, seg_of);
         count_launch();
-        // big nodes: chunk extremes, boxes, chunk maps
-        scan(ChunkCount{L.n}, StoreExcl{L.chunk_base}, m, tile, scal + 0, s);
-        k_chunk_box<<<(unsigned)max_chunks, CHUNK_THREADS, 0, s>>>(P[cur], L, scal + 0, cv, cidx);
-        k_node_box<<<grid_for((uint64_t)m * 32, TB), TB, 0, s>>>(P[cur], L, cv, cidx, vx, vy, vz);
-        k_chunk_maps<<<(unsigned)max_chunks, CHUNK_THREADS, 0, s>>>(P[cur], L, scal + 0, maps, nz);
-        k_classify<<<grid_for(m, 128), 128, 0, s>>>(P[cur], L, maps, nz, vx, vy, vz);
-        k_oct_init<<<grid_for(N, TB), TB, 0, s>>>(P[cur], L, seg_of, N, idx[0], oct[0]);
-        for (int i = 0; i < 5; i++) count_launch();
-        // the eight swapping passes; the result lands back in buffer 0
-        for (uint32_t o = 0; o < 8; o++) {
-            int in = o & 1, out = in ^ 1;
-            Pass p{seg_of, L.start, L.n, L.cnt, L.kind, oct[in], o};
-            scan(Claimed{p}, StoreExcl{C}, N, tile, scal + 1, s);
-            k_pass_front<<<grid_for(N, TB), TB, 0, s>>>(p, N, C, idx[in], idx[out], oct[out], upos, L.cnt);
-            k_pass_back<<<grid_for(N, TB), TB, 0, s>>>(p, N, C, upos, idx[in], idx[out], oct[out], err);
-            count_launch();
+        bool has_big = largest > BIG;
+        if (has_big) {   // chunk extremes of big nodes
+            scan(ChunkCount{L.n}, StoreExcl{L.chunk_base}, m, tile, scal + 0, s);
+            k_chunk_box<<<(unsigned)max_chunks, CHUNK_THREADS, 0, s>>>(P[cur], L, scal + 0, cv, cidx);
             count_launch();
         }
+        k_box_thread<<<grid_for(m, TB), TB, 0, s>>>(P[cur], L, vx, vy, vz);
+        count_launch();
+        if (largest > TINY) {
+            k_box_warp<<<grid_for((uint64_t)m * 32, TB), TB, 0, s>>>(P[cur], L, cv, cidx, vx, vy, vz, big, scal + 3);
+            count_launch();
+        }
+        if (has_big) {
+            k_chunk_maps<<<(unsigned)max_chunks, CHUNK_THREADS, 0, s>>>(P[cur], L, scal + 0, maps, nz, max_chunks);
+            count_launch();
+        }
+        k_classify<<<grid_for((uint64_t)m * 32, TB), TB, 0, s>>>(P[cur], L, vx, vy, vz);
+        count_launch();
+        if (has_big) {
+            k_centre_big<<<grid_for(max_big * 3 * 32, CENTRE_WARPS * 32), CENTRE_WARPS * 32, 0, s>>>(
+                P[cur], L, big, scal + 3, maps, nz, max_chunks, vx, vy, vz);
+            count_launch();
+        }
+        k_oct_init<<<grid_for(N, TB), TB, 0, s>>>(P[cur], L, seg_of, N, idx[0], oct[0]);
+        count_launch();
+        if (largest > SMALL) {
+            // the eight swapping passes of nodes above SMALL; the result lands back in buffer 0
+            unsigned nt = (unsigned)((N + SCAN_TILE - 1) / SCAN_TILE);
+            for (uint32_t o = 0; o < 8; o++) {
+                int in = o & 1, out = in ^ 1;
+                Pass p{seg_of, L.start, L.n, L.cnt, L.kind, o};
+                k_pass_count<<<nt, SCAN_THREADS, 0, s>>>(p, oct[in], N, tile, hbefore);
+                k_scan_tiles<<<1, 1024, 0, s>>>(tile, nt, scal + 1);
+                k_pass_front<<<nt, SCAN_THREADS, 0, s>>>(p, N, tile, hbefore, oct[in], idx[in], oct[out], idx[out], C,
+                                                         upos, L.cnt);
+                k_pass_back<<<grid_for(N, TB), TB, 0, s>>>(p, N, C, upos, oct[in], idx[in], oct[out], idx[out], err);
+                for (int i = 0; i < 4; i++) count_launch();
+            }
+        }
+        k_partition_warp<<<grid_for((uint64_t)m * 32, PART_WARPS * 32), PART_WARPS * 32, 0, s>>>(L, idx[0], oct[0],
+                                                                                              err);
         k_gather<<<grid_for(N, TB), TB, 0, s>>>(N, idx[0], P[cur], P[cur ^ 1]);
         cur ^= 1;
-        k_finish<<<grid_for(m, TB), TB, 0, s>>>(L, stats + 4 * lv, err);
+        k_finish<<<grid_for(m, TB), TB, 0, s>>>(L, stats + 4 * lv, scal + 4, err);
+        count_launch();
         count_launch();
         count_launch();
         scan(ChildCount{L.mask}, StoreExcl{L.first_child}, m, tile, scal + 2, s);
         TRY(cudaGetLastError());
-        TRY(cudaMemcpyAsync(h_next, scal + 2, 4, cudaMemcpyDeviceToHost, s));
+        TRY(cudaMemcpyAsync(h_next, scal + 2, 12, cudaMemcpyDeviceToHost, s));
         TRY(cudaStreamSynchronize(s));
         uint32_t mn = h_next[0];
+        largest = h_next[2];
         if (mn == 0) break;
         Level Nx;
         TRY(level_alloc(Nx, mn, s));
