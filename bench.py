@@ -295,6 +295,59 @@ def measure_editing(vg, vox, edits=1000, seed=16):
                     "volume) on the host tree, then vox_cuda_tree_refresh of its device copy"}
 
 
+def measure_tree_build(vg, sizes=((256, 2, 0.08), (512, 3, 0.10)), reps=5):
+    """Time to a searchable device tree for the noise volumes: the drop-in
+    path (the library's vox_make_tree on the host, then
+    vox_cuda_tree_upload) against the tree built on the GPU from the same
+    voxel set in host memory (vox_cuda_tree_build), already on the device
+    (vox_cuda_tree_build_device) and from the raw u8 samples with the band
+    test on the GPU (vox_cuda_tree_build_raw).  Medians of `reps` after one
+    warm-up; wall-clock, all synchronous calls."""
+    import torch
+    from voxvision_gb300 import workloads as wl
+    out = []
+    for n, seed, solid in sizes:
+        vol = wl.value_noise_u8(n, seed)
+        lo, w = wl.band_for_fraction(vol, solid)
+        vox = wl.voxels_from_mask((vol >= lo) & (vol < lo + w))
+        raw = vol.tobytes()
+        d_vox = torch.from_numpy(vox).cuda()
+
+        def timed(fn):
+            fn().close()
+            ts = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                r = fn()
+                ts.append(time.perf_counter() - t0)
+                r.close()
+            return float(np.median(ts)) * 1e3
+
+        def host_path():
+            h = vg.HostTree.from_voxels(vox)
+            d = vg.DeviceTree(h.ptr)
+            d._host = h
+            return d
+
+        t0 = time.perf_counter()
+        h = vg.HostTree.from_voxels(vox)
+        t_make = (time.perf_counter() - t0) * 1e3
+        t0 = time.perf_counter()
+        vg.DeviceTree(h.ptr).close()
+        t_up = (time.perf_counter() - t0) * 1e3
+        h.close()
+        rec = {"volume": f"{n}^3 u8 value noise, seed {seed}, band {lo}..{lo + w - 1}", "voxels": int(len(vox)),
+               "host_make_tree_ms": t_make, "upload_ms": t_up,
+               "host_path_ms": timed(host_path) if n <= 256 else t_make + t_up,
+               "device_build_ms": timed(lambda: vg.DeviceTree.build(vox)),
+               "device_build_resident_ms": timed(lambda: vg.DeviceTree.build_device(d_vox)),
+               "device_build_raw_ms": timed(lambda: vg.DeviceTree.from_raw(raw, vol.shape, 1, lo, lo + w - 1))}
+        rec["speedup_vs_host_path"] = rec["host_path_ms"] / rec["device_build_ms"]
+        out.append(rec)
+        del d_vox
+    return out
+
+
 def build_batch_trees(vg):
     from voxvision_gb300 import workloads as wl
     trees = []
@@ -611,6 +664,7 @@ def run_ours(args):
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
         line["served"] = measure_served(vg, btrees, tex)
         line["editing"] = measure_editing(vg, vox)
+        line["tree_build"] = measure_tree_build(vg)
     if not args.no_cpu_baseline and world >= 1:
         line["cpu_baseline"] = cpu_baseline_sample(ht.ptr, states, tex)
     print(json.dumps(line), flush=True)
