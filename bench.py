@@ -70,6 +70,9 @@ def parse_args():
                    help="skip the incoherent-query and batched-frame measurements")
     p.add_argument("--frames", type=int, default=NFRAMES,
                    help="orbit frames per step (profiling runs only; the benchmark uses 120)")
+    p.add_argument("--tree-build", type=int, default=0, metavar="N",
+                   help="only time the device tree build of the N^3 noise volume (profiling runs)")
+    p.add_argument("--reps", type=int, default=5, help="timed repetitions of --tree-build")
     return p.parse_args()
 
 
@@ -708,6 +711,12 @@ def run_reference(args):
 
 def main():
     args = parse_args()
+    if args.tree_build:
+        import voxvision_gb300 as vg
+        vg.set_voxel_size((1, 1, 1))
+        size = {256: (256, 2, 0.08), 512: (512, 3, 0.10)}.get(args.tree_build, (args.tree_build, 2, 0.08))
+        print(json.dumps({"tree_build": measure_tree_build(vg, (size,), reps=args.reps)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
