@@ -15,9 +15,11 @@ diagonal (665.1) at 20 degrees elevation around (128, 128, 128); texture
          (an event between launches would end the overlap of consecutive
          frame kernels); L2 flushed (256 MiB write) between steps, outside
          the timed events.
-  e2e    the same orbit through vox_cuda_render with host buffers: every
-         frame copies the texture in and the 8.3 MB frame out (pinned host
-         memory), timed on the host.
+  e2e    the same orbit through the host-buffer call vox_cuda_render_frames:
+         every step copies the texture and cameras in and delivers each
+         8.3 MB frame into its own page-locked host buffer (copied out while
+         the next frames are drawn), timed on the host; per_call_value gives
+         the same frames through one synchronous vox_cuda_render call each.
   roofline  algorithmic bytes per frame (32 B per node box tested, 16 B per
          inner node entered, 16 B per voxel tested, 4 B per pixel stored;
          counted by the counting kernel, less the root test of the rays
@@ -606,17 +608,31 @@ def run_ours(args):
         total_s = float(t.item())
     value = world * rays_step * args.steps / total_s / 1e6
 
-    # e2e: the host-buffer entry point, texture in and frame out every call
-    host_frame = torch.empty(H * W, dtype=torch.int32).pin_memory()
-    hf_p = C.c_void_p(host_frame.data_ptr())
+    # e2e: the orbit through the host-buffer entry point vox_cuda_render_frames:
+    # every step copies the host texture in and delivers all nf frames into
+    # their own page-locked host buffers (drawn in place over the host link)
+    host_frames = torch.empty((nf, H * W), dtype=torch.int32).pin_memory()
+    frame_ptrs = (C.c_void_p * nf)(*[host_frames[i].data_ptr() for i in range(nf)])
+    cam_arr = (vg.CameraStruct * nf)(*cams)
     htex = np.ascontiguousarray(tex)
     htex_p = htex.ctypes.data_as(C.c_void_p)
+    vg.check(L.vox_cuda_render_frames(dt.h, cam_arr, nf, W, H, htex_p, frame_ptrs, sp), "vox_cuda_render_frames")
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc = L.vox_cuda_render_frames(dt.h, cam_arr, nf, W, H, htex_p, frame_ptrs, sp)
+        if rc:
+            raise vg.VoxCudaError(rc, "vox_cuda_render_frames")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    # the same frames one synchronous vox_cuda_render call each (one host frame)
+    hf_p = C.c_void_p(host_frames[0].data_ptr())
     fn_h = L.vox_cuda_render
     for cr in cam_refs[:8]:
         fn_h(dt.h, cr, W, H, htex_p, hf_p, sp)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         for cr in cam_refs:
@@ -624,14 +640,19 @@ def run_ours(args):
             if rc:
                 raise vg.VoxCudaError(rc, "vox_cuda_render")
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    single_s = time.perf_counter() - t0
     if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        t = torch.tensor([e2e_s, single_s], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s, single_s = float(t[0].item()), float(t[1].item())
     e2e = {"value": world * rays_step * args.steps / e2e_s / 1e6, "unit": "Mrays/s",
-           "h2d_bytes_per_step": nf * 32768, "d2h_bytes_per_step": nf * W * H * 4,
-           "call": "vox_cuda_render (host texture in, host ARGB frame out, pinned)"}
+           "h2d_bytes_per_step": 32768 + nf * C.sizeof(vg.CameraStruct), "d2h_bytes_per_step": nf * W * H * 4,
+           "call": "vox_cuda_render_frames (host texture and cameras in; each frame drawn on the device and "
+                   "copied into its own page-locked host buffer on a second stream while the next frames are "
+                   "drawn; returns when all are in host memory)",
+           "per_call_value": world * rays_step * args.steps / single_s / 1e6,
+           "per_call": "vox_cuda_render, one synchronous call per frame (same frames, one host frame)"}
+    del host_frames
 
     if rank != 0:
         dist.destroy_process_group()

@@ -188,6 +188,16 @@ int vox_cuda_ball_batch_device(const vox_cuda_tree *tree, const float *centres,
 int vox_cuda_render(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
                     uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
                     void *stream);
+/* n BEST frames of one tree, camera cams[i] into the host buffer frames[i]
+ * (w*h ARGB each), with `tex` copied in once: what n calls of
+ * vox_cuda_render give, but the frames overlap on the GPU as device frames
+ * enqueued back to back do, and each is copied out on a second stream while
+ * the next ones are drawn (page-locked frames: the copies run asynchronously;
+ * pageable ones hold the calling thread for their copy).  Device frames of up
+ * to 2 GiB per call are kept per thread for later calls.  Returns when all n
+ * frames are in host memory; VOX_CUDA_ESTACK if any search overflowed. */
+int vox_cuda_render_frames(const vox_cuda_tree *tree, const vox_cuda_camera *cams, uint32_t n, uint32_t w,
+                           uint32_t h, const uint8_t *texture, uint32_t *const *frames, void *stream);
 int vox_cuda_render_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
                            uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
                            void *stream);

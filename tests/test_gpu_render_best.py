@@ -189,6 +189,45 @@ def test_host_frame_pinned_and_pageable(tree256):
         assert np.array_equal(pageable.reshape(1080, 1920), ref)
 
 
+def test_host_frames_call_equals_single_frames(tree256):
+    """vox_cuda_render_frames: an orbit's frames into distinct host buffers,
+    pinned (drawn in place, frames overlapping) and pageable mixed, each
+    equal to the oracle's frame with every pixel written."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import orbit_camera
+    ht, dt = tree256
+    vg().set_render_config(1, 1)
+    tex = wl.texture32(9)
+    w, h = 960, 544
+    cams = [orbit_camera(f, 24, w, h, (128, 128, 128), 1.5 * 256 * 3 ** 0.5) for f in range(0, 24, 3)]
+    bufs = [torch.full((h, w), GARBAGE, dtype=torch.int32).pin_memory() if i % 3 else
+            np.full((h, w), GARBAGE, np.uint32) for i in range(len(cams))]
+    dt.render_frames([c.gpu_struct() for c in cams], w, h, tex, bufs)
+    for i, (cam, b) in enumerate(zip(cams, bufs)):
+        ref, _ = orc.render_best(ht.ptr, cam.state(), w, h, tex)
+        img = b if isinstance(b, np.ndarray) else b.numpy().view(np.uint32)
+        assert np.array_equal(img, ref), f"frame {i}: {(img != ref).sum()} pixels differ"
+
+
+def test_host_frames_call_reuses_device_frames(tree64):
+    """More frames than the 2 GiB of device frames hold (36 frames of 4096^2):
+    the slots are reused round robin, each only after its copy finished."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import orbit_camera
+    ht, dt = tree64
+    tex = wl.texture32(3)
+    w = h = 4096
+    cams = [orbit_camera(f, 36, w, h, (32, 32, 32), 1.5 * 64 * 3 ** 0.5).gpu_struct() for f in range(36)]
+    bufs = [np.full((h, w), GARBAGE, np.uint32) for _ in cams]
+    dt.render_frames(cams, w, h, tex, bufs)
+    d_tex = torch.from_numpy(tex).cuda()
+    d_frame = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    for i in (0, 1, 31, 32, 35):
+        dt.render_device(cams[i], w, h, d_tex, d_frame)
+        torch.cuda.synchronize()
+        assert np.array_equal(bufs[i], d_frame.cpu().numpy().view(np.uint32)), f"frame {i} differs"
+
+
 def test_host_calls_follow_texture_changes(tree64):
     """The host-buffer call keeps the last texture on the device and uploads
     a new one only when its bytes change: frames drawn with textures A, B, A,

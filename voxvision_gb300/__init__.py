@@ -218,6 +218,19 @@ class DeviceTree:
               "vox_cuda_render")
         return out
 
+    def render_frames(self, cameras, w: int, h: int, texture: np.ndarray, frames=None, stream=None):
+        """vox_cuda_render_frames: one BEST frame per camera into host
+        buffers (numpy arrays, or pinned torch tensors drawn in place)."""
+        cams = (CameraStruct * len(cameras))(*cameras)
+        tex = np.ascontiguousarray(texture, dtype=np.uint8)
+        if frames is None:
+            frames = [np.empty((h, w), np.uint32) for _ in cameras]
+        ptrs = (C.c_void_p * len(frames))(*[f.ctypes.data if isinstance(f, np.ndarray) else f.data_ptr()
+                                             for f in frames])
+        check(lib().vox_cuda_render_frames(self.h, C.byref(cams), len(cameras), w, h, _p(tex), ptrs, stream),
+              "vox_cuda_render_frames")
+        return frames
+
     def render_quality(self, camera: CameraStruct, w: int, h: int, quality: int, texture: np.ndarray,
                        stream=None):
         tex = np.ascontiguousarray(texture, dtype=np.uint8)

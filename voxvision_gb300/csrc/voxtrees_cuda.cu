@@ -22,6 +22,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "flatten.h"
 #include "lights_internal.h"
@@ -986,12 +987,55 @@ struct HostCallState {
     uint8_t *h_tex = nullptr;      // pinned: the bytes d_tex holds (valid if tex_ok)
     uint32_t *h_status = nullptr;  // pinned: the tree's status word read back
     bool tex_ok = false;
+    // vox_cuda_render_frames: device frames the kernels draw into, a stream
+    // copying each finished frame out, and per slot "drawn" / "copied" events
+    uint32_t *d_stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaStream_t copy = nullptr;
+    std::vector<cudaEvent_t> drawn, copied;
+    cudaEvent_t fin = nullptr;
     ~HostCallState()               // at thread exit; errors after the CUDA context is gone are moot
     {
         if (d_tex) cudaFree(d_tex);
         if (h_tex) cudaFreeHost(h_tex);
+        if (d_stage) cudaFree(d_stage);
+        for (cudaEvent_t e : drawn) cudaEventDestroy(e);
+        for (cudaEvent_t e : copied) cudaEventDestroy(e);
+        if (fin) cudaEventDestroy(fin);
+        if (copy) cudaStreamDestroy(copy);
     }
 };
+
+// Staging frames and events for `slots` frames of `bytes` each (grow only).
+static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots)
+{
+    cudaError_t e = cudaSuccess;
+    if (!hc->copy) e = cudaStreamCreateWithFlags(&hc->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !hc->fin) e = cudaEventCreateWithFlags(&hc->fin, cudaEventDisableTiming);
+    while (e == cudaSuccess && hc->drawn.size() < slots) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            if (a) cudaEventDestroy(a);
+            break;
+        }
+        hc->drawn.push_back(a);
+        hc->copied.push_back(b);
+    }
+    if (e == cudaSuccess && hc->stage_bytes < bytes) {
+        if (hc->d_stage) {
+            cudaDeviceSynchronize();   // an earlier call's copies may still read the old frames
+            cudaFree(hc->d_stage);
+            hc->d_stage = nullptr;
+            hc->stage_bytes = 0;
+        }
+        e = cudaMalloc(&hc->d_stage, bytes);
+        if (e == cudaSuccess) hc->stage_bytes = bytes;
+        else hc->d_stage = nullptr;
+    }
+    return e;
+}
 
 static HostCallState *host_call_state()
 {
@@ -1066,6 +1110,48 @@ EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     cudaError_t e = host_call_texture(hc, tex, s);
     if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, hc->d_tex, d_argb, nullptr, s);
     if (e == cudaSuccess && !in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+    return host_call_finish(hc, t, s, e);
+}
+
+// Host-buffer frames of one tree: the texture copied in once; each frame
+// drawn into a device frame by kernels enqueued back to back (so that frames
+// overlap as device frames do) and copied out on a second stream as soon as it
+// is drawn; one synchronisation at the end.  Up to STAGE_BYTES of device
+// frames are used, reused round robin beyond that.
+static constexpr size_t STAGE_BYTES = size_t(2) << 30;
+
+EXPORT int vox_cuda_render_frames(const vox_cuda_tree *t, const vox_cuda_camera *cams, uint32_t n, uint32_t w,
+                                  uint32_t h, const uint8_t *tex, uint32_t *const *frames, void *stream)
+{
+    if (!t || (n && (!cams || !frames))) return VOX_CUDA_EINVAL;
+    if (n == 0) return VOX_CUDA_OK;
+    for (uint32_t i = 0; i < n; i++) {
+        int rc = check_render_args(t, &cams[i], w, h, tex, frames[i]);
+        if (rc) return rc;
+    }
+    cudaStream_t s = as_stream(stream);
+    size_t npx = (size_t)w * h, fb = npx * 4;
+    uint32_t slots = (uint32_t)std::min<size_t>(n, std::max<size_t>(1, STAGE_BYTES / fb));
+    HostCallState *hc = host_call_state();
+    if (!hc) return VOX_CUDA_ENOMEM;
+    cudaError_t e = stage_reserve(hc, slots * fb, slots);
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? VOX_CUDA_ENOMEM : VOX_CUDA_ECUDA;
+    hc->tex_ok = false;   // copied in by every call: the texture is an input of the frames
+    e = host_call_texture(hc, tex, s);
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
+        uint32_t b = i % slots;
+        uint32_t *d_argb = hc->d_stage + (size_t)b * npx;
+        if (i >= slots) e = cudaStreamWaitEvent(s, hc->copied[b], 0);   // slot copied out
+        if (e == cudaSuccess) e = launch_render<false>(t, cams[i], w, h, hc->d_tex, d_argb, nullptr, s, true);
+        if (e == cudaSuccess) e = cudaEventRecord(hc->drawn[b], s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(hc->copy, hc->drawn[b], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(frames[i], d_argb, fb, cudaMemcpyDeviceToHost, hc->copy);
+        if (e == cudaSuccess) e = cudaEventRecord(hc->copied[b], hc->copy);
+    }
+    // the call's stream waits for every copy enqueued, so its synchronisation covers them
+    cudaError_t e2 = cudaEventRecord(hc->fin, hc->copy);
+    if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, hc->fin, 0);
+    if (e == cudaSuccess) e = e2;
     return host_call_finish(hc, t, s, e);
 }
 
