@@ -78,6 +78,24 @@ def parse_args():
     return p.parse_args()
 
 
+def max_over_ranks(values, device="cpu"):
+    """Element-wise maximum of `values` over the ranks of the default process
+    group (a job takes its slowest rank's time); unchanged without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` replicas that each processed
+    `units_per_rank` units in `seconds` (the slowest rank's time)."""
+    return world * units_per_rank / seconds
+
+
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -601,12 +619,8 @@ def run_ours(args):
         b.record(stream)
         b.synchronize()
         alone.append(a.elapsed_time(b))
-    total_s = sum(step_ms) * 1e-3
-    if world > 1:
-        t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * rays_step * args.steps / total_s / 1e6
+    total_s = max_over_ranks([sum(step_ms) * 1e-3], "cuda")[0]
+    value = job_rate(rays_step * args.steps, world, total_s) / 1e6
 
     # e2e: the orbit through the host-buffer entry point vox_cuda_render_frames:
     # every step copies the host texture in and delivers all nf frames into
@@ -641,16 +655,13 @@ def run_ours(args):
                 raise vg.VoxCudaError(rc, "vox_cuda_render")
     torch.cuda.synchronize()
     single_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s, single_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s, single_s = float(t[0].item()), float(t[1].item())
-    e2e = {"value": world * rays_step * args.steps / e2e_s / 1e6, "unit": "Mrays/s",
+    e2e_s, single_s = max_over_ranks([e2e_s, single_s], "cuda")
+    e2e = {"value": job_rate(rays_step * args.steps, world, e2e_s) / 1e6, "unit": "Mrays/s",
            "h2d_bytes_per_step": 32768 + nf * C.sizeof(vg.CameraStruct), "d2h_bytes_per_step": nf * W * H * 4,
            "call": "vox_cuda_render_frames (host texture and cameras in; each frame drawn on the device and "
                    "copied into its own page-locked host buffer on a second stream while the next frames are "
                    "drawn; returns when all are in host memory)",
-           "per_call_value": world * rays_step * args.steps / single_s / 1e6,
+           "per_call_value": job_rate(rays_step * args.steps, world, single_s) / 1e6,
            "per_call": "vox_cuda_render, one synchronous call per frame (same frames, one host frame)"}
     del host_frames
 
