@@ -9,12 +9,13 @@ simple-camera, fov 1.0 (90 degrees), orbit radius 1.5 x the bounding-box
 diagonal (665.1) at 20 degrees elevation around (128, 128, 128); texture
 32^3 u8 from splitmix64 seed 7.
 
-  value  device throughput: 120 vox_cuda_render_device launches per step,
-         back to back on one stream, tree, texture and frame resident in HBM,
-         timed with one pair of CUDA events per step on the launching stream
-         (an event between launches would end the overlap of consecutive
-         frame kernels); L2 flushed (256 MiB write) between steps, outside
-         the timed events.
+  value  device throughput: the 120-frame orbit as one vox_cuda_batch of
+         120 jobs (one persistent batch kernel launch from a CUDA graph per
+         step, configuration autotuned once before timing), tree, texture and
+         the 120 frames resident in HBM, timed with a pair of CUDA events per
+         step on the launching stream; L2 flushed (256 MiB write) between
+         steps, outside the timed events.  roofline.plain gives the same
+         orbit as 120 vox_cuda_render_device launches back to back.
   e2e    the same orbit through the host-buffer call vox_cuda_render_frames:
          every step copies the texture and cameras in and delivers each
          8.3 MB frame into its own page-locked host buffer (copied out while
@@ -72,6 +73,10 @@ def parse_args():
                    help="skip the incoherent-query and batched-frame measurements")
     p.add_argument("--frames", type=int, default=NFRAMES,
                    help="orbit frames per step (profiling runs only; the benchmark uses 120)")
+    p.add_argument("--batch-config", default=None, metavar="TW,TH,GRAB,BPS",
+                   help="batch kernel configuration instead of autotuning (profiling runs)")
+    p.add_argument("--kernels-only", action="store_true",
+                   help="time only the batched orbit (no plain launches, e2e or extras; profiling runs)")
     p.add_argument("--tree-build", type=int, default=0, metavar="N",
                    help="only time the device tree build of the N^3 noise volume (profiling runs)")
     p.add_argument("--reps", type=int, default=5, help="timed repetitions of --tree-build")
@@ -575,7 +580,21 @@ def run_ours(args):
     tex_p, frame_p = C.c_void_p(d_tex.data_ptr()), C.c_void_p(frame.data_ptr())
     cam_refs = [C.byref(c) for c in cams]
 
+    # the orbit as one batch: nf frames into their own device frames, drawn by
+    # the persistent batch kernel (warp tiles of every frame from one work
+    # queue), replayed from a CUDA graph; tuned once, untimed
+    frames_dev = torch.empty((nf, H * W), dtype=torch.int32, device="cuda")
+    batch = vg.FrameBatch([(dt, cams[i], W, H, d_tex, frames_dev[i]) for i in range(nf)])
+    if args.batch_config:
+        batch.set_config(vg.BatchConfig(*[int(x) for x in args.batch_config.split(",")]))
+        tuned = batch.config()
+    else:
+        tuned, _ = batch.autotune(stream=sp, reps=3)
+
     def step():
+        batch.launch(sp)
+
+    def plain_step():
         for cr in cam_refs:
             rc = fn(dt.h, cr, W, H, tex_p, frame_p, sp)
             if rc:
@@ -608,7 +627,28 @@ def run_ours(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = [evs[0].elapsed_time(evs[1]) for evs in all_evs]
-    launch_ms = [m / nf for m in step_ms]
+    if args.kernels_only:
+        total_s = max_over_ranks([sum(step_ms) * 1e-3], "cuda")[0]
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": job_rate(rays_step * args.steps, world, total_s) / 1e6,
+                              "unit": "Mrays/s", "ms_per_step": sum(step_ms) / len(step_ms),
+                              "batch_config": tuned, "gpu_launches": int(launches), "clocks": clk}), flush=True)
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # the same orbit as nf plain per-frame launches back to back (their kernels
+    # overlap); one event pair per orbit, as an event between launches would
+    # end the overlap
+    plain_ms = []
+    for r in range(args.warmup + args.steps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plain_step()
+        b.record(stream)
+        b.synchronize()
+        if r >= args.warmup:
+            plain_ms.append(a.elapsed_time(b))
     # one frame alone (events on both sides, so no overlap), for reference
     alone = []
     for i in range(0, nf, max(1, nf // 12)):
@@ -670,18 +710,25 @@ def run_ours(args):
         return
 
     peak, peak_kind = measured_peaks()
-    mean_launch_s = float(np.mean(launch_ms)) * 1e-3
-    achieved = traced_bytes_step / nf / mean_launch_s / 1e9
+    mean_launch_s = float(np.mean(step_ms)) * 1e-3
+    achieved = traced_bytes_step / mean_launch_s / 1e9
     traffic = traffic_per_launch()
     l2 = l2_copy_gbs(torch)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s",
-                "traffic": traffic, "kernel": "render_kernel (BEST, fused ray gen + search + colour)",
-                "alg_bytes_per_launch": traced_bytes_step / nf,
-                "alg_bytes_per_launch_every_pixel": alg_bytes_step / nf,
-                "culled_rays_per_launch": culled / nf,
+                "traffic": traffic,
+                "kernel": f"batch_kernel (persistent, {nf} BEST frames a launch, fused ray gen + search + colour)",
+                "batch_config": tuned,
+                "alg_bytes_per_launch": traced_bytes_step,
+                "alg_bytes_per_launch_every_pixel": alg_bytes_step,
+                "culled_rays_per_launch": culled,
                 "mean_launch_ms": mean_launch_s * 1e3,
+                "ms_per_frame": mean_launch_s * 1e3 / nf,
+                "plain": {"value": job_rate(rays_step, world, float(np.mean(plain_ms)) * 1e-3) / 1e6,
+                          "ms_per_frame": float(np.mean(plain_ms)) / nf,
+                          "kernel": "render_kernel, one vox_cuda_render_device launch per frame, consecutive "
+                                    "launches overlapping"},
                 "launch_alone_ms": float(np.median(alone)),
                 "bytes_per_ray": traced_bytes_step / rays_step,
                 "visits_per_ray": {"nodes": nodes / rays_step, "inner": inner / rays_step,

@@ -72,11 +72,62 @@ __device__ __forceinline__ uint32_t find_job(const uint32_t *base, uint32_t njob
     return lo;
 }
 
+// One tile of TW x TH pixels of frame J (its `local`-th tile, taken outward
+// from where the tree's centre projects): ray, search, colour, store.
+template <int CAP, int TW, int TH>
+__device__ __forceinline__ void run_tile(const BatchJobDev &J, uint32_t local, uint32_t lane)
+{
+    constexpr int RPT = TW * TH / 32;   // rays per thread per tile
+    uint32_t ty = vox::centre_out(local / J.ntx, J.cty, J.nty);
+    uint32_t tx = vox::centre_out(local % J.ntx, J.ctx, J.ntx);
+    const DevTree t = J.tree;
+    const vox_cuda_camera cam = J.cam;
+    const uint32_t w = J.w, x1 = J.x1, y1 = J.y1;
+#pragma unroll 1
+    for (int r = 0; r < RPT; r++) {
+        uint32_t p = lane + 32u * (uint32_t)r;
+        uint32_t px = J.x0 + tx * TW + p % TW, py = J.y0 + ty * TH + p / TW;
+        if (px < x1 && py < y1) {
+            float dx, dy, dz;
+            vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
+            RayHit hh;
+            vox::Counts c{0, 0, 0};
+            bool overflow = false, hit = false;
+            if (t.root != VOXP_EMPTY)
+                hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1], cam.position[2], dx,
+                                                 dy, dz, hh, c, overflow);
+            J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
+            if (overflow) atomicOr(J.status, 1u);
+        }
+    }
+}
+
+// The `c`-th clearing item of frame J: CLEAR_ROWS rows, the parts outside
+// the traced rectangle.
+__device__ __forceinline__ void run_clear(const BatchJobDev &J, uint32_t c, uint32_t lane)
+{
+    const uint32_t w = J.w, y0r = c * CLEAR_ROWS;
+    const uint32_t yend = min(y0r + CLEAR_ROWS, J.h);
+    const bool vec = (reinterpret_cast<uintptr_t>(J.argb) & 15u) == 0;
+    for (uint32_t y = y0r; y < yend; y++) {
+        uint32_t *row = J.argb + (size_t)y * w;
+        uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
+        if (y >= J.y0 && y < J.y1) { b0 = J.x0; a1 = J.x1; b1 = w; }
+        if (vec) {
+            uint4 *r4 = reinterpret_cast<uint4 *>(row);
+            for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+            for (uint32_t i = a1 / 4 + lane; i < b1 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+        } else {
+            for (uint32_t i = a0 + lane; i < b0; i += 32) row[i] = 0u;
+            for (uint32_t i = a1 + lane; i < b1; i += 32) row[i] = 0u;
+        }
+    }
+}
+
 template <int CAP, int TW, int TH>
 __global__ void __launch_bounds__(128) batch_kernel(const BatchHead *__restrict__ head, uint32_t grab,
                                                     uint32_t *__restrict__ counter)
 {
-    constexpr int RPT = TW * TH / 32;   // rays per thread per tile
     __shared__ uint32_t tbase[MAX_JOBS], cbase[MAX_JOBS];
     const BatchJobDev *jobs = reinterpret_cast<const BatchJobDev *>(head + 1);
     const uint32_t njobs = head->njobs, ntiles = head->total_tiles, total = ntiles + head->total_clear;
@@ -95,48 +146,52 @@ __global__ void __launch_bounds__(128) batch_kernel(const BatchHead *__restrict_
         for (uint32_t item = t0; item < t1; item++) {
             if (item < ntiles) {
                 const BatchJobDev &J = jobs[find_job(tbase, njobs, item)];
-                uint32_t local = item - J.tile_base;
-                uint32_t ty = vox::centre_out(local / J.ntx, J.cty, J.nty);
-                uint32_t tx = vox::centre_out(local % J.ntx, J.ctx, J.ntx);
-                const DevTree t = J.tree;
-                const vox_cuda_camera cam = J.cam;
-                const uint32_t w = J.w, x1 = J.x1, y1 = J.y1;
-#pragma unroll 1
-                for (int r = 0; r < RPT; r++) {
-                    uint32_t p = lane + 32u * (uint32_t)r;
-                    uint32_t px = J.x0 + tx * TW + p % TW, py = J.y0 + ty * TH + p / TW;
-                    if (px < x1 && py < y1) {
-                        float dx, dy, dz;
-                        vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
-                        RayHit hh;
-                        vox::Counts c{0, 0, 0};
-                        bool overflow = false, hit = false;
-                        if (t.root != VOXP_EMPTY)
-                            hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1],
-                                                             cam.position[2], dx, dy, dz, hh, c, overflow);
-                        J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
-                        if (overflow) atomicOr(J.status, 1u);
-                    }
-                }
+                run_tile<CAP, TW, TH>(J, item - J.tile_base, lane);
             } else {
-                // clearing item: CLEAR_ROWS rows, the parts outside the rectangle
                 uint32_t c = item - ntiles;
                 const BatchJobDev &J = jobs[find_job(cbase, njobs, c)];
-                const uint32_t w = J.w, y0r = (c - J.clear_base) * CLEAR_ROWS;
-                const uint32_t yend = min(y0r + CLEAR_ROWS, J.h);
-                const bool vec = (reinterpret_cast<uintptr_t>(J.argb) & 15u) == 0;
-                for (uint32_t y = y0r; y < yend; y++) {
-                    uint32_t *row = J.argb + (size_t)y * w;
-                    uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
-                    if (y >= J.y0 && y < J.y1) { b0 = J.x0; a1 = J.x1; b1 = w; }
-                    if (vec) {
-                        uint4 *r4 = reinterpret_cast<uint4 *>(row);
-                        for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
-                        for (uint32_t i = a1 / 4 + lane; i < b1 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
-                    } else {
-                        for (uint32_t i = a0 + lane; i < b0; i += 32) row[i] = 0u;
-                        for (uint32_t i = a1 + lane; i < b1; i += 32) row[i] = 0u;
-                    }
+                run_clear(J, c - J.clear_base, lane);
+            }
+        }
+    }
+}
+
+// Frames handed out one after another (each frame's tiles, then its clearing
+// items, in one queue), each announced when complete: the warp that finishes
+// a frame's last item stores `epoch` into flags[job] in host memory, after
+// every store of the frame is visible device-wide (the copy engine may read
+// the frame as soon as the host sees the flag).  done[] counts finished items
+// per frame and starts at zero.
+template <int CAP, int TW, int TH>
+__global__ void __launch_bounds__(128) frames_kernel(const BatchHead *__restrict__ head, uint32_t grab,
+                                                     uint32_t *__restrict__ counter, uint32_t *__restrict__ done,
+                                                     uint32_t *flags, uint32_t epoch)
+{
+    __shared__ uint32_t base[MAX_JOBS];
+    const BatchJobDev *jobs = reinterpret_cast<const BatchJobDev *>(head + 1);
+    const uint32_t njobs = head->njobs, total = head->total_tiles;
+    for (uint32_t i = threadIdx.x; i < njobs; i += blockDim.x) base[i] = jobs[i].tile_base;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = atomicAdd(counter, grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= total) break;
+        uint32_t t1 = min(t0 + grab, total);
+        for (uint32_t item = t0; item < t1; item++) {
+            uint32_t j = find_job(base, njobs, item);
+            const BatchJobDev &J = jobs[j];
+            uint32_t local = item - J.tile_base, ntile = J.ntx * J.nty;
+            if (local < ntile) run_tile<CAP, TW, TH>(J, local, lane);
+            else run_clear(J, local - ntile, lane);
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();   // this warp's stores (ordered before by the warp barrier), then the count
+                uint32_t items = (j + 1 < njobs ? base[j + 1] : total) - J.tile_base;
+                if (atomicAdd(&done[j], 1u) + 1u == items) {
+                    __threadfence_system();
+                    *(volatile uint32_t *)&flags[j] = epoch;
                 }
             }
         }
@@ -569,8 +624,42 @@ EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32
 
 size_t frame_job_table_bytes(uint32_t njobs) { return table_bytes(njobs); }
 
+int enqueue_announced_frames(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
+                             uint32_t *d_counter, uint32_t *d_done, uint32_t *flags, uint32_t epoch, int nsm,
+                             cudaStream_t s)
+{
+    if (njobs == 0 || njobs > MAX_JOBS) return VOX_CUDA_EINVAL;
+    BatchHead *head = static_cast<BatchHead *>(h_table);
+    BatchJobDev *table = reinterpret_cast<BatchJobDev *>(head + 1);
+    *head = BatchHead{njobs, 0u, 0u, 0u};
+    uint32_t items = 0;
+    int cap = 0;
+    for (uint32_t q = 0; q < njobs; q++) {
+        BatchHead h{0u, 0u, 0u, 0u};
+        fill_job(table[q], jobs[q], 8, 4, h);
+        table[q].tile_base = items;   // this frame's tiles, then its clearing items
+        table[q].clear_base = items + h.total_tiles;
+        items += h.total_tiles + h.total_clear;
+        cap = std::max(cap, jobs[q].tree->cap_class);
+    }
+    head->total_tiles = items;
+    if (cudaMemcpyAsync(d_table, h_table, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s) != cudaSuccess ||
+        cudaMemsetAsync(d_done, 0, njobs * sizeof(uint32_t), s) != cudaSuccess)
+        return VOX_CUDA_ECUDA;
+    const BatchHead *dt = static_cast<const BatchHead *>(d_table);
+    dim3 grid(nsm * 8), block(128);
+    switch (cap) {
+    case 0: frames_kernel<CAP0, 8, 4><<<grid, block, 0, s>>>(dt, 2, d_counter, d_done, flags, epoch); break;
+    case 1: frames_kernel<CAP1, 8, 4><<<grid, block, 0, s>>>(dt, 2, d_counter, d_done, flags, epoch); break;
+    default: frames_kernel<CAP2, 8, 4><<<grid, block, 0, s>>>(dt, 2, d_counter, d_done, flags, epoch); break;
+    }
+    count_launch();
+    return status_of(cudaGetLastError());
+}
+
 int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
-                       uint32_t *d_counter, int nsm, cudaStream_t s)
+                       uint32_t *d_counter, int nsm, cudaStream_t s, const vox_cuda_batch_config *cfg)
 {
     if (njobs == 0 || njobs > MAX_JOBS) return VOX_CUDA_EINVAL;
     BatchHead *head = static_cast<BatchHead *>(h_table);
@@ -584,7 +673,7 @@ int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_t
     if (cudaMemcpyAsync(d_table, h_table, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s) != cudaSuccess)
         return VOX_CUDA_ECUDA;
-    vox_cuda_batch_config c{8, 4, 2, 4};
+    vox_cuda_batch_config c = cfg ? *cfg : vox_cuda_batch_config{8, 4, 2, 4};
     const BatchHead *dt = static_cast<const BatchHead *>(d_table);
     cudaError_t e;
     switch (cap) {

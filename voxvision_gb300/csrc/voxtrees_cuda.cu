@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -991,6 +992,15 @@ struct HostCallState {
     // copying each finished frame out, and per slot "drawn" / "copied" events
     uint32_t *d_stage = nullptr;
     size_t stage_bytes = 0;
+    unsigned char *h_tables = nullptr;   // pinned: one job table per chunk of frames
+    size_t tables_bytes = 0;
+    void *d_table = nullptr;             // device: the job table of the chunk being drawn, its queue head
+    size_t d_table_bytes = 0;
+    uint32_t *d_done = nullptr;          // device: finished items per frame of a launch
+    uint32_t *h_flags = nullptr;         // pinned: per frame of a launch, the epoch once complete
+    uint32_t *d_flags = nullptr;         // the device's address of h_flags
+    size_t flags_n = 0;
+    uint32_t epoch = 0;
     cudaStream_t copy = nullptr;
     std::vector<cudaEvent_t> drawn, copied;
     cudaEvent_t fin = nullptr;
@@ -999,6 +1009,10 @@ struct HostCallState {
         if (d_tex) cudaFree(d_tex);
         if (h_tex) cudaFreeHost(h_tex);
         if (d_stage) cudaFree(d_stage);
+        if (h_tables) cudaFreeHost(h_tables);
+        if (d_table) cudaFree(d_table);
+        if (d_done) cudaFree(d_done);
+        if (h_flags) cudaFreeHost(h_flags);
         for (cudaEvent_t e : drawn) cudaEventDestroy(e);
         for (cudaEvent_t e : copied) cudaEventDestroy(e);
         if (fin) cudaEventDestroy(fin);
@@ -1006,10 +1020,38 @@ struct HostCallState {
     }
 };
 
-// Staging frames and events for `slots` frames of `bytes` each (grow only).
-static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots)
+// Staging frames (`bytes` for `slots` frames), `tables` bytes of pinned job
+// tables, a device job table of `table` bytes, and completion counters and
+// flags for `group` frames (grow only).
+static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots, size_t tables, size_t table,
+                                 uint32_t group)
 {
     cudaError_t e = cudaSuccess;
+    if (hc->flags_n < group) {
+        if (hc->d_done || hc->h_flags) cudaDeviceSynchronize();
+        if (hc->d_done) cudaFree(hc->d_done);
+        if (hc->h_flags) cudaFreeHost(hc->h_flags);
+        hc->d_done = nullptr;
+        hc->h_flags = hc->d_flags = nullptr;
+        hc->flags_n = 0;
+        void *hp = nullptr, *dp = nullptr;
+        e = cudaMalloc(&hc->d_done, group * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMallocHost(&hp, group * sizeof(uint32_t));
+        if (e == cudaSuccess) {
+            std::memset(hp, 0, group * sizeof(uint32_t));
+            e = cudaHostGetDevicePointer(&dp, hp, 0);
+        }
+        if (e == cudaSuccess) {
+            hc->h_flags = static_cast<uint32_t *>(hp);
+            hc->d_flags = static_cast<uint32_t *>(dp);
+            hc->flags_n = group;
+        } else {
+            if (hc->d_done) cudaFree(hc->d_done);
+            if (hp) cudaFreeHost(hp);
+            hc->d_done = nullptr;
+            return e;
+        }
+    }
     if (!hc->copy) e = cudaStreamCreateWithFlags(&hc->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess && !hc->fin) e = cudaEventCreateWithFlags(&hc->fin, cudaEventDisableTiming);
     while (e == cudaSuccess && hc->drawn.size() < slots) {
@@ -1022,6 +1064,28 @@ static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots
         }
         hc->drawn.push_back(a);
         hc->copied.push_back(b);
+    }
+    if (e == cudaSuccess && hc->tables_bytes < tables) {
+        if (hc->h_tables) {
+            cudaDeviceSynchronize();
+            cudaFreeHost(hc->h_tables);
+            hc->h_tables = nullptr;
+            hc->tables_bytes = 0;
+        }
+        e = cudaMallocHost(&hc->h_tables, tables);
+        if (e == cudaSuccess) hc->tables_bytes = tables;
+        else hc->h_tables = nullptr;
+    }
+    if (e == cudaSuccess && hc->d_table_bytes < table + 256) {
+        if (hc->d_table) {
+            cudaDeviceSynchronize();
+            cudaFree(hc->d_table);
+            hc->d_table = nullptr;
+            hc->d_table_bytes = 0;
+        }
+        e = cudaMalloc(&hc->d_table, table + 256);
+        if (e == cudaSuccess) hc->d_table_bytes = table + 256;
+        else hc->d_table = nullptr;
     }
     if (e == cudaSuccess && hc->stage_bytes < bytes) {
         if (hc->d_stage) {
@@ -1113,12 +1177,31 @@ EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     return host_call_finish(hc, t, s, e);
 }
 
-// Host-buffer frames of one tree: the texture copied in once; each frame
-// drawn into a device frame by kernels enqueued back to back (so that frames
-// overlap as device frames do) and copied out on a second stream as soon as it
-// is drawn; one synchronisation at the end.  Up to STAGE_BYTES of device
-// frames are used, reused round robin beyond that.
+// Host-buffer frames of one tree: the texture copied in once; all frames
+// drawn by one persistent launch into device frames, one after another, each
+// announced when complete; the calling thread waits for each announcement and
+// has the frame copied out on a second stream at once, while later frames are
+// still drawn; one synchronisation at the end.  Up to STAGE_BYTES of device
+// frames (at most 1024 frames) go into one launch; beyond that, launches
+// follow one another, reusing the device frames once copied out.
 static constexpr size_t STAGE_BYTES = size_t(2) << 30;
+static constexpr uint32_t LAUNCH_FRAMES = 1024;
+
+// Waits for flags[j] == epoch; gives up when the stream holding the launch
+// has finished or failed without it, or after `limit_s` seconds.
+static int wait_announced(const volatile uint32_t *flag, uint32_t epoch, cudaStream_t s, double limit_s)
+{
+    auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t spin = 0;; spin++) {
+        if (*flag == epoch) return VOX_CUDA_OK;
+        if ((spin & 1023u) == 1023u) {
+            cudaError_t q = cudaStreamQuery(s);
+            if (q != cudaErrorNotReady) return *flag == epoch ? VOX_CUDA_OK : VOX_CUDA_ECUDA;
+            if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > limit_s)
+                return VOX_CUDA_ETIMEOUT;
+        }
+    }
+}
 
 EXPORT int vox_cuda_render_frames(const vox_cuda_tree *t, const vox_cuda_camera *cams, uint32_t n, uint32_t w,
                                   uint32_t h, const uint8_t *tex, uint32_t *const *frames, void *stream)
@@ -1129,30 +1212,48 @@ EXPORT int vox_cuda_render_frames(const vox_cuda_tree *t, const vox_cuda_camera 
         int rc = check_render_args(t, &cams[i], w, h, tex, frames[i]);
         if (rc) return rc;
     }
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return VOX_CUDA_ENODEV;
     cudaStream_t s = as_stream(stream);
     size_t npx = (size_t)w * h, fb = npx * 4;
     uint32_t slots = (uint32_t)std::min<size_t>(n, std::max<size_t>(1, STAGE_BYTES / fb));
+    uint32_t group = std::min(slots, LAUNCH_FRAMES), ngroups = (n + group - 1) / group;
+    size_t tb = align256(frame_job_table_bytes(group));
     HostCallState *hc = host_call_state();
     if (!hc) return VOX_CUDA_ENOMEM;
-    cudaError_t e = stage_reserve(hc, slots * fb, slots);
+    cudaError_t e = stage_reserve(hc, slots * fb, slots, ngroups * tb, tb, group);
     if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? VOX_CUDA_ENOMEM : VOX_CUDA_ECUDA;
+    uint32_t *d_counter = reinterpret_cast<uint32_t *>(static_cast<unsigned char *>(hc->d_table) + tb);
     hc->tex_ok = false;   // copied in by every call: the texture is an input of the frames
     e = host_call_texture(hc, tex, s);
-    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
-        uint32_t b = i % slots;
-        uint32_t *d_argb = hc->d_stage + (size_t)b * npx;
-        if (i >= slots) e = cudaStreamWaitEvent(s, hc->copied[b], 0);   // slot copied out
-        if (e == cudaSuccess) e = launch_render<false>(t, cams[i], w, h, hc->d_tex, d_argb, nullptr, s, true);
-        if (e == cudaSuccess) e = cudaEventRecord(hc->drawn[b], s);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(hc->copy, hc->drawn[b], 0);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(frames[i], d_argb, fb, cudaMemcpyDeviceToHost, hc->copy);
-        if (e == cudaSuccess) e = cudaEventRecord(hc->copied[b], hc->copy);
+    int rc = VOX_CUDA_OK;
+    std::vector<vox_cuda_frame_job> jobs(group);
+    for (uint32_t g = 0; g < ngroups && e == cudaSuccess && rc == VOX_CUDA_OK; g++) {
+        uint32_t a = g * group, cnt = std::min(group, n - a), epoch = ++hc->epoch;
+        for (uint32_t j = 0; j < cnt && e == cudaSuccess; j++) {
+            uint32_t i = a + j, b = i % slots;
+            if (i >= slots) e = cudaStreamWaitEvent(s, hc->copied[b], 0);   // device frame copied out
+            jobs[j] = vox_cuda_frame_job{t, cams[i], w, h, hc->d_tex, hc->d_stage + (size_t)b * npx};
+        }
+        if (e != cudaSuccess) break;
+        rc = enqueue_announced_frames(jobs.data(), cnt, hc->h_tables + (size_t)g * tb, hc->d_table, d_counter,
+                                      hc->d_done, hc->d_flags, epoch, nsm, s);
+        for (uint32_t j = 0; j < cnt && rc == VOX_CUDA_OK && e == cudaSuccess; j++) {
+            uint32_t i = a + j, b = i % slots;
+            rc = wait_announced(hc->h_flags + j, epoch, s, 60.0);
+            if (rc) break;
+            e = cudaMemcpyAsync(frames[i], hc->d_stage + (size_t)b * npx, fb, cudaMemcpyDeviceToHost, hc->copy);
+            if (e == cudaSuccess) e = cudaEventRecord(hc->copied[b], hc->copy);
+        }
     }
     // the call's stream waits for every copy enqueued, so its synchronisation covers them
     cudaError_t e2 = cudaEventRecord(hc->fin, hc->copy);
     if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(s, hc->fin, 0);
     if (e == cudaSuccess) e = e2;
-    return host_call_finish(hc, t, s, e);
+    int rf = host_call_finish(hc, t, s, e);
+    return rc ? rc : rf;
 }
 
 EXPORT int vox_cuda_render_counts_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
