@@ -59,7 +59,7 @@ CENTRE = (128.0, 128.0, 128.0)
 RADIUS = 1.5 * 256 * math.sqrt(3.0)
 METRIC = "Mrays/s at 1080p on 256^3"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
-TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "render_best_1080p_256.md")
+TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "batch_orbit_1080p_256.md")
 
 
 def parse_args():

@@ -190,12 +190,14 @@ int vox_cuda_render(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
                     void *stream);
 /* n BEST frames of one tree, camera cams[i] into the host buffer frames[i]
  * (w*h ARGB each), with `tex` copied in once: what n calls of
- * vox_cuda_render give, but the frames overlap on the GPU as device frames
- * enqueued back to back do, and each is copied out on a second stream while
- * the next ones are drawn (page-locked frames: the copies run asynchronously;
- * pageable ones hold the calling thread for their copy).  Device frames of up
- * to 2 GiB per call are kept per thread for later calls.  Returns when all n
- * frames are in host memory; VOX_CUDA_ESTACK if any search overflowed. */
+ * vox_cuda_render give, drawn by one persistent launch (up to 1024 frames
+ * and 2 GiB of device frames a launch) and each copied out on a second
+ * stream as soon as it is complete, while the rest are drawn; the calling
+ * thread waits for each frame's completion (page-locked frames: the copies
+ * run asynchronously; pageable ones hold the thread for their copy).  The
+ * device frames are kept per thread for later calls.  Returns when all n
+ * frames are in host memory; VOX_CUDA_ESTACK if any search overflowed,
+ * VOX_CUDA_ETIMEOUT if a frame was not complete within 60 s. */
 int vox_cuda_render_frames(const vox_cuda_tree *tree, const vox_cuda_camera *cams, uint32_t n, uint32_t w,
                            uint32_t h, const uint8_t *texture, uint32_t *const *frames, void *stream);
 int vox_cuda_render_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
