@@ -124,8 +124,16 @@ __device__ __forceinline__ void run_clear(const BatchJobDev &J, uint32_t c, uint
     }
 }
 
+// Register bound of the persistent kernels: 8 resident blocks of 128 threads
+// per SM (64 registers, a few bytes spilled).  On the 120-frame 1080p orbit
+// this draws 12% faster than the unbounded build (68 registers, 7 blocks);
+// 10 and 12 blocks (48 and 40 registers) spill more and draw slower.
+#ifndef BATCH_MIN_BLOCKS
+#define BATCH_MIN_BLOCKS 8
+#endif
+
 template <int CAP, int TW, int TH>
-__global__ void __launch_bounds__(128) batch_kernel(const BatchHead *__restrict__ head, uint32_t grab,
+__global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) batch_kernel(const BatchHead *__restrict__ head, uint32_t grab,
                                                     uint32_t *__restrict__ counter)
 {
     __shared__ uint32_t tbase[MAX_JOBS], cbase[MAX_JOBS];
@@ -163,7 +171,7 @@ __global__ void __launch_bounds__(128) batch_kernel(const BatchHead *__restrict_
 // the frame as soon as the host sees the flag).  done[] counts finished items
 // per frame and starts at zero.
 template <int CAP, int TW, int TH>
-__global__ void __launch_bounds__(128) frames_kernel(const BatchHead *__restrict__ head, uint32_t grab,
+__global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const BatchHead *__restrict__ head, uint32_t grab,
                                                      uint32_t *__restrict__ counter, uint32_t *__restrict__ done,
                                                      uint32_t *flags, uint32_t epoch)
 {
