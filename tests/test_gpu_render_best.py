@@ -228,6 +228,23 @@ def test_host_frames_call_reuses_device_frames(tree64):
         assert np.array_equal(bufs[i], d_frame.cpu().numpy().view(np.uint32)), f"frame {i} differs"
 
 
+def test_host_frames_call_many_small_frames_and_empty_tree(tree64):
+    """1100 small frames (more than one launch holds) equal the single-frame
+    call's; an empty tree gives all-zero frames."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import orbit_camera
+    ht, dt = tree64
+    tex = wl.texture32(5)
+    w, h = 32, 16
+    cams = [orbit_camera(f, 1100, w, h, (32, 32, 32), 1.5 * 64 * 3 ** 0.5).gpu_struct() for f in range(1100)]
+    bufs = dt.render_frames(cams, w, h, tex)
+    for i in (0, 1, 511, 1023, 1024, 1099):
+        assert np.array_equal(bufs[i], dt.render(cams[i], w, h, tex)), f"frame {i} differs"
+    empty = vg().DeviceTree(None)
+    zs = empty.render_frames(cams[:5], w, h, tex, [np.full((h, w), GARBAGE, np.uint32) for _ in range(5)])
+    assert all(not z.any() for z in zs)
+
+
 def test_host_calls_follow_texture_changes(tree64):
     """The host-buffer call keeps the last texture on the device and uploads
     a new one only when its bytes change: frames drawn with textures A, B, A,
