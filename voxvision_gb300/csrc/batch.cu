@@ -681,7 +681,7 @@ int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_t
     if (cudaMemcpyAsync(d_table, h_table, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s) != cudaSuccess)
         return VOX_CUDA_ECUDA;
-    vox_cuda_batch_config c = cfg ? *cfg : vox_cuda_batch_config{8, 4, 2, 4};
+    vox_cuda_batch_config c = cfg ? *cfg : vox_cuda_batch_config{8, 4, 1, 8};
     const BatchHead *dt = static_cast<const BatchHead *>(d_table);
     cudaError_t e;
     switch (cap) {

@@ -114,8 +114,8 @@ void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, 
 /* The batched frame kernel over a job table the caller allocated for one
  * launch (batch.cu): fills h_table (pinned, frame_job_table_bytes(njobs)
  * bytes, 16-byte aligned), copies it to d_table, zeroes *d_counter and
- * launches, all on s, with `cfg` (tiles 8x4, 2 a grab, 4 blocks per SM when
- * NULL). */
+ * launches, all on s, with `cfg` (tiles 8x4, 1 a grab, 8 blocks per SM --
+ * what the autotuner picks for a mix of frames -- when NULL). */
 size_t frame_job_table_bytes(uint32_t njobs);
 int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
                        uint32_t *d_counter, int nsm, cudaStream_t s, const vox_cuda_batch_config *cfg = nullptr);
