@@ -159,7 +159,10 @@ int vox_cuda_tree_node_id(const vox_cuda_tree *tree, const struct vox_node *node
  * (n x 3, written only on a hit, like `res`).  roots: NULL to start every
  * ray at the tree's root, else n pre-order indices of the node each search
  * starts from (vox_ray_tree_intersection accepts any node as its root;
- * renderer.c:297).  slot and points may be NULL.
+ * renderer.c:297).  slot and points may be NULL.  Batches of 65,536 rays or
+ * more are traced grouped by direction and origin (results are the same for
+ * any order), with a stream-ordered scratch allocation (cudaMallocAsync) of
+ * about 6 bytes per ray for that order.
  * Replaces vox_ray_tree_intersection (src/voxtrees/search.h:24-26). */
 int vox_cuda_ray_batch(const vox_cuda_tree *tree, const float *origins, const float *dirs,
                        const uint32_t *roots, size_t n, uint32_t *leaf_id, uint8_t *slot,

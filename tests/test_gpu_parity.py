@@ -251,6 +251,28 @@ def test_device_entry_points_on_a_torch_stream(tree256):
     assert same_points(pts.cpu().numpy(), hpts, hleaf != MISS)[0]
 
 
+def test_ray_order_changes_no_result(tree256):
+    """Batches of 2^16 rays or more are traced in coherent order: the same
+    300k rays (half of them leaf-rooted) in one batch and in 2^15-ray batches
+    (traced as given) give identical leaves, slots and points."""
+    from voxvision_gb300 import workloads as wl
+    ht, dt = tree256
+    n = 300_000
+    o, d = wl.incoherent_rays(n, -128.0, 384.0, 91)
+    nodes = dt.info()["nodes"]
+    rng = np.random.default_rng(92)
+    roots = np.where(rng.random(n) < 0.5, rng.integers(0, nodes, n), MISS).astype(np.uint32)
+    leaf, slot, pts = dt.rays(o, d, roots)
+    parts = [dt.rays(o[i:i + 32768], d[i:i + 32768], roots[i:i + 32768]) for i in range(0, n, 32768)]
+    l2 = np.concatenate([p[0] for p in parts])
+    s2 = np.concatenate([p[1] for p in parts])
+    p2 = np.concatenate([p[2] for p in parts])
+    hit = leaf != MISS
+    assert np.array_equal(leaf, l2) and np.array_equal(slot, s2)
+    assert np.array_equal(pts[hit].view(np.uint32), p2[hit].view(np.uint32))
+    assert 0.1 < hit.mean() < 0.9
+
+
 def test_dropin_single_queries_return_reference_nodes():
     """vox_ray_tree_intersection / vox_tree_ball_collidep with the reference's
     signatures return the same host node / boolean as the oracle."""

@@ -120,6 +120,13 @@ size_t frame_job_table_bytes(uint32_t njobs);
 int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
                        uint32_t *d_counter, int nsm, cudaStream_t s, const vox_cuda_batch_config *cfg = nullptr);
 
+/* The coherent order of a ray batch (raysort.cu): *order (in `scratch`, of
+ * ray_order_bytes(n) bytes) lists the rays' indices grouped by direction
+ * octant and origin cell; enqueued on s. */
+size_t ray_order_bytes(size_t n);
+cudaError_t ray_order(const vox_cuda_tree *t, const float *o, const float *d, size_t n, void *scratch,
+                      uint32_t **order, cudaStream_t s);
+
 /* Frames one after another in one persistent launch (batch.cu), each
  * announced when complete: flags[j] (host memory the device can write)
  * becomes `epoch` once every store of frame j is visible to the copy engine.

@@ -1,0 +1,157 @@
+/*
+ * raysort.cu -- the order in which a large ray batch is traced.
+ *
+ * Every ray of a batch is an independent search, so the order in which they
+ * are traced changes no result, only how alike the 32 searches of a warp are.
+ * Rays given in random order (origins anywhere, directions anywhere) put 32
+ * unrelated searches in every warp.  Tracing them grouped by the octant of
+ * their direction, then by the cell of their origin on an 8x8x8 grid around
+ * the tree (Morton order), makes the searches of a warp start close together
+ * and walk the same way: on 16M random rays over the 256^3 tree the ray
+ * kernel takes 2.9 ms instead of 5.4 ms.
+ *
+ * The order is a counting sort on those 12-bit keys: per block of
+ * RAYS_PER_BLOCK rays a histogram in shared memory, the position of each
+ * (key, block) pair from a prefix over blocks and keys, then each ray's slot
+ * in `order`; the search kernel reads the j-th ray of the order from where
+ * it was given and writes its result there.  Rays of one (key, block) pair
+ * land in any order among themselves; that, too, changes no result.
+ * (Copying the rays into order instead makes a 16M-ray batch slower: each
+ * ray's six floats become scattered partial-sector stores.)
+ */
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "internal.h"
+
+namespace {
+
+constexpr int KEY_BITS = 12;
+constexpr uint32_t NKEYS = 1u << KEY_BITS;
+constexpr int SORT_THREADS = 1024;
+constexpr uint32_t RAYS_PER_BLOCK = 65536;
+
+struct KeyFrame {
+    float lo[3], inv[3];   // origin cell = floor((o - lo) * inv), clamped to 0..7
+};
+
+__device__ __forceinline__ uint32_t ray_key(const float *o, const float *d, size_t i, const KeyFrame &f)
+{
+    uint32_t cell[3];
+    for (int a = 0; a < 3; a++) {
+        float q = (o[3 * i + a] - f.lo[a]) * f.inv[a];
+        cell[a] = q >= 7.0f ? 7u : (q > 0.0f ? (uint32_t)q : 0u);   // NaN -> 0
+    }
+    uint32_t m = 0;
+    for (int b = 0; b < 3; b++)
+        for (int a = 0; a < 3; a++) m |= ((cell[a] >> b) & 1u) << (3 * b + a);
+    uint32_t oct = (d[3 * i] < 0.0f) | ((d[3 * i + 1] < 0.0f) << 1) | ((d[3 * i + 2] < 0.0f) << 2);
+    return (oct << 9) | m;
+}
+
+// Keys of a block's rays and the block's histogram (block-major).
+__global__ void __launch_bounds__(SORT_THREADS) k_keys(const float *o, const float *d, size_t n, KeyFrame f,
+                                                        uint16_t *keys, uint32_t *hist)
+{
+    __shared__ uint32_t h[NKEYS];
+    for (uint32_t k = threadIdx.x; k < NKEYS; k += SORT_THREADS) h[k] = 0;
+    __syncthreads();
+    size_t b0 = (size_t)blockIdx.x * RAYS_PER_BLOCK, b1 = b0 + RAYS_PER_BLOCK < n ? b0 + RAYS_PER_BLOCK : n;
+    for (size_t i = b0 + threadIdx.x; i < b1; i += SORT_THREADS) {
+        uint32_t k = ray_key(o, d, i, f);
+        keys[i] = (uint16_t)k;
+        atomicAdd(&h[k], 1u);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < NKEYS; k += SORT_THREADS) hist[(size_t)blockIdx.x * NKEYS + k] = h[k];
+}
+
+// For every key: its count before each block (in place) and its total.
+__global__ void k_key_blocks(uint32_t *hist, uint32_t nblocks, uint32_t *total)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= NKEYS) return;
+    uint32_t run = 0;
+    for (uint32_t b = 0; b < nblocks; b++) {
+        uint32_t c = hist[(size_t)b * NKEYS + k];
+        hist[(size_t)b * NKEYS + k] = run;
+        run += c;
+    }
+    total[k] = run;
+}
+
+// Exclusive scan of the NKEYS totals in place (one block).
+__global__ void __launch_bounds__(1024) k_key_starts(uint32_t *total)
+{
+    __shared__ uint32_t part[1024];
+    constexpr uint32_t PER = NKEYS / 1024;
+    uint32_t v[PER], s = 0;
+    for (uint32_t j = 0; j < PER; j++) {
+        v[j] = total[threadIdx.x * PER + j];
+        s += v[j];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1) {   // inclusive scan of the parts
+        uint32_t x = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += x;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (uint32_t j = 0; j < PER; j++) {
+        total[threadIdx.x * PER + j] = run;
+        run += v[j];
+    }
+}
+
+// Each ray's slot in the traced order.
+__global__ void __launch_bounds__(SORT_THREADS) k_place(const uint16_t *keys, size_t n, const uint32_t *hist,
+                                                         const uint32_t *start, uint32_t *order)
+{
+    __shared__ uint32_t base[NKEYS];
+    for (uint32_t k = threadIdx.x; k < NKEYS; k += SORT_THREADS)
+        base[k] = start[k] + hist[(size_t)blockIdx.x * NKEYS + k];
+    __syncthreads();
+    size_t b0 = (size_t)blockIdx.x * RAYS_PER_BLOCK, b1 = b0 + RAYS_PER_BLOCK < n ? b0 + RAYS_PER_BLOCK : n;
+    for (size_t i = b0 + threadIdx.x; i < b1; i += SORT_THREADS) order[atomicAdd(&base[keys[i]], 1u)] = (uint32_t)i;
+}
+
+}  // namespace
+
+static size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t ray_order_bytes(size_t n)
+{
+    size_t nb = (n + RAYS_PER_BLOCK - 1) / RAYS_PER_BLOCK;
+    return up256(n * 2) + up256(n * 4) + nb * NKEYS * 4 + NKEYS * 4 + 256;
+}
+
+cudaError_t ray_order(const vox_cuda_tree *t, const float *o, const float *d, size_t n, void *scratch,
+                      uint32_t **order, cudaStream_t s)
+{
+    size_t nb = (n + RAYS_PER_BLOCK - 1) / RAYS_PER_BLOCK;
+    char *p = static_cast<char *>(scratch);
+    uint16_t *keys = reinterpret_cast<uint16_t *>(p);
+    p += up256(n * 2);
+    *order = reinterpret_cast<uint32_t *>(p);
+    p += up256(n * 4);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(p);
+    uint32_t *total = hist + nb * NKEYS;
+    // origin cells: 8 per axis over the tree's box widened by its largest side
+    KeyFrame f;
+    float ext = 0.0f;
+    for (int a = 0; a < 3; a++) ext = fmaxf(ext, t->bbox[3 + a] - t->bbox[a]);
+    if (!(ext > 0.0f)) ext = 1.0f;
+    for (int a = 0; a < 3; a++) {
+        f.lo[a] = t->bbox[a] - ext;
+        f.inv[a] = 8.0f / (t->bbox[3 + a] - t->bbox[a] + 2.0f * ext);
+    }
+    k_keys<<<(unsigned)nb, SORT_THREADS, 0, s>>>(o, d, n, f, keys, hist);
+    k_key_blocks<<<NKEYS / 256, 256, 0, s>>>(hist, (uint32_t)nb, total);
+    k_key_starts<<<1, 1024, 0, s>>>(total);
+    k_place<<<(unsigned)nb, SORT_THREADS, 0, s>>>(keys, n, hist, total, *order);
+    for (int i = 0; i < 4; i++) count_launch();
+    return cudaGetLastError();
+}

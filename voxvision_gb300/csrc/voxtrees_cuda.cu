@@ -67,12 +67,14 @@ __global__ void __launch_bounds__(256) ray_kernel(DevTree t, const float *__rest
                                                   uint32_t *__restrict__ leaf, uint8_t *__restrict__ slot,
                                                   float *__restrict__ pts,
                                                   unsigned long long *__restrict__ counts,
-                                                  uint32_t *__restrict__ status)
+                                                  uint32_t *__restrict__ status,
+                                                  const uint32_t *__restrict__ order)
 {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     Counts c{0, 0, 0};
     bool overflow = false;
-    if (i < n) {
+    if (j < n) {
+        size_t i = order ? order[j] : j;   // the j-th ray traced (raysort.cu)
         uint32_t start = t.root;
         if (roots) {
             uint32_t id = roots[i];
@@ -306,20 +308,36 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
 
 // ---------------------------------------------------------------- launchers
 
+// Batches of at least this many rays are traced in coherent order (raysort.cu).
+constexpr size_t RAY_SORT_MIN = 1 << 16;
+
 template <bool COUNT>
 cudaError_t launch_rays(const vox_cuda_tree *t, const float *o, const float *d, const uint32_t *roots,
                         size_t n, uint32_t *leaf, uint8_t *slot, float *pts,
                         unsigned long long *counts, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
+    void *scratch = nullptr;
+    uint32_t *order = nullptr;
+    if (!COUNT && n >= RAY_SORT_MIN && n <= 0xFFFFFFFFull) {
+        cudaError_t e = cudaMallocAsync(&scratch, ray_order_bytes(n), s);
+        if (e != cudaSuccess) return e;
+        e = ray_order(t, o, d, n, scratch, &order, s);
+        if (e != cudaSuccess) {
+            cudaFreeAsync(scratch, s);
+            return e;
+        }
+    }
     dim3 block(256), grid((unsigned)((n + 255) / 256));
     switch (t->cap_class) {
-    case 0: ray_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
-    case 1: ray_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
-    default: ray_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status); break;
+    case 0: ray_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status, order); break;
+    case 1: ray_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status, order); break;
+    default: ray_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, o, d, roots, n, leaf, slot, pts, counts, t->d_status, order); break;
     }
     count_launch();
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (scratch) cudaFreeAsync(scratch, s);
+    return e;
 }
 
 template <bool COUNT>
