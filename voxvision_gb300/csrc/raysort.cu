@@ -8,7 +8,9 @@
  * their direction, then by the cell of their origin on an 8x8x8 grid around
  * the tree (Morton order), makes the searches of a warp start close together
  * and walk the same way: on 16M random rays over the 256^3 tree the ray
- * kernel takes 2.9 ms instead of 5.4 ms.
+ * kernel takes 2.9 ms instead of 5.4 ms.  (Ball batches are not reordered:
+ * 1M random balls searched in centre order take 0.31 ms instead of 0.48 ms
+ * when sorted beforehand, but sorting them here costs as much as it saves.)
  *
  * The order is a counting sort on those 12-bit keys: per block of
  * RAYS_PER_BLOCK rays a histogram in shared memory, the position of each
@@ -33,21 +35,30 @@ constexpr int SORT_THREADS = 1024;
 constexpr uint32_t RAYS_PER_BLOCK = 65536;
 
 struct KeyFrame {
-    float lo[3], inv[3];   // origin cell = floor((o - lo) * inv), clamped to 0..7
+    float lo[3], inv[3];   // cell = floor((p - lo) * inv), clamped to the grid
 };
 
-__device__ __forceinline__ uint32_t ray_key(const float *o, const float *d, size_t i, const KeyFrame &f)
+// Morton index of point i's cell on a (2^bits)^3 grid.
+template <int BITS>
+__device__ __forceinline__ uint32_t morton_cell(const float *pt, size_t i, const KeyFrame &f)
 {
+    constexpr float TOP = (float)((1 << BITS) - 1);
     uint32_t cell[3];
     for (int a = 0; a < 3; a++) {
-        float q = (o[3 * i + a] - f.lo[a]) * f.inv[a];
-        cell[a] = q >= 7.0f ? 7u : (q > 0.0f ? (uint32_t)q : 0u);   // NaN -> 0
+        float q = (pt[3 * i + a] - f.lo[a]) * f.inv[a];
+        cell[a] = q >= TOP ? (uint32_t)TOP : (q > 0.0f ? (uint32_t)q : 0u);   // NaN -> 0
     }
     uint32_t m = 0;
-    for (int b = 0; b < 3; b++)
+    for (int b = 0; b < BITS; b++)
         for (int a = 0; a < 3; a++) m |= ((cell[a] >> b) & 1u) << (3 * b + a);
+    return m;
+}
+
+// Direction octant, then the origin's cell on an 8^3 grid.
+__device__ __forceinline__ uint32_t ray_key(const float *o, const float *d, size_t i, const KeyFrame &f)
+{
     uint32_t oct = (d[3 * i] < 0.0f) | ((d[3 * i + 1] < 0.0f) << 1) | ((d[3 * i + 2] < 0.0f) << 2);
-    return (oct << 9) | m;
+    return (oct << 9) | morton_cell<3>(o, i, f);
 }
 
 // Keys of a block's rays and the block's histogram (block-major).
