@@ -324,13 +324,18 @@ def measure_editing(vg, vox, edits=1000, seed=16):
 
 
 def measure_tree_build(vg, sizes=((256, 2, 0.08), (512, 3, 0.10)), reps=5):
-    """Time to a searchable device tree for the noise volumes: the drop-in
-    path (the library's vox_make_tree on the host, then
-    vox_cuda_tree_upload) against the tree built on the GPU from the same
-    voxel set in host memory (vox_cuda_tree_build), already on the device
-    (vox_cuda_tree_build_device) and from the raw u8 samples with the band
-    test on the GPU (vox_cuda_tree_build_raw).  Medians of `reps` after one
-    warm-up; wall-clock, all synchronous calls."""
+    """Time to a searchable device tree for the noise volumes: the host build
+    (vox_make_tree_host, tree.c's algorithm on one host thread, then
+    vox_cuda_tree_upload); the drop-in path (vox_make_tree, which builds sets
+    this large on the GPU and makes the host tree from the image, then
+    vox_cuda_tree_upload, which takes the device copy it kept); and the tree
+    built on the GPU without a host tree from the voxel set in host memory
+    (vox_cuda_tree_build), already on the device (vox_cuda_tree_build_device)
+    and from the raw u8 samples with the band test on the GPU
+    (vox_cuda_tree_build_raw).  Medians of `reps` after one warm-up;
+    wall-clock, all synchronous calls."""
+    import ctypes as C
+
     import torch
     from voxvision_gb300 import workloads as wl
     out = []
@@ -351,26 +356,35 @@ def measure_tree_build(vg, sizes=((256, 2, 0.08), (512, 3, 0.10)), reps=5):
                 r.close()
             return float(np.median(ts)) * 1e3
 
-        def host_path():
-            h = vg.HostTree.from_voxels(vox)
-            d = vg.DeviceTree(h.ptr)
-            d._host = h
-            return d
+        L = vg.lib()
 
-        t0 = time.perf_counter()
-        h = vg.HostTree.from_voxels(vox)
-        t_make = (time.perf_counter() - t0) * 1e3
-        t0 = time.perf_counter()
-        vg.DeviceTree(h.ptr).close()
-        t_up = (time.perf_counter() - t0) * 1e3
-        h.close()
+        def built_by(fn):
+            s = np.ascontiguousarray(vox, np.float32).copy()   # the build reorders its set
+            t0 = time.perf_counter()
+            h = vg.HostTree(fn(s.ctypes.data_as(C.c_void_p), s.shape[0]))
+            t1 = time.perf_counter()
+            d = vg.DeviceTree(h.ptr)
+            t2 = time.perf_counter()
+            d.close()
+            h.close()
+            return (t1 - t0) * 1e3, (t2 - t1) * 1e3
+
+        def median_of(fn, k):
+            fn()
+            runs = [fn() for _ in range(k)]
+            return [float(np.median([r[i] for r in runs])) for i in range(2)]
+
+        host_make, host_up = median_of(lambda: built_by(L.vox_make_tree_host), reps if n <= 256 else 1)
+        drop_make, drop_up = median_of(lambda: built_by(L.vox_make_tree), reps)
         rec = {"volume": f"{n}^3 u8 value noise, seed {seed}, band {lo}..{lo + w - 1}", "voxels": int(len(vox)),
-               "host_make_tree_ms": t_make, "upload_ms": t_up,
-               "host_path_ms": timed(host_path) if n <= 256 else t_make + t_up,
+               "host_make_tree_ms": host_make, "upload_ms": host_up, "host_path_ms": host_make + host_up,
+               "dropin_make_tree_ms": drop_make, "dropin_first_upload_ms": drop_up,
+               "dropin_path_ms": drop_make + drop_up,
                "device_build_ms": timed(lambda: vg.DeviceTree.build(vox)),
                "device_build_resident_ms": timed(lambda: vg.DeviceTree.build_device(d_vox)),
                "device_build_raw_ms": timed(lambda: vg.DeviceTree.from_raw(raw, vol.shape, 1, lo, lo + w - 1))}
         rec["speedup_vs_host_path"] = rec["host_path_ms"] / rec["device_build_ms"]
+        rec["dropin_speedup_vs_host_path"] = rec["host_path_ms"] / rec["dropin_path_ms"]
         out.append(rec)
         del d_vox
     return out

@@ -49,8 +49,12 @@ struct vox_node {             /* tree.h:28-38 */
 /* Voxel size (tree.c:11).  Read by vox_make_tree and by vox_cuda_tree_upload. */
 extern vox_dot vox_voxel;
 
-/* tree.h:60 -- build a tree; `set` is reordered in place and may be freed after. */
+/* tree.h:60 -- build a tree; `set` is reordered in place and may be freed after.
+ * Large sets are built on the GPU when one is present (the same tree, and the
+ * same order of `set`; see vox_cuda_make_tree_gpu_min in voxtrees_cuda.h). */
 struct vox_node *vox_make_tree(vox_dot set[], size_t n);
+/* Extension: vox_make_tree on the host only (tree.c:249-338). */
+struct vox_node *vox_make_tree_host(vox_dot set[], size_t n);
 /* tree.h:67 */
 void vox_destroy_tree(struct vox_node *tree);
 /* tree.h:72 */

@@ -118,6 +118,15 @@ int vox_cuda_tree_build(const float *set, size_t n, vox_cuda_tree **out);
 /* `d_set`: n voxels (3n floats) in device memory of the current device. */
 int vox_cuda_tree_build_device(const float *d_set, size_t n, vox_cuda_tree **out);
 
+/* vox_make_tree builds sets of at least this many voxels on the GPU (when a
+ * device is present): the host tree is then made from the device image --
+ * node for node the tree of vox_make_tree_host, `set` left in the same order
+ * -- and the device copy is kept for the tree's first vox_cuda_tree_upload
+ * (single queries and render contexts upload through it), dropped by an edit
+ * or vox_destroy_tree.  Default 65536; SIZE_MAX keeps every build on the
+ * host.  Returns the previous value. */
+size_t vox_cuda_make_tree_gpu_min(size_t n);
+
 /* Which samples are solid.  With mask == NULL: lo <= sample <= hi (the
  * demo's "sample > threshold" is lo = threshold + 1, hi = 0xFFFFFFFF; the
  * engine's ranged reader [min, max) is lo = min, hi = max - 1).  Otherwise

@@ -105,6 +105,8 @@ SIGNATURES = {
     "vox_cuda_tree_refresh": (C.c_int, [_vp, _vp]),
     "vox_cuda_render_frames": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp]),
     "vox_cuda_tree_build": (C.c_int, [_vp, _sz, C.POINTER(_vp)]),
+    "vox_cuda_make_tree_gpu_min": (_sz, [_sz]),
+    "vox_make_tree_host": (_vp, [_vp, _sz]),
     "vox_cuda_tree_build_device": (C.c_int, [_vp, _sz, C.POINTER(_vp)]),
     "vox_cuda_tree_build_raw": (C.c_int, [_vp, C.POINTER(C.c_uint * 3), C.c_uint, C.POINTER(RawTest),
                                           C.POINTER(_vp)]),

@@ -27,7 +27,7 @@ CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-fvisibility=hidden", "-ffp-contract=
             "-Wno-unused-parameter"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall"]
 
-CUDA_SOURCES = ["voxtrees_cuda.cu", "batch.cu", "server.cu", "build.cu", "raysort.cu"]
+CUDA_SOURCES = ["voxtrees_cuda.cu", "batch.cu", "server.cu", "build.cu", "raysort.cu", "make_tree.cu"]
 C_SOURCES = ["host_tree.c", "cameras.c", "lights.c"]
 CXX_SOURCES = ["flatten.cpp", "dropin_search.cpp", "renderer.cpp"]
 

@@ -1006,7 +1006,8 @@ __global__ void k_down(Level L, Level Nx)
 }
 
 // Node records (pool_layout.h) and the pre-order id map.
-__global__ void k_emit(Level L, uint4 *pool, uint32_t *rec_of_id, uint64_t units, uint64_t nodes, uint32_t *err)
+__global__ void k_emit(Level L, uint4 *pool, uint32_t *rec_of_id, uint64_t units, uint64_t nodes, uint32_t *err,
+                       uint32_t *dots_of_id)
 {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= L.m) return;
@@ -1016,6 +1017,7 @@ __global__ void k_emit(Level L, uint4 *pool, uint32_t *rec_of_id, uint64_t units
         atomicOr(err, ERR_LAYOUT);
         return;
     }
+    if (dots_of_id) dots_of_id[id] = L.n[k];   // the node's dots_num (tree.c:262)
     uint4 extra = make_uint4(0u, 0u, 0u, 0u);
     if (kind == K_DENSE) {
         meta = VOXP_KIND_DENSE;
@@ -1119,8 +1121,9 @@ int fail(cudaError_t e) { return e == cudaErrorMemoryAllocation ? VOX_CUDA_ENOME
     } while (0)
 
 // Builds the tree of the N voxels at d_set (device, 3N floats, not modified)
-// into t.  Synchronous on s.
-int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s)
+// into t.  Synchronous on s.  With `x`, also hands back what a host tree
+// needs beyond the image (see HostTreeExtras).
+int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s, HostTreeExtras *x = nullptr)
 {
     const float vx = vox_voxel[0], vy = vox_voxel[1], vz = vox_voxel[2];
     ImageStats st{};
@@ -1297,8 +1300,9 @@ int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s)
         count_launch();
     }
     uint4 *pool = nullptr;
-    uint32_t *map = nullptr;
+    uint32_t *map = nullptr, *dots = nullptr;
     size_t pool_bytes = units * 16, map_bytes = nodes * 4;
+    if (x) TRY(d.get(&dots, nodes));
     TRY(cudaMalloc(&pool, pool_bytes));
     if (cudaMalloc(&map, map_bytes) != cudaSuccess) {
         cudaFree(pool);
@@ -1306,13 +1310,20 @@ int build_tree(vox_cuda_tree *t, const float *d_set, uint64_t N, cudaStream_t s)
     }
     for (int lv = 0; lv < nl; lv++) {
         Level L = levels[lv];
-        k_emit<<<grid_for(L.m, 256), 256, 0, s>>>(L, pool, map, units, nodes, err);
+        k_emit<<<grid_for(L.m, 256), 256, 0, s>>>(L, pool, map, units, nodes, err, dots);
         k_emit_voxels<<<grid_for((uint64_t)L.m * 32, 256), 256, 0, s>>>(L, P[cur], pool, units, err);
         count_launch();
         count_launch();
     }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h_root[1], err, 4, cudaMemcpyDeviceToHost, s);
+    if (x) {
+        x->dots_of_id.resize(nodes);
+        if (e == cudaSuccess && x->order)
+            e = cudaMemcpyAsync(x->order, P[cur], 12 * N, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(x->dots_of_id.data(), dots, nodes * 4, cudaMemcpyDeviceToHost, s);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess || h_root[1]) {
         cudaFree(pool);
@@ -1426,6 +1437,21 @@ int check_raw_args(const unsigned dim[3], unsigned samplesize, const vox_cuda_ra
 }  // namespace
 
 // ======================================================================== API
+
+int build_for_host_tree(const float *set, size_t n, vox_cuda_tree **out, HostTreeExtras *x)
+{
+    if (n == 0 || n > MAX_VOXELS || !set) return VOX_CUDA_EINVAL;
+    return new_tree(out, [&](vox_cuda_tree *t, cudaStream_t s) {
+        float *d = nullptr;
+        if (cudaMallocAsync(&d, 12ull * n, s) != cudaSuccess) return (int)VOX_CUDA_ENOMEM;
+        int rc = VOX_CUDA_OK;
+        if (cudaMemcpyAsync(d, set, 12ull * n, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = VOX_CUDA_ECUDA;
+        if (rc == VOX_CUDA_OK) rc = build_tree(t, d, n, s, x);
+        cudaFreeAsync(d, s);
+        cudaStreamSynchronize(s);
+        return rc;
+    });
+}
 
 EXPORT int vox_cuda_tree_build_device(const float *d_set, size_t n, vox_cuda_tree **out)
 {

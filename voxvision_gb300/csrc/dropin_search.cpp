@@ -21,6 +21,11 @@
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
+// voxtrees_cuda.cu: the upload proper (flatten and copy), and whether a device
+// tree matches the current device and voxel size.
+int tree_upload_flat(const vox_node *root, vox_cuda_tree **out);
+bool tree_fits_now(const vox_cuda_tree *t);
+
 namespace {
 
 struct Entry {
@@ -30,6 +35,32 @@ struct Entry {
 
 std::mutex g_mu;
 std::vector<Entry> g_trees;
+// Device copies made by vox_make_tree when it built the tree on the GPU,
+// waiting for the first vox_cuda_tree_upload (or single query) of the root.
+std::vector<Entry> g_prebuilt;
+
+vox_cuda_tree *take_prebuilt_locked(const vox_node *root)
+{
+    for (size_t i = 0; i < g_prebuilt.size(); i++) {
+        if (g_prebuilt[i].root == root) {
+            vox_cuda_tree *t = g_prebuilt[i].tree;
+            g_prebuilt[i] = g_prebuilt.back();
+            g_prebuilt.pop_back();
+            return t;
+        }
+    }
+    return nullptr;
+}
+
+// The device copy vox_make_tree made of the tree at `root`, for its first
+// upload; a copy made for another device or another voxel size is dropped.
+vox_cuda_tree *take_prebuilt_usable_locked(const vox_node *root)
+{
+    vox_cuda_tree *t = take_prebuilt_locked(root);
+    if (!t || tree_fits_now(t)) return t;
+    vox_cuda_tree_free(t);
+    return nullptr;
+}
 
 // Device tree holding `node` and the node's pre-order id, uploading a new
 // tree rooted at `node` when no registered tree contains it.
@@ -42,8 +73,8 @@ bool resolve(const vox_node *node, vox_cuda_tree **tree, uint32_t *id)
             return true;
         }
     }
-    vox_cuda_tree *t = nullptr;
-    if (vox_cuda_tree_upload(node, &t) != VOX_CUDA_OK) return false;
+    vox_cuda_tree *t = take_prebuilt_usable_locked(node);
+    if (!t && tree_upload_flat(node, &t) != VOX_CUDA_OK) return false;
     g_trees.push_back({node, t});
     *tree = t;
     *id = 0;
@@ -89,6 +120,7 @@ EXPORT int vox_tree_ball_collidep(const struct vox_node *tree, const vox_dot cen
 EXPORT void vox_cuda_forget_tree(const struct vox_node *root)
 {
     std::lock_guard<std::mutex> lock(g_mu);
+    if (vox_cuda_tree *p = take_prebuilt_locked(root)) vox_cuda_tree_free(p);
     for (size_t i = 0; i < g_trees.size(); i++) {
         if (g_trees[i].root == root) {
             vox_cuda_tree_free(g_trees[i].tree);
@@ -103,6 +135,16 @@ EXPORT void vox_cuda_forget_tree(const struct vox_node *root)
 extern "C" void vox_dropin_forget_containing(const struct vox_node *node)
 {
     std::lock_guard<std::mutex> lock(g_mu);
+    for (size_t i = 0; i < g_prebuilt.size();) {
+        uint32_t id;
+        if (vox_cuda_tree_node_id(g_prebuilt[i].tree, node, &id) == VOX_CUDA_OK) {
+            vox_cuda_tree_free(g_prebuilt[i].tree);
+            g_prebuilt[i] = g_prebuilt.back();
+            g_prebuilt.pop_back();
+        } else {
+            i++;
+        }
+    }
     for (size_t i = 0; i < g_trees.size();) {
         uint32_t id;
         if (vox_cuda_tree_node_id(g_trees[i].tree, node, &id) == VOX_CUDA_OK) {
@@ -113,4 +155,20 @@ extern "C" void vox_dropin_forget_containing(const struct vox_node *node)
             i++;
         }
     }
+}
+
+// vox_make_tree (make_tree.cpp): keep the device copy of a tree it built on
+// the GPU until the tree's first upload, edit or destruction.
+void dropin_keep_prebuilt(const vox_node *root, vox_cuda_tree *t)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (vox_cuda_tree *old = take_prebuilt_locked(root)) vox_cuda_tree_free(old);
+    g_prebuilt.push_back({root, t});
+}
+
+// vox_cuda_tree_upload: the kept device copy of `root`, if there is one.
+vox_cuda_tree *dropin_take_prebuilt(const vox_node *root)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    return take_prebuilt_usable_locked(root);
 }

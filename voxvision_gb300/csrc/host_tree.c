@@ -18,6 +18,8 @@
 
 #define EXPORT __attribute__((visibility("default")))
 
+static void destroy_nodes(struct vox_node *tree);
+
 EXPORT vox_dot vox_voxel = {1.0f, 1.0f, 1.0f};
 
 EXPORT void vox_set_voxel_size(float x, float y, float z)
@@ -108,7 +110,7 @@ typedef struct {
     struct vox_node **slot;   /* where the built node is stored */
 } build_job;
 
-EXPORT struct vox_node *vox_make_tree(vox_dot set[], size_t n)
+EXPORT struct vox_node *vox_make_tree_host(vox_dot set[], size_t n)
 {
     struct vox_node *root = NULL;
     if (n == 0) return NULL;
@@ -178,19 +180,31 @@ EXPORT struct vox_node *vox_make_tree(vox_dot set[], size_t n)
 
 oom:
     free(jobs);
-    vox_destroy_tree(root);
+    destroy_nodes(root);
     return NULL;
 }
 
-EXPORT void vox_destroy_tree(struct vox_node *tree)
+static void destroy_nodes(struct vox_node *tree)
 {
     if (!tree) return;
     if (tree->flags & VOX_LEAF) {
         free(tree->data.dots);
     } else if (!(tree->flags & VOX_LEAF_MASK)) {
-        for (int i = 0; i < 8; i++) vox_destroy_tree(tree->data.inner.children[i]);
+        for (int i = 0; i < 8; i++) destroy_nodes(tree->data.inner.children[i]);
     }
     free(tree);
+}
+
+/* Drops cached device copies of trees that contain `node` (dropin_search.cpp). */
+void vox_dropin_forget_containing(const struct vox_node *node);
+
+EXPORT void vox_destroy_tree(struct vox_node *tree)
+{
+    if (!tree) return;
+    // a later tree may be allocated at the same addresses: no device copy of
+    // this one may outlive it
+    vox_dropin_forget_containing(tree);
+    destroy_nodes(tree);
 }
 
 EXPORT size_t vox_voxels_in_tree(const struct vox_node *tree)
@@ -224,8 +238,6 @@ EXPORT struct vox_node *vox_make_dense_leaf(const struct vox_box *box)
  * boxes grow on insertion and are not shrunk on deletion, as there.
  * ---------------------------------------------------------------------- */
 
-/* Drops cached device copies of trees that contain `node` (dropin_search.cpp). */
-void vox_dropin_forget_containing(const struct vox_node *node);
 
 /* tree.c:185-194 */
 static void align_to_grid(vox_dot d)
@@ -396,7 +408,7 @@ static int insert_at(struct vox_node **slot, const vox_dot d)
         if (!t) {
             vox_dot one[1];
             memcpy(one[0], d, sizeof(vox_dot));
-            node = vox_make_tree(one, 1);
+            node = vox_make_tree_host(one, 1);
             if (!node) return 1;
             *slot = node;
             return 0;
@@ -409,7 +421,7 @@ static int insert_at(struct vox_node **slot, const vox_dot d)
             } else {
                 node = vox_make_dense_leaf(&t->bounding_box);
                 if (!node) return 1;
-                vox_destroy_tree(t);
+                destroy_nodes(t);
             }
             *slot = node;
             return 0;
@@ -421,9 +433,9 @@ static int insert_at(struct vox_node **slot, const vox_dot d)
                 vox_dot set[VOX_MAX_DOTS];
                 collect(t, set);
                 memcpy(set[t->dots_num], d, sizeof(vox_dot));
-                node = vox_make_tree(set, t->dots_num + 1);
+                node = vox_make_tree_host(set, t->dots_num + 1);
                 if (!node) return 1;
-                vox_destroy_tree(t);
+                destroy_nodes(t);
             } else {
                 node = insert_beside_dense(t, d);
                 if (!node) return 1;
@@ -444,10 +456,10 @@ static int insert_at(struct vox_node **slot, const vox_dot d)
             if (!set) return 1;
             memcpy(set, t->data.dots, t->dots_num * sizeof(vox_dot));
             memcpy(set[t->dots_num], d, sizeof(vox_dot));
-            node = vox_make_tree(set, t->dots_num + 1);
+            node = vox_make_tree_host(set, t->dots_num + 1);
             free(set);
             if (!node) return 1;
-            vox_destroy_tree(t);
+            destroy_nodes(t);
             *slot = node;
             return 0;
         }
@@ -508,7 +520,7 @@ static struct vox_node *delete_from_stripe(struct vox_node *t, const vox_dot d)
     n->data.inner.children[0] = c;
     c->dots_num--;
     c->bounding_box.min[axis] += vox_voxel[axis];
-    vox_destroy_tree(t);
+    destroy_nodes(t);
     return n;
 }
 
@@ -526,7 +538,7 @@ static struct vox_node *delete_from_dense(struct vox_node *t, const vox_dot d)
         if (!n) return NULL;
         for (int i = 0; i < 7; i++)
             if (octant_box(&t->bounding_box, past, &b, i)) n->data.inner.children[i] = vox_make_dense_leaf(&b);
-        vox_destroy_tree(t);
+        destroy_nodes(t);
         return n;
     }
     n = inner_node(&t->bounding_box, t->dots_num - 1, d);
@@ -535,7 +547,7 @@ static struct vox_node *delete_from_dense(struct vox_node *t, const vox_dot d)
         if (octant_box(&t->bounding_box, d, &b, i)) n->data.inner.children[i] = vox_make_dense_leaf(&b);
     /* the voxel is now the corner of octant 0 */
     n->data.inner.children[0] = delete_from_dense(n->data.inner.children[0], d);
-    vox_destroy_tree(t);
+    destroy_nodes(t);
     return n;
 }
 
@@ -545,7 +557,7 @@ static void delete_at(struct vox_node **slot, const vox_dot d)
     for (;;) {
         struct vox_node *t = *slot;
         if (t->dots_num == 1) {
-            vox_destroy_tree(t);
+            destroy_nodes(t);
             *slot = NULL;
             return;
         }
@@ -568,8 +580,8 @@ static void delete_at(struct vox_node **slot, const vox_dot d)
                 unsigned i = 0;
                 while (i < t->dots_num && !same_voxel(set[i], d)) i++;
                 memmove(set + i, set + i + 1, sizeof(vox_dot) * (t->dots_num - i - 1));
-                *slot = vox_make_tree(set, t->dots_num - 1);
-                vox_destroy_tree(t);
+                *slot = vox_make_tree_host(set, t->dots_num - 1);
+                destroy_nodes(t);
             } else {
                 *slot = delete_from_dense(t, d);
             }

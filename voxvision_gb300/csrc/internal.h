@@ -54,6 +54,25 @@ struct ImageStats {
 int adopt_image(vox_cuda_tree *t, uint4 *pool, size_t pool_bytes, uint32_t *map, size_t map_bytes,
                 const ImageStats &st);
 
+/* What a host tree (struct vox_node) needs beyond the device image when it
+ * is rebuilt from a device-built tree: each node's dots_num (an inner or
+ * dense node's is in no record) by pre-order id, and the set in the order
+ * vox_make_tree leaves it (tree.c sorts its input in place). */
+struct HostTreeExtras {
+    std::vector<uint32_t> dots_of_id;
+    float *order = nullptr;   // 3n floats of host memory, or NULL
+};
+
+/* vox_cuda_tree_upload without looking for a device copy vox_make_tree kept
+ * (voxtrees_cuda.cu); whether a device tree suits the current device and
+ * voxel size. */
+int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out);
+bool tree_fits_now(const vox_cuda_tree *t);
+
+/* The tree of the n voxels at `set` (host) built on the GPU into a new
+ * handle, with the extras (build.cu). */
+int build_for_host_tree(const float *set, size_t n, vox_cuda_tree **out, HostTreeExtras *x);
+
 // Ray stacks hold at most 3 pending children per inner level on the path.
 constexpr int CAP0 = 28, CAP1 = 64, CAP2 = 256;
 

@@ -784,7 +784,29 @@ int adopt_image(vox_cuda_tree *t, uint4 *pool, size_t pool_bytes, uint32_t *map,
     return VOX_CUDA_OK;
 }
 
+// dropin_search.cpp: a device copy vox_make_tree kept for the tree at `root`.
+vox_cuda_tree *dropin_take_prebuilt(const vox_node *root);
+
+bool tree_fits_now(const vox_cuda_tree *t)
+{
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess && dev == t->device && t->flat.voxel[0] == vox_voxel[0] &&
+           t->flat.voxel[1] == vox_voxel[1] && t->flat.voxel[2] == vox_voxel[2];
+}
+
 EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out)
+{
+    if (!out) return VOX_CUDA_EINVAL;
+    if (root) {
+        if (vox_cuda_tree *t = dropin_take_prebuilt(root)) {   // built on the GPU by vox_make_tree
+            *out = t;
+            return VOX_CUDA_OK;
+        }
+    }
+    return tree_upload_flat(root, out);
+}
+
+int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
 {
     if (!out) return VOX_CUDA_EINVAL;
     *out = nullptr;
