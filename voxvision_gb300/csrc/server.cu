@@ -8,13 +8,14 @@
  * order while the budget and the in-flight slots allow, and put everything
  * admitted since the previous launch into one launch on the next of several
  * streams -- all frames into one persistent work-queue kernel (the batched
- * kernel of batch.cu), each ball request into the ball kernel.  Results are
- * written in place into the pinned host buffers the clients read (frames by
- * the frame kernel's stores, hits by the ball kernel's, which also reads its
- * staged inputs from pinned memory): on GB300 these stores cross the host
- * link while the kernels run, so a request needs no device buffer and no
- * copy.  The device budget holds the resident trees and the per-launch job
- * tables; the pinned-host budget holds the results and staged inputs.
+ * kernel of batch.cu), each ball request into the ball kernel.  Frames are
+ * drawn into device memory and copied into the pinned host buffers the
+ * clients read as soon as their launch's kernel ends (frame stores straight
+ * into host memory slow the frame kernel by a third); ball hits, one byte a
+ * query, are written in place by the ball kernel, which also reads its staged
+ * inputs from pinned memory.  The device budget holds the resident trees,
+ * the per-launch job tables and the frames being drawn; the pinned-host
+ * budget holds the results and staged inputs.
  * Requests that arrive while earlier launches are still on the GPU go out
  * in the next launch and overlap with them on the device instead of waiting
  * for them.
@@ -126,6 +127,7 @@ struct Launch {
     void *h_table = nullptr;
     size_t h_table_cls = 0;
     void *d_table = nullptr;        // job table + queue head
+    void *d_frames = nullptr;       // the launch's frames, drawn here before their copies
     std::atomic<bool> finished{false};   // set by the stream callback
     std::atomic<uint64_t> t_cb{0};       // completion time seen by the callback
     bool has_callback = false;      // then only `finished` may retire the launch
@@ -223,6 +225,7 @@ void release_launch(vox_cuda_server *s, Launch *L)
 {
     for (auto &hp : L->host_free) s->pinned.put(hp.first, hp.second);
     if (L->d_table) cudaFreeAsync(L->d_table, L->stream);
+    if (L->d_frames) cudaFreeAsync(L->d_frames, L->stream);
     s->pinned.put(L->h_table, L->h_table_cls);
     if (L->done) cudaEventDestroy(L->done);
     delete L;
@@ -239,6 +242,8 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
     uint64_t t = now_ns();
     std::vector<vox_cuda_frame_job> jobs;
     std::vector<Request *> frames;
+    std::vector<size_t> frame_at;   // offset of each frame in the launch's device frames
+    size_t frame_bytes = 0;
     for (Request *r : batch) {
         r->t_launch = t;
         L->reqs.push_back(r);
@@ -246,7 +251,7 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
         r->res_bytes = out_bytes;
         r->h_res = s->pinned.get(out_bytes, &r->h_cls);
         void *d_res = nullptr;
-        if (!r->h_res || cudaHostGetDevicePointer(&d_res, r->h_res, 0) != cudaSuccess) {
+        if (!r->h_res || (r->kind != FRAME && cudaHostGetDevicePointer(&d_res, r->h_res, 0) != cudaSuccess)) {
             r->status = VOX_CUDA_ENOMEM;
             continue;
         }
@@ -257,9 +262,11 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
             j.w = r->w;
             j.h = r->h;
             j.texture = s->d_tex;
-            j.argb = static_cast<uint32_t *>(d_res);
+            j.argb = nullptr;   // set once the launch's device frames exist
             jobs.push_back(j);
             frames.push_back(r);
+            frame_at.push_back(frame_bytes);
+            frame_bytes += (out_bytes + 255) & ~size_t(255);
         } else {
             size_t n = r->n, in_bytes = n * 16;
             void *d_in = nullptr;
@@ -281,10 +288,17 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
         size_t tb = (frame_job_table_bytes((uint32_t)jobs.size()) + 255) & ~(size_t)255;
         L->h_table = s->pinned.get(tb, &L->h_table_cls);
         int rc = VOX_CUDA_ENOMEM;
-        if (L->h_table && cudaMallocAsync(&L->d_table, tb + 256, st) == cudaSuccess) {
+        if (L->h_table && cudaMallocAsync(&L->d_table, tb + 256, st) == cudaSuccess &&
+            cudaMallocAsync(&L->d_frames, frame_bytes, st) == cudaSuccess) {
+            for (size_t q = 0; q < jobs.size(); q++)
+                jobs[q].argb = reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_frames) + frame_at[q]);
             uint32_t *counter = reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_table) + tb);
             rc = enqueue_frame_jobs(jobs.data(), (uint32_t)jobs.size(), L->h_table, L->d_table, counter,
                                     s->nsm, st);
+            for (size_t q = 0; q < frames.size() && rc == VOX_CUDA_OK; q++)   // results out after the kernel
+                if (cudaMemcpyAsync(frames[q]->h_res, jobs[q].argb, frames[q]->res_bytes, cudaMemcpyDeviceToHost,
+                                    st) != cudaSuccess)
+                    rc = VOX_CUDA_ECUDA;
         }
         if (rc)
             for (Request *r : frames) r->status = rc;
@@ -363,12 +377,12 @@ void worker_loop(vox_cuda_server *s)
     }
 }
 
-// device bytes a request holds while admitted: its share of the launch's job
-// table (its result and inputs live in pinned host memory)
+// device bytes a request holds while admitted: a frame's share of the
+// launch's job table and the frame it is drawn into (ball inputs and results
+// live in pinned host memory)
 uint64_t request_bytes(Kind k, uint64_t a, uint64_t b)
 {
-    (void)a; (void)b;
-    return k == FRAME ? 256 : 0;
+    return k == FRAME ? 256 + ((a * b * 4 + 255) & ~uint64_t(255)) : 0;
 }
 
 // pinned host bytes a request holds while admitted: its result, and for ball
