@@ -4,9 +4,9 @@
  *
  * vox_render (renderer.c:200-319) draws a whole frame: the scene tree is
  * uploaded once per vox_context_set_scene, the camera state is read from the
- * built-in camera object, and one fused kernel produces the ARGB frame in
- * device memory.  vox_redraw (renderer.c:321-327) then brings the frame to
- * the host buffer returned by vox_context_pixels.  Instead of an SDL
+ * built-in camera object, and one fused kernel draws the ARGB frame straight
+ * into the context's page-locked frame.  vox_redraw (renderer.c:321-327)
+ * then brings the frame to the host buffer returned by vox_context_pixels.  Instead of an SDL
  * surface the context owns a headless frame.
  */
 #include <cuda_runtime.h>
@@ -39,6 +39,7 @@ struct vox_rnd_ctx {
     uint8_t *d_tex = nullptr;
     uint32_t *d_frame = nullptr;
     uint32_t *h_stage = nullptr;                   // pinned copy of the frame
+    uint32_t *d_stage = nullptr;                   // the device's address of h_stage (frames drawn in place)
     uint32_t *pixels = nullptr;                    // what vox_context_pixels returns
     cudaStream_t stream = nullptr;
     int status = VOX_CUDA_OK;
@@ -94,6 +95,9 @@ EXPORT struct vox_rnd_ctx *vox_make_context_headless(unsigned int width, unsigne
         delete c;
         return nullptr;
     }
+    void *alias = nullptr;
+    if (cudaHostGetDevicePointer(&alias, c->h_stage, 0) == cudaSuccess) c->d_stage = static_cast<uint32_t *>(alias);
+    else cudaGetLastError();
     return c;
 }
 
@@ -171,11 +175,16 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
         if (rc) { ctx->status = rc; return; }
         ctx->d_lights_version = ctx->lights->version;
     }
+    // one frame waited on: drawn straight into the pinned frame when the device
+    // can address it (its stores cross the host link while the frame is
+    // traced; no copy follows), else into device memory and copied
+    uint32_t *target = ctx->d_stage ? ctx->d_stage : ctx->d_frame;
     int rc = vox_cuda_render_lit_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
-                                        ctx->lights ? ctx->d_lights : nullptr, ctx->d_frame, ctx->stream);
+                                        ctx->lights ? ctx->d_lights : nullptr, target, ctx->stream);
     if (rc) { ctx->status = rc; return; }
     size_t bytes = (size_t)ctx->w * ctx->h * 4;
-    if (cudaMemcpyAsync(ctx->h_stage, ctx->d_frame, bytes, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+    if ((!ctx->d_stage &&
+         cudaMemcpyAsync(ctx->h_stage, ctx->d_frame, bytes, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess) ||
         cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         ctx->status = VOX_CUDA_ECUDA;
         return;
