@@ -237,6 +237,17 @@ int vox_cuda_render_lit(const vox_cuda_tree *tree, const vox_cuda_camera *camera
 int vox_cuda_render_lit_device(const vox_cuda_tree *tree, const vox_cuda_camera *camera, uint32_t w, uint32_t h,
                                unsigned int quality, const uint8_t *texture, const vox_cuda_lights *lights,
                                uint32_t *argb, void *stream);
+/* A frame through a camera class the device cannot compute (replaces the
+ * camera->iface->screen2world calls of vox_render, renderer.c:200-319): the
+ * caller gives every pixel's direction in `dirs` (device memory, 3 floats a
+ * pixel, rows of w pixels; the camera's screen2world(x, y)) and the camera's
+ * position in `origin` (host, 3 floats).  Any quality, FAST and ADAPTIVE as
+ * the reference draws them from those directions; BEST traces every pixel
+ * from the root.  `lights` may be NULL.  Same geometry rules and errors as
+ * vox_cuda_render_lit_device. */
+int vox_cuda_render_rays_device(const vox_cuda_tree *tree, const float *origin, const float *dirs, uint32_t w,
+                                uint32_t h, unsigned int quality, const uint8_t *texture,
+                                const vox_cuda_lights *lights, uint32_t *argb, void *stream);
 
 /* Settings of the BEST-quality frame kernel behind vox_cuda_render*,
  * process-wide (no counterpart in the reference, whose renderer has no

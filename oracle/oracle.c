@@ -547,6 +547,11 @@ static void cross(const float *v1, const float *v2, float *r)
 /* simple-camera.c:21-31 with vect-ops.c:28-36; doom-camera.c:24-57 */
 void orc_screen2world(const orc_camera *cam, int sx, int sy, float *ray)
 {
+    if (cam->kind == 2) {   /* renderer.c:251,260,292: camera->iface->screen2world of another class */
+        const float *r = cam->rays + 3 * ((size_t)sy * (size_t)cam->rays_w + (size_t)sx);
+        ray[0] = r[0]; ray[1] = r[1]; ray[2] = r[2];
+        return;
+    }
     if (cam->kind == 1) {
         float d0 = cam->mul * (float)sx - cam->xsub;
         float d1 = 1;

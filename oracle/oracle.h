@@ -55,13 +55,17 @@ typedef struct {
 } orc_counts;
 
 /* Camera state consumed by screen2world (simple-camera.c:10-17,
- * doom-camera.c:8-15). kind 0 = simple-camera, 1 = doom-camera. */
+ * doom-camera.c:8-15). kind 0 = simple-camera, 1 = doom-camera, 2 = any
+ * other class, known by what its screen2world returns: pixel (x, y)'s
+ * direction is rays[3 * (y * rays_w + x) ...]. */
 typedef struct {
     int32_t kind;
     float position[3];
     float rotation[4];
     float mul, xsub, ysub;
     float sinphi, cosphi, k;
+    const float *rays;
+    int32_t rays_w;
 } orc_camera;
 
 void orc_set_voxel(float x, float y, float z);

@@ -32,7 +32,8 @@ def build(force: bool = False) -> str:
 class OrcCamera(C.Structure):
     _fields_ = [("kind", C.c_int32), ("position", C.c_float * 3), ("rotation", C.c_float * 4),
                 ("mul", C.c_float), ("xsub", C.c_float), ("ysub", C.c_float),
-                ("sinphi", C.c_float), ("cosphi", C.c_float), ("k", C.c_float)]
+                ("sinphi", C.c_float), ("cosphi", C.c_float), ("k", C.c_float),
+                ("rays", C.c_void_p), ("rays_w", C.c_int32)]
 
 
 def lib():
@@ -171,6 +172,11 @@ def camera(state: dict) -> OrcCamera:
     cam.rotation[:] = [float(x) for x in state.get("rotation", (1, 0, 0, 0))]
     for k in ("mul", "xsub", "ysub", "sinphi", "cosphi", "k"):
         setattr(cam, k, float(state.get(k, 0.0)))
+    if cam.kind == 2:   # directions of every pixel, shape (h, w, 3)
+        rays = np.ascontiguousarray(state["rays"], dtype=np.float32)
+        cam._rays = rays
+        cam.rays = rays.ctypes.data
+        cam.rays_w = rays.shape[1]
     return cam
 
 

@@ -100,3 +100,24 @@ def test_oracle_render_matches_reference_search():
     c = tex[idx[:, 0] * 1024 + idx[:, 1] * 32 + idx[:, 2]].astype(np.uint32)
     expect = np.where(hit, 0xFF000000 | (c << 16) | (c << 8) | c, 0).astype(np.uint32)
     assert np.array_equal(img.ravel(), expect)
+
+
+def test_oracle_ray_buffer_camera_draws_its_directions():
+    """Camera kind 2 (a class known only by what its screen2world returns)
+    draws, in every quality, the frame of the class whose directions it
+    holds: here the reference-pinned simple camera of the render64 case."""
+    g = load("render64")
+    orc.set_voxel((1, 1, 1))
+    t = orc.OracleTree.from_voxels(g["voxels"].astype(np.float32))
+    from voxvision_gb300 import workloads as wl
+    tex = wl.texture32(7)
+    st = dict(kind=0, position=g["cam_position"], rotation=g["cam_rotation"], mul=g["cam_mul"],
+              xsub=g["cam_xsub"], ysub=g["cam_ysub"])
+    w, h = int(g["w"]), int(g["h"])
+    table = np.array([[orc.screen2world(st, x, y) for x in range(w)] for y in range(h)], np.float32)
+    buf = dict(kind=2, position=g["cam_position"], rays=table)
+    assert np.array_equal(orc.screen2world(buf, 5, 3), table[3, 5])
+    for q in (0, 1, 2, 2 | 4, 2 | 8):
+        a, _ = orc.render_quality(t.ptr, st, w, h, q, tex, nthreads=2)
+        b, _ = orc.render_quality(t.ptr, buf, w, h, q, tex, nthreads=2)
+        assert np.array_equal(a, b), q

@@ -265,6 +265,15 @@ class DeviceTree:
         check(lib().vox_cuda_render_device(self.h, C.byref(camera), w, h, _dptr(texture), _dptr(argb),
                                            stream), "vox_cuda_render_device")
 
+    def render_rays_device(self, origin, dirs, w: int, h: int, quality: int, texture, argb,
+                           lights: "DeviceLights | None" = None, stream=None):
+        """vox_cuda_render_rays_device: a frame from each pixel's direction
+        (`dirs`, device, (h, w, 3) float32) and the camera's position."""
+        o = np.ascontiguousarray(np.asarray(origin, np.float32).reshape(3))
+        check(lib().vox_cuda_render_rays_device(self.h, _p(o), _dptr(dirs), w, h, quality, _dptr(texture),
+                                                lights.h if lights is not None else None, _dptr(argb), stream),
+              "vox_cuda_render_rays_device")
+
     def render_counts_device(self, camera: CameraStruct, w: int, h: int, counts, stream=None):
         check(lib().vox_cuda_render_counts_device(self.h, C.byref(camera), w, h, _dptr(counts), stream),
               "vox_cuda_render_counts_device")

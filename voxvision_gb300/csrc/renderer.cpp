@@ -5,15 +5,23 @@
  * vox_render (renderer.c:200-319) draws a whole frame: the scene tree is
  * uploaded once per vox_context_set_scene, the camera state is read from the
  * built-in camera object, and one fused kernel draws the ARGB frame straight
- * into the context's page-locked frame.  vox_redraw (renderer.c:321-327)
+ * into the context's page-locked frame.  A camera of any other class (one
+ * whose iface is not the built-in simple or doom camera's) is asked for every
+ * pixel's direction through its own screen2world on the host threads, as the
+ * reference's tasks ask it, and the frame is drawn from that ray buffer.
+ * vox_redraw (renderer.c:321-327)
  * then brings the frame to the host buffer returned by vox_context_pixels.  Instead of an SDL
  * surface the context owns a headless frame.
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "../../include/voxrnd.h"
 #include "../../include/voxtrees_cuda.h"
@@ -46,6 +54,8 @@ struct vox_rnd_ctx {
     struct vox_light_manager *lights = nullptr;    // renderer.h:66
     vox_cuda_lights *d_lights = nullptr;           // its device copy
     uint64_t d_lights_version = 0;                 // the manager's version that copy holds
+    float *h_rays = nullptr;                       // pixel directions of a host-computed camera (pinned)
+    float *d_rays = nullptr;                       // their device copy
 };
 
 namespace {
@@ -72,8 +82,41 @@ void release(vox_rnd_ctx *c)
     if (c->d_tex) cudaFree(c->d_tex);
     if (c->d_frame) cudaFree(c->d_frame);
     if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->h_rays) cudaFreeHost(c->h_rays);
+    if (c->d_rays) cudaFree(c->d_rays);
     if (c->stream) cudaStreamDestroy(c->stream);
     std::free(c->pixels);
+}
+
+// Every pixel's direction from the camera's own screen2world, rows dealt to
+// the host threads (the reference calls it from its parallel tasks too), then
+// copied to the device on the context's stream.
+int fill_rays(vox_rnd_ctx *c)
+{
+    const size_t n = (size_t)c->w * c->h * 3;
+    if (!c->h_rays && cudaMallocHost(&c->h_rays, n * sizeof(float)) != cudaSuccess) {
+        c->h_rays = nullptr;
+        return VOX_CUDA_ENOMEM;
+    }
+    if (!c->d_rays && cudaMalloc(&c->d_rays, n * sizeof(float)) != cudaSuccess) {
+        c->d_rays = nullptr;
+        return VOX_CUDA_ENOMEM;
+    }
+    struct vox_camera *cam = c->camera;
+    std::atomic<unsigned int> next{0};
+    auto rows = [&]() {
+        for (unsigned int y; (y = next.fetch_add(1)) < c->h;)
+            for (unsigned int x = 0; x < c->w; x++)
+                cam->iface->screen2world(cam, c->h_rays + 3 * ((size_t)y * c->w + x), (int)x, (int)y);
+    };
+    unsigned int nt = std::min(std::max(1u, std::thread::hardware_concurrency()), std::max(1u, c->h / 16));
+    std::vector<std::thread> pool;
+    for (unsigned int i = 1; i < nt; i++) pool.emplace_back(rows);
+    rows();
+    for (auto &th : pool) th.join();
+    if (cudaMemcpyAsync(c->d_rays, c->h_rays, n * sizeof(float), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+        return VOX_CUDA_ECUDA;
+    return VOX_CUDA_OK;
 }
 
 }  // namespace
@@ -153,8 +196,7 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
     std::memset(&cam, 0, sizeof cam);
     int kind = vox_camera_gpu_state(ctx->camera, cam.position, cam.rotation, &cam.mul, &cam.xsub, &cam.ysub,
                                     &cam.sinphi, &cam.cosphi, &cam.k);
-    if (kind < 0) return;   // only the built-in camera classes run on the GPU
-    cam.kind = kind;
+    cam.kind = kind;        // < 0: a class the device cannot compute
     if (!ctx->tree) {
         int rc = vox_cuda_tree_upload(ctx->scene, &ctx->tree);
         if (rc) { ctx->status = rc; return; }
@@ -179,8 +221,21 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
     // can address it (its stores cross the host link while the frame is
     // traced; no copy follows), else into device memory and copied
     uint32_t *target = ctx->d_stage ? ctx->d_stage : ctx->d_frame;
-    int rc = vox_cuda_render_lit_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
-                                        ctx->lights ? ctx->d_lights : nullptr, target, ctx->stream);
+    const vox_cuda_lights *lights = ctx->lights ? ctx->d_lights : nullptr;
+    int rc;
+    if (kind < 0) {
+        // the previous frame's directions may still be in use: wait for it first
+        if (ctx->h_rays && cudaStreamSynchronize(ctx->stream) != cudaSuccess) { ctx->status = VOX_CUDA_ECUDA; return; }
+        rc = fill_rays(ctx);
+        if (rc) { ctx->status = rc; return; }
+        vox_dot origin;
+        ctx->camera->iface->get_position(ctx->camera, origin);   // renderer.c:231
+        rc = vox_cuda_render_rays_device(ctx->tree, origin, ctx->d_rays, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
+                                         lights, target, ctx->stream);
+    } else {
+        rc = vox_cuda_render_lit_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex, lights, target,
+                                        ctx->stream);
+    }
     if (rc) { ctx->status = rc; return; }
     size_t bytes = (size_t)ctx->w * ctx->h * 4;
     if ((!ctx->d_stage &&

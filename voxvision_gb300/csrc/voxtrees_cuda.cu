@@ -208,12 +208,28 @@ __device__ __forceinline__ float sqr3(float ax, float ay, float az, float bx, fl
     return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
 }
 
-template <int CAP>
+// The direction of pixel (x, y): the camera's screen2world, or with RAYS the
+// pixel's entry of a ray buffer (3 floats a pixel, rows of w pixels) that the
+// host filled through a camera class the device cannot compute.
+template <bool RAYS>
+__device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const float *__restrict__ rays, uint32_t w,
+                                          int x, int y, float &dx, float &dy, float &dz)
+{
+    if (RAYS) {
+        const float *r = rays + 3 * ((size_t)y * w + (uint32_t)x);
+        dx = r[0]; dy = r[1]; dz = r[2];
+    } else {
+        vox::screen2world(cam, x, y, dx, dy, dz);
+    }
+}
+
+template <int CAP, bool RAYS>
 __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
                                                              uint32_t h, unsigned int quality,
                                                              const uint8_t *__restrict__ tex,
                                                              uint32_t *__restrict__ argb,
-                                                             uint32_t *__restrict__ status, vox::DevLights lights)
+                                                             uint32_t *__restrict__ status, vox::DevLights lights,
+                                                             const float *__restrict__ rays)
 {
     const int order[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};   // renderer.c:23-25
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -242,7 +258,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
         block_merge = (merge_mode == VOX_CUDA_QUALITY_RAY_MERGE);
         istart = 1;
         float d1x, d1y, d1z;
-        vox::screen2world(cam, xstart, ystart, d1x, d1y, d1z);
+        pixel_dir<RAYS>(cam, rays, w, xstart, ystart, d1x, d1y, d1z);
         RayHit h1;
         bool c1 = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d1x, d1y, d1z, h1, c, overflow);
         block_mode = VOX_CUDA_QUALITY_FAST;
@@ -253,7 +269,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
             iend = 15;
             out[0] = vox::hit_color(tex, t, lights, h1.x, h1.y, h1.z, overflow);
             float d2x, d2y, d2z;
-            vox::screen2world(cam, xstart + 3, ystart + 3, d2x, d2y, d2z);
+            pixel_dir<RAYS>(cam, rays, w, xstart + 3, ystart + 3, d2x, d2y, d2z);
             RayHit h2;
             bool c2 = vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d2x, d2y, d2z, h2, c, overflow);
             if (c2) {
@@ -279,7 +295,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
         int py = p >> 2, px = p & 3;
         bool merge = block_merge && (i & 1);
         float dx, dy, dz;
-        vox::screen2world(cam, px + xstart, py + ystart, dx, dy, dz);
+        pixel_dir<RAYS>(cam, rays, w, px + xstart, py + ystart, dx, dy, dz);
         if (!merge) {
             RayHit hh;
             if (block_mode == VOX_CUDA_QUALITY_FAST) {
@@ -412,19 +428,23 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
     return cudaGetLastError();
 }
 
+// FAST / ADAPTIVE frames, and with a ray buffer frames of every quality.
 cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s,
-                                  const vox::DevLights *lights = nullptr)
+                                  const vox::DevLights *lights = nullptr, const float *rays = nullptr)
 {
     uint32_t ws = w / 4, hs = h / 4;
     dim3 block(128), grid((ws + 15) / 16, (hs + 7) / 8);
     vox::DevLights L{};
     if (lights) L = *lights;
-    switch (t->cap_class) {
-    case 0: render_squares_kernel<CAP0><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L); break;
-    case 1: render_squares_kernel<CAP1><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L); break;
-    default: render_squares_kernel<CAP2><<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L); break;
-    }
+    void (*kern)(DevTree, vox_cuda_camera, uint32_t, uint32_t, unsigned int, const uint8_t *, uint32_t *,
+                 uint32_t *, vox::DevLights, const float *);
+    const int cap = t->cap_class;
+    if (rays) kern = cap == 0 ? render_squares_kernel<CAP0, true>
+                   : cap == 1 ? render_squares_kernel<CAP1, true> : render_squares_kernel<CAP2, true>;
+    else kern = cap == 0 ? render_squares_kernel<CAP0, false>
+              : cap == 1 ? render_squares_kernel<CAP1, false> : render_squares_kernel<CAP2, false>;
+    kern<<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L, rays);
     count_launch();
     return cudaGetLastError();
 }
@@ -1389,6 +1409,27 @@ EXPORT int vox_cuda_render_lit_device(const vox_cuda_tree *t, const vox_cuda_cam
                                       uint32_t *argb, void *stream)
 {
     return render_any_device(t, cam, w, h, quality, tex, lights, argb, stream);
+}
+
+/* vox_render for a camera class the device cannot compute (renderer.c:200-319
+ * with camera->iface->screen2world run by the caller): each pixel's direction
+ * is read from `dirs` (device memory, 3 floats a pixel, row by row), all rays
+ * start at `origin`.  Every quality is drawn in 4x4 squares as the reference
+ * draws them. */
+EXPORT int vox_cuda_render_rays_device(const vox_cuda_tree *t, const float *origin, const float *dirs, uint32_t w,
+                                       uint32_t h, unsigned int quality, const uint8_t *tex,
+                                       const vox_cuda_lights *lights, uint32_t *argb, void *stream)
+{
+    if (!origin || !dirs) return VOX_CUDA_EINVAL;
+    vox_cuda_camera cam;
+    std::memset(&cam, 0, sizeof cam);
+    cam.kind = VOX_CUDA_CAMERA_SIMPLE;   // only its position is read
+    for (int a = 0; a < 3; a++) cam.position[a] = origin[a];
+    int rc = check_render_args(t, &cam, w, h, tex, argb);
+    if (rc) return rc;
+    if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
+    return status_of(launch_render_squares(t, cam, w, h, quality, tex, argb, as_stream(stream),
+                                           lights ? &lights->dev : nullptr, dirs));
 }
 
 static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
