@@ -50,6 +50,7 @@ extern "C" {
 #define VOX_CUDA_ETIMEOUT   -9   /* a bounded wait gave up                         */
 #define VOX_CUDA_ENODEV    -10   /* no usable CUDA device                          */
 #define VOX_CUDA_ECAPACITY -11   /* request larger than a fixed-capacity entry point */
+#define VOX_CUDA_ERANGE    -12   /* checked build: a search met an index outside the tree */
 
 #define VOX_CUDA_MISS       0xFFFFFFFFu
 #define VOX_CUDA_SLOT_DENSE 0xFFu
@@ -458,6 +459,13 @@ int vox_cuda_server_replay(vox_cuda_server *srv, const vox_cuda_replay_request *
  * process (all entry points); used to report launch counts. */
 const char *vox_cuda_version(void);
 uint64_t vox_cuda_launch_count(void);
+
+/* 1 in the checked build (libvoxtrees_cuda_checked.so, compiled with
+ * -DVOX_CUDA_CHECKED): every search load first checks its index against the
+ * uploaded tree and light arrays, and a search that meets an index outside
+ * them ends with VOX_CUDA_ERANGE instead of reading; 0 in the normal build,
+ * which relies on the upload-time validation of the tree image. */
+int vox_cuda_build_checked(void);
 
 #ifdef __cplusplus
 }

@@ -10,7 +10,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libvoxtrees_cuda.so")
+# VOXTREES_CUDA_LIB selects another build of the library (the checked one).
+LIB_PATH = os.environ.get("VOXTREES_CUDA_LIB") or os.path.join(HERE, "libvoxtrees_cuda.so")
 
 VOX_CUDA_MISS = 0xFFFFFFFF
 VOX_CUDA_SLOT_DENSE = 0xFF
@@ -135,6 +136,7 @@ SIGNATURES = {
     "vox_cuda_render_lit": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp, _vp, _vp, _vp]),
     "vox_cuda_render_lit_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp, _vp, _vp,
                                              _vp]),
+    "vox_cuda_build_checked": (C.c_int, []),
     "vox_cuda_render_rays_device": (C.c_int, [_vp, _vp, _vp, _u32, _u32, C.c_uint, _vp, _vp, _vp, _vp]),
     "vox_cuda_batch_create": (C.c_int, [C.POINTER(FrameJob), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
     "vox_cuda_batch_set_camera": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct)]),

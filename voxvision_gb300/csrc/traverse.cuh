@@ -10,6 +10,13 @@
  *
  * Recursion becomes an explicit per-thread stack of pending tasks {record
  * offset, ray origin} (see trace_ray).
+ *
+ * Checked build (-DVOX_CUDA_CHECKED, libvoxtrees_cuda_checked.so): every
+ * load from the tree image and the light tree first proves its index inside
+ * the uploaded arrays; an index outside marks the tree's status word with
+ * VOX_STATUS_RANGE and ends that search as an error instead of reading.  It
+ * stands in for a memory checker on the search kernels; the normal build
+ * relies on the upload-time validation of the image instead.
  */
 #ifndef VOX_TRAVERSE_CUH
 #define VOX_TRAVERSE_CUH
@@ -29,11 +36,33 @@ struct DevTree {
     uint32_t n_nodes;
     float vx, vy, vz;            // vox_voxel at upload time
     uint32_t max_steps;          // nodes + voxels: no search takes more loop steps
+    uint32_t n_units;            // 16-byte units in the image (pool)
+    uint32_t *fault;             // the tree's status word (checked build only)
 };
 
 struct Counts {
     uint32_t nodes, inner, voxels;
 };
+
+// Status word bits: a search ran out of stack or steps; (checked build) an
+// index outside the uploaded arrays.
+constexpr uint32_t VOX_STATUS_STACK = 1u, VOX_STATUS_RANGE = 2u;
+
+#ifdef VOX_CUDA_CHECKED
+constexpr bool CHECKED = true;
+#else
+constexpr bool CHECKED = false;
+#endif
+
+// Units [at, at + span) lie in an array of n units; without the checked
+// build always true (and compiled away).  Marks `fault` when not.
+__device__ __forceinline__ bool in_range(uint64_t at, uint32_t span, uint64_t n, uint32_t *fault)
+{
+    if (!CHECKED) return true;
+    if (at + span <= n) return true;
+    if (fault) atomicOr(fault, VOX_STATUS_RANGE);
+    return false;
+}
 
 __device__ __forceinline__ float ubf(uint32_t u) { return __uint_as_float(u); }
 
@@ -232,6 +261,8 @@ __device__ __forceinline__ int ray_step(const DevTree &t, RaySearch &s, uint4 (&
     if (++s.steps > t.max_steps) return STEP_ERROR;
     const uint4 *pool = t.pool;
     const float dx = s.dx, dy = s.dy, dz = s.dz;
+    if (!in_range(s.scan ? (uint64_t)s.cur + s.vi : s.cur, s.scan ? 1u : VOXP_REC_UNITS, t.n_units, t.fault))
+        return STEP_ERROR;
     uint4 u0 = ld16(pool + (s.scan ? s.cur + s.vi : s.cur));
     uint4 u1 = make_uint4(0u, 0u, 0u, 0u), u2 = make_uint4(0u, 0u, 0u, 0u);
     if (!s.scan) {
@@ -365,6 +396,7 @@ __device__ __forceinline__ bool trace_ball(const DevTree &t, float cx, float cy,
     uint32_t steps = 0;
     for (;;) {
         if (++steps > t.max_steps) { overflow = true; return false; }   // damaged pool
+        if (!in_range(cur, 2, t.n_units, t.fault)) { overflow = true; return false; }
         uint4 a = ld16(pool + cur);
         uint4 b = ld16(pool + cur + 1);
         if (COUNT) cnt.nodes++;
@@ -373,6 +405,7 @@ __device__ __forceinline__ bool trace_ball(const DevTree &t, float cx, float cy,
             if (kind == VOXP_KIND_DENSE) return true;
             if (kind == VOXP_KIND_LEAF) {
                 uint32_t n = b.z >> 2;
+                if (!in_range(link, n, t.n_units, t.fault)) { overflow = true; return false; }
                 for (uint32_t i = 0; i < n; i++) {
                     uint4 v = ld16(pool + link + i);
                     if (COUNT) cnt.voxels++;
@@ -449,6 +482,7 @@ struct DevLights {
     const float4 *spheres;   // 2 per light sphere
     float ar, ag, ab;        // ambient light
     uint32_t on;             // 0: draw without lights (grey texels)
+    uint32_t n_nodes, n_spheres;
 };
 
 constexpr int LIGHT_STACK = 64;   // (children - 1) per level; the upload refuses deeper trees
@@ -478,7 +512,7 @@ __device__ __forceinline__ void add_light(const float4 &sa, const float4 &sb, fl
  * without a second test), then min(light, 1) * texel per channel, truncated
  * to 8 bits.  `overflow` is set if the search stack would overflow. */
 __device__ __forceinline__ uint32_t lit_color(const DevLights &L, uint32_t c, float px, float py, float pz,
-                                              bool &overflow)
+                                              bool &overflow, uint32_t *fault)
 {
     float r = L.ar, g = L.ag, b = L.ab;
     if (L.nodes) {
@@ -486,12 +520,14 @@ __device__ __forceinline__ uint32_t lit_color(const DevLights &L, uint32_t c, fl
         int sp = 0;
         uint32_t cur = 0;
         for (;;) {
+            if (!in_range(cur, 1, L.n_nodes, fault)) { overflow = true; break; }
             float4 na = L.nodes[2 * cur];
             float4 nb = L.nodes[2 * cur + 1];
             uint32_t leaf = __float_as_uint(nb.x), num = __float_as_uint(nb.y), first = __float_as_uint(nb.z);
             bool next_from_stack = true;
             if (sqr_dist(na.x, na.y, na.z, px, py, pz) < na.w) {
                 if (leaf) {
+                    if (!in_range(first, num, L.n_spheres, fault)) { overflow = true; break; }
                     if (num == 1) {
                         add_light(L.spheres[2 * first], L.spheres[2 * first + 1], px, py, pz, r, g, b);
                     } else {
@@ -530,7 +566,7 @@ __device__ __forceinline__ uint32_t hit_color(const uint8_t *__restrict__ tex, c
     int iz = abs(__float2int_rz(__fdiv_rn(z, t.vz))) & 31;
     uint32_t c = __ldg(tex + ix * 1024 + iy * 32 + iz);
     if (!L.on) return 0xFF000000u | (c << 16) | (c << 8) | c;
-    return lit_color(L, c, x, y, z, overflow);
+    return lit_color(L, c, x, y, z, overflow, t.fault);
 }
 
 }  // namespace vox

@@ -450,6 +450,12 @@ cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera 
 }
 
 
+// The error a nonzero status word reports.
+int status_error(uint32_t st)
+{
+    return (st & vox::VOX_STATUS_RANGE) ? VOX_CUDA_ERANGE : VOX_CUDA_ESTACK;
+}
+
 // Reads and clears the tree's overflow flag after a synchronous call.
 int check_tree_status(const vox_cuda_tree *t, cudaStream_t s)
 {
@@ -459,7 +465,7 @@ int check_tree_status(const vox_cuda_tree *t, cudaStream_t s)
     if (st) {
         cudaMemsetAsync(t->d_status, 0, 4, s);
         cudaStreamSynchronize(s);
-        return VOX_CUDA_ESTACK;
+        return status_error(st);
     }
     return VOX_CUDA_OK;
 }
@@ -660,11 +666,14 @@ EXPORT const char *vox_cuda_strerror(int code)
     case VOX_CUDA_ETIMEOUT: return "bounded wait timed out";
     case VOX_CUDA_ENODEV: return "no CUDA device";
     case VOX_CUDA_ECAPACITY: return "request exceeds the entry point's fixed capacity";
+    case VOX_CUDA_ERANGE: return "a search met an index outside the uploaded tree (checked build)";
     default: return "unknown error";
     }
 }
 
 EXPORT const char *vox_cuda_version(void) { return "voxtrees_cuda 0.1 (sm_103a)"; }
+
+EXPORT int vox_cuda_build_checked(void) { return vox::CHECKED ? 1 : 0; }
 
 EXPORT uint64_t vox_cuda_launch_count(void) { return g_launches.load(); }
 
@@ -736,6 +745,8 @@ static int load_tree(vox_cuda_tree *t, const struct vox_node *root)
     t->dev.vz = flat.voxel[2];
     uint64_t steps = (uint64_t)nodes + flat.n_dots + 2;
     t->dev.max_steps = steps > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)steps;
+    t->dev.n_units = (uint32_t)units;
+    t->dev.fault = t->d_status;
     t->n_nodes = nodes;
     t->n_units = flat.units.size();
     // The flattened image is on the device now; keep only the maps.
@@ -788,6 +799,8 @@ int adopt_image(vox_cuda_tree *t, uint4 *pool, size_t pool_bytes, uint32_t *map,
     t->dev.vz = st.voxel[2];
     uint64_t steps = st.nodes + st.dots + 2;
     t->dev.max_steps = steps > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)steps;
+    t->dev.n_units = (uint32_t)(empty ? VOXP_REC_UNITS : st.units);
+    t->dev.fault = t->d_status;
     t->n_nodes = st.nodes;
     t->n_units = empty ? 0 : st.units;
     FlatTree f;
@@ -1209,7 +1222,7 @@ static int host_call_finish(HostCallState *hc, const vox_cuda_tree *t, cudaStrea
     if (*hc->h_status) {
         cudaMemsetAsync(t->d_status, 0, 4, s);
         cudaStreamSynchronize(s);
-        return VOX_CUDA_ESTACK;
+        return status_error(*hc->h_status);
     }
     return VOX_CUDA_OK;
 }
@@ -1501,6 +1514,8 @@ EXPORT int vox_cuda_lights_upload(const struct vox_light_manager *lm, vox_cuda_l
         if (e == cudaSuccess) e = cudaStreamSynchronize(cudaStreamLegacy);
         l->dev.nodes = l->d_nodes;
         l->dev.spheres = l->d_spheres;
+        l->dev.n_nodes = (uint32_t)img.n_nodes;
+        l->dev.n_spheres = (uint32_t)img.n_spheres;
     }
     lights_image_free(&img);
     if (e != cudaSuccess) {
