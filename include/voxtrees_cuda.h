@@ -377,17 +377,18 @@ int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njob
  * resident trees, admitted by memory budgets and batched continuously:
  * everything admitted since the previous launch goes out in the next one, on
  * the next of several streams, so requests that arrive while others run
- * overlap with them on the device.  Results are written by the kernels in
- * place into pinned host memory (no device buffer, no copy per request).
- * The device budget holds the resident trees and the per-launch job tables
- * (256 bytes per frame); the pinned-host budget holds each admitted
- * request's result (w*h*4 bytes, or n) and staged ball inputs (16 bytes per
- * ball), in power-of-two size classes from 4 KiB.  Each result equals the
- * plain entry point's for the same request alone.
+ * overlap with them on the device.  Frames are drawn into device memory and
+ * copied into pinned host memory after their launch's kernel; ball hits are
+ * written there in place.  The device budget holds the resident trees, the
+ * per-launch job tables (256 bytes per frame) and the frames being drawn
+ * (w*h*4 bytes); the pinned-host budget holds each admitted request's result
+ * (w*h*4 bytes, or n) and staged ball inputs (16 bytes per ball), in
+ * power-of-two size classes from 4 KiB.  Each result equals the plain entry
+ * point's for the same request alone.
  * Replaces: applications calling vox_render / vox_tree_ball_collidep from
  * many threads (renderer.h:208 is callable from any thread). */
 typedef struct {
-    uint64_t budget_bytes;       /* device bytes for resident trees + job tables      */
+    uint64_t budget_bytes;       /* device bytes: resident trees, job tables, frames  */
     uint64_t host_budget_bytes;  /* pinned host bytes for results and staged inputs   */
     uint32_t max_inflight;   /* requests admitted at once                         */
     uint32_t max_batch;      /* requests per launch (1..1024)                     */
@@ -428,6 +429,21 @@ int vox_cuda_server_release(vox_cuda_server *srv, uint64_t ticket);
 int vox_cuda_server_get_stats(vox_cuda_server *srv, vox_cuda_server_stats *stats);
 /* Finish all queued requests, then stop. */
 int vox_cuda_server_destroy(vox_cuda_server *srv);
+
+/* Host-side fault injection, for tests of the server's failure handling (no
+ * GPU fault is made; the reference has no counterpart).  The fault hits the
+ * next launch the server builds:
+ *   VOX_CUDA_INJECT_REQUEST_ERROR: its requests end with VOX_CUDA_ECUDA, as if
+ *     their enqueue had failed; later requests are served as usual.
+ *   VOX_CUDA_INJECT_WORKER_FAILURE: building it throws an allocation failure
+ *     in the server's worker.  The worker waits for the launches in flight
+ *     (their requests keep their results), ends every other request with
+ *     VOX_CUDA_ENOMEM and stops; later submissions return VOX_CUDA_ENOMEM and
+ *     vox_cuda_server_destroy still frees everything.  A real allocation
+ *     failure in the worker takes the same path. */
+#define VOX_CUDA_INJECT_REQUEST_ERROR  1
+#define VOX_CUDA_INJECT_WORKER_FAILURE 2
+int vox_cuda_server_inject(vox_cuda_server *srv, int what);
 
 /* Replay a request trace against a server, for capacity measurements (no
  * counterpart in the reference).  Requests are submitted from the calling

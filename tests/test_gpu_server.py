@@ -167,3 +167,75 @@ def test_replay_serves_a_poisson_trace(setup):
     st = srv.stats()
     assert st["completed"] == st["submitted"] == len(reqs)
     srv.close()
+
+
+def _frame_request(wl, w=160, h=120, az=0.7):
+    from voxvision_gb300.cameras import HostCamera
+    cam = HostCamera(0)
+    cam.set_window_size(w, h)
+    cam.set_position(wl.pose_position((32.0,) * 3, 1.5 * 64 * 3 ** 0.5, az, 20.0))
+    cam.look_at((32.0,) * 3)
+    return ("frame", 0, cam.gpu_struct(), w, h)
+
+
+def test_injected_request_error_spares_other_requests(setup):
+    """A launch whose enqueue fails (a host-side injected fault) ends its own
+    requests with VOX_CUDA_ECUDA; the requests before and after it are
+    served exactly, and the server's accounting stays whole."""
+    vg, wl, hosts, trees, tex = setup
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, 1 << 30, 16, 4, 1, 1))
+    ids = [srv.add_tree(t) for t in trees]
+    req = _frame_request(wl)
+    expect = _alone(trees, tex, req)
+    t0 = srv.submit_frame(ids[0], req[2], req[3], req[4])
+    assert srv.wait(t0) == 0
+    srv.inject(1)
+    t1 = srv.submit_frame(ids[0], req[2], req[3], req[4])
+    assert srv.wait(t1) == -3
+    with pytest.raises(vg.VoxCudaError) as e:
+        srv.result(t1)
+    assert e.value.code == -3
+    srv.release(t1)
+    t2 = srv.submit_frame(ids[0], req[2], req[3], req[4])
+    c, r = wl.balls(5000, 0.0, 64.0, 0.5, 8.0, 77)
+    t3 = srv.submit_balls(ids[0], c, r)
+    assert srv.wait(t2) == 0 and srv.wait(t3) == 0
+    for t in (t0, t2):
+        assert np.array_equal(srv.result(t)[0], expect)
+    assert np.array_equal(srv.result(t3)[0], trees[0].balls(c, r))
+    for t in (t0, t2, t3):
+        srv.release(t)
+    st = srv.stats()
+    assert st["submitted"] == st["completed"] == 4
+    assert st["inflight"] == 0 and st["pending"] == 0
+    srv.close()
+
+
+def test_injected_worker_failure_ends_requests_and_refuses_new_ones(setup):
+    """An allocation failure in the server's worker (injected on the host):
+    the requests it had not launched end with VOX_CUDA_ENOMEM instead of
+    hanging their waiters, later submissions are refused with
+    VOX_CUDA_ENOMEM, finished results stay readable and the server is
+    destroyed cleanly."""
+    vg, wl, hosts, trees, tex = setup
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, 1 << 30, 16, 4, 1, 1))
+    ids = [srv.add_tree(t) for t in trees]
+    resident = srv.stats()["bytes_in_use"]          # the trees
+    req = _frame_request(wl, az=2.0)
+    t0 = srv.submit_frame(ids[0], req[2], req[3], req[4])
+    assert srv.wait(t0) == 0
+    srv.inject(2)
+    pending = [srv.submit_frame(ids[0], req[2], req[3], req[4]) for _ in range(3)]
+    for t in pending:
+        assert srv.wait(t, 20000) == -2
+    with pytest.raises(vg.VoxCudaError) as e:
+        srv.submit_frame(ids[0], req[2], req[3], req[4])
+    assert e.value.code == -2
+    assert np.array_equal(srv.result(t0)[0], _alone(trees, tex, req))
+    for t in [t0] + pending:
+        srv.release(t)
+    st = srv.stats()
+    assert st["submitted"] == st["completed"] == 4
+    assert st["inflight"] == 0 and st["pending"] == 0
+    assert st["bytes_in_use"] == resident and st["host_bytes_in_use"] == 0
+    srv.close()

@@ -492,6 +492,11 @@ class Server:
     def release(self, ticket: int):
         check(lib().vox_cuda_server_release(self.h, ticket), "vox_cuda_server_release")
 
+    def inject(self, what: int):
+        """vox_cuda_server_inject: a host-side fault for the next launch
+        (1: its requests fail, 2: the worker fails)."""
+        check(lib().vox_cuda_server_inject(self.h, what), "vox_cuda_server_inject")
+
     def replay(self, requests, collectors: int = 8):
         """vox_cuda_server_replay over a trace: a list of ("frame", tree_id,
         camera, w, h, arrival_s) and ("balls", tree_id, centres, radii,

@@ -137,6 +137,7 @@ SIGNATURES = {
     "vox_cuda_render_lit_device": (C.c_int, [_vp, C.POINTER(CameraStruct), _u32, _u32, C.c_uint, _vp, _vp, _vp,
                                              _vp]),
     "vox_cuda_build_checked": (C.c_int, []),
+    "vox_cuda_server_inject": (C.c_int, [_vp, C.c_int]),
     "vox_cuda_render_rays_device": (C.c_int, [_vp, _vp, _vp, _u32, _u32, C.c_uint, _vp, _vp, _vp, _vp]),
     "vox_cuda_batch_create": (C.c_int, [C.POINTER(FrameJob), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
     "vox_cuda_batch_set_camera": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct)]),

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "abi_guard.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -366,7 +367,7 @@ void release(vox_cuda_batch *b)
 
 EXPORT int vox_cuda_batch_create(const vox_cuda_frame_job *jobs, uint32_t njobs,
                                  const vox_cuda_batch_config *config, vox_cuda_batch **out)
-{
+try {
     if (!out || !jobs || njobs == 0 || njobs > MAX_JOBS) return VOX_CUDA_EINVAL;
     *out = nullptr;
     for (uint32_t i = 0; i < njobs; i++) {
@@ -409,10 +410,10 @@ EXPORT int vox_cuda_batch_create(const vox_cuda_frame_job *jobs, uint32_t njobs,
     }
     *out = b;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_batch_set_camera(vox_cuda_batch *b, uint32_t job, const vox_cuda_camera *camera)
-{
+try {
     if (!b || !camera || job >= b->jobs.size()) return VOX_CUDA_EINVAL;
     if (camera->kind != VOX_CUDA_CAMERA_SIMPLE && camera->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
     // the frame's rectangle, and with it every later frame's queue range,
@@ -420,10 +421,10 @@ EXPORT int vox_cuda_batch_set_camera(vox_cuda_batch *b, uint32_t job, const vox_
     b->jobs[job].camera = *camera;
     fill_table(b);
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_batch_launch(vox_cuda_batch *b, void *stream)
-{
+try {
     if (!b || !b->exec) return VOX_CUDA_EINVAL;
     // The graph reads h_stage when it runs: wait for the previous replay before
     // refreshing it with the current cameras.
@@ -435,26 +436,26 @@ EXPORT int vox_cuda_batch_launch(vox_cuda_batch *b, void *stream)
     if (cudaEventRecord(b->done, s) != cudaSuccess) return VOX_CUDA_ECUDA;
     b->launched = true;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_batch_get_config(const vox_cuda_batch *b, vox_cuda_batch_config *config)
-{
+try {
     if (!b || !config) return VOX_CUDA_EINVAL;
     *config = b->cfg;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_batch_set_config(vox_cuda_batch *b, const vox_cuda_batch_config *config)
-{
+try {
     if (!b || !config || !valid_config(*config)) return VOX_CUDA_EINVAL;
     if (b->launched && cudaEventSynchronize(b->done) != cudaSuccess) return VOX_CUDA_ECUDA;
     b->cfg = *config;
     return build_graph(b);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_batch_autotune(vox_cuda_batch *b, void *stream, uint32_t reps,
                                    vox_cuda_batch_config *chosen, float *best_ms)
-{
+try {
     if (!b) return VOX_CUDA_EINVAL;
     if (reps == 0) reps = 3;
     cudaStream_t s = as_stream(stream);
@@ -496,16 +497,16 @@ out:
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_batch_free(vox_cuda_batch *b)
-{
+try {
     if (!b) return VOX_CUDA_EINVAL;
     if (b->launched) cudaEventSynchronize(b->done);
     release(b);
     delete b;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 /* ---------------------------------------------------------------------------
  * Frames without any allocation.
@@ -573,7 +574,7 @@ void launch_noalloc(const BatchHead *table, uint32_t *head, int nsm, cudaStream_
 }  // namespace
 
 EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njobs, void *stream)
-{
+try {
     if (!jobs || njobs == 0) return VOX_CUDA_EINVAL;
     if (njobs > VOX_CUDA_NOALLOC_MAX_JOBS) return VOX_CUDA_ECAPACITY;
     int cap = 0;
@@ -623,7 +624,7 @@ EXPORT int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32
     }
     count_launch();
     return status_of(cudaGetLastError());
-}
+} VOX_ABI_FAIL_INT
 
 /* ---------------------------------------------------------------------------
  * Frame jobs for the request server (server.cpp): the batch kernel over a job

@@ -63,6 +63,7 @@
 #include <unistd.h>
 
 #include "internal.h"
+#include "abi_guard.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -1454,13 +1455,13 @@ int build_for_host_tree(const float *set, size_t n, vox_cuda_tree **out, HostTre
 }
 
 EXPORT int vox_cuda_tree_build_device(const float *d_set, size_t n, vox_cuda_tree **out)
-{
+try {
     if (n && !d_set) return VOX_CUDA_EINVAL;
     return new_tree(out, [&](vox_cuda_tree *t, cudaStream_t s) { return build_tree(t, d_set, n, s); });
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_build(const float *set, size_t n, vox_cuda_tree **out)
-{
+try {
     if (n && !set) return VOX_CUDA_EINVAL;
     return new_tree(out, [&](vox_cuda_tree *t, cudaStream_t s) {
         if (n > MAX_VOXELS) return (int)VOX_CUDA_ETOOBIG;
@@ -1473,22 +1474,22 @@ EXPORT int vox_cuda_tree_build(const float *set, size_t n, vox_cuda_tree **out)
         cudaStreamSynchronize(s);
         return rc;
     });
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_build_raw(const void *samples, const unsigned dim[3], unsigned samplesize,
                                    const vox_cuda_raw_test *test, vox_cuda_tree **out)
-{
+try {
     int rc = check_raw_args(dim, samplesize, test);
     if (rc) return rc;
     if (!samples && (uint64_t)dim[0] * dim[1] * dim[2]) return VOX_CUDA_EINVAL;
     return new_tree(out, [&](vox_cuda_tree *t, cudaStream_t s) {
         return raw_build(t, samples, dim, samplesize, test, s);
     });
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_read_raw_data(const char *filename, const unsigned dim[3], unsigned samplesize,
                                   const vox_cuda_raw_test *test, vox_cuda_tree **out, const char **error)
-{
+try {
     if (out) *out = nullptr;
     int rc = check_raw_args(dim, samplesize, test);
     if (rc || !filename || !out) {
@@ -1534,4 +1535,4 @@ EXPORT int vox_cuda_read_raw_data(const char *filename, const unsigned dim[3], u
     if (buf) cudaFreeHost(buf);
     if (rc && error) *error = vox_cuda_strerror(rc);
     return rc;
-}
+} VOX_ABI_FAIL_INT

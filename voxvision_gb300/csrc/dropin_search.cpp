@@ -18,6 +18,7 @@
 
 #include "../../include/voxtrees.h"
 #include "../../include/voxtrees_cuda.h"
+#include "abi_guard.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -75,7 +76,12 @@ bool resolve(const vox_node *node, vox_cuda_tree **tree, uint32_t *id)
     }
     vox_cuda_tree *t = take_prebuilt_usable_locked(node);
     if (!t && tree_upload_flat(node, &t) != VOX_CUDA_OK) return false;
-    g_trees.push_back({node, t});
+    try {
+        g_trees.push_back({node, t});
+    } catch (...) {
+        vox_cuda_tree_free(t);
+        throw;
+    }
     *tree = t;
     *id = 0;
     return true;
@@ -85,7 +91,7 @@ bool resolve(const vox_node *node, vox_cuda_tree **tree, uint32_t *id)
 
 EXPORT const struct vox_node *vox_ray_tree_intersection(const struct vox_node *tree, const vox_dot origin,
                                                         const vox_dot dir, vox_dot res)
-{
+try {
     if (!tree) return nullptr;
     vox_cuda_tree *t;
     uint32_t id;
@@ -94,10 +100,10 @@ EXPORT const struct vox_node *vox_ray_tree_intersection(const struct vox_node *t
     if (vox_cuda_ray_batch(t, origin, dir, id ? &id : nullptr, 1, &leaf, nullptr, res, nullptr) != VOX_CUDA_OK)
         return nullptr;
     return leaf == VOX_CUDA_MISS ? nullptr : vox_cuda_tree_node(t, leaf);
-}
+} VOX_ABI_FAIL_NULL
 
 EXPORT int vox_tree_ball_collidep(const struct vox_node *tree, const vox_dot center, float radius)
-{
+try {
     if (!tree) return 0;
     vox_cuda_tree *t;
     uint32_t id;
@@ -115,10 +121,10 @@ EXPORT int vox_tree_ball_collidep(const struct vox_node *tree, const vox_dot cen
     uint8_t hit = 0;
     if (vox_cuda_ball_batch(t, center, &radius, 1, &hit, nullptr) != VOX_CUDA_OK) return 0;
     return hit;
-}
+} VOX_ABI_FAIL_ZERO
 
 EXPORT void vox_cuda_forget_tree(const struct vox_node *root)
-{
+try {
     std::lock_guard<std::mutex> lock(g_mu);
     if (vox_cuda_tree *p = take_prebuilt_locked(root)) vox_cuda_tree_free(p);
     for (size_t i = 0; i < g_trees.size(); i++) {
@@ -128,13 +134,20 @@ EXPORT void vox_cuda_forget_tree(const struct vox_node *root)
             return;
         }
     }
+} VOX_ABI_FAIL_VOID
+
+// Every cached device copy dropped (g_mu held).
+static void forget_all_locked()
+{
+    for (Entry &e : g_prebuilt) vox_cuda_tree_free(e.tree);
+    for (Entry &e : g_trees) vox_cuda_tree_free(e.tree);
+    g_prebuilt.clear();
+    g_trees.clear();
 }
 
-// Called by the tree-editing functions before they change a tree: a cached
-// device copy of any tree that contains `node` is dropped.
-extern "C" void vox_dropin_forget_containing(const struct vox_node *node)
+// The cached device copies of trees that contain `node` dropped (g_mu held).
+static void forget_containing_locked(const struct vox_node *node)
 {
-    std::lock_guard<std::mutex> lock(g_mu);
     for (size_t i = 0; i < g_prebuilt.size();) {
         uint32_t id;
         if (vox_cuda_tree_node_id(g_prebuilt[i].tree, node, &id) == VOX_CUDA_OK) {
@@ -157,13 +170,32 @@ extern "C" void vox_dropin_forget_containing(const struct vox_node *node)
     }
 }
 
-// vox_make_tree (make_tree.cpp): keep the device copy of a tree it built on
-// the GPU until the tree's first upload, edit or destruction.
-void dropin_keep_prebuilt(const vox_node *root, vox_cuda_tree *t)
+// Called by the tree-editing functions before they change a tree: a cached
+// device copy of any tree that contains `node` is dropped.  If the node
+// lookup cannot be made (its index could not be allocated), every copy is
+// dropped: a later query uploads again.
+extern "C" void vox_dropin_forget_containing(const struct vox_node *node)
+{
+    std::lock_guard<std::mutex> lock(g_mu);
+    try {
+        forget_containing_locked(node);
+    } catch (...) {
+        forget_all_locked();
+    }
+}
+
+// vox_make_tree (make_tree.cu): keep the device copy of a tree it built on
+// the GPU until the tree's first upload, edit or destruction (or free it, if
+// it cannot be kept: it only saves that upload).
+void dropin_keep_prebuilt(const vox_node *root, vox_cuda_tree *t) noexcept
 {
     std::lock_guard<std::mutex> lock(g_mu);
     if (vox_cuda_tree *old = take_prebuilt_locked(root)) vox_cuda_tree_free(old);
-    g_prebuilt.push_back({root, t});
+    try {
+        g_prebuilt.push_back({root, t});
+    } catch (...) {
+        vox_cuda_tree_free(t);
+    }
 }
 
 // vox_cuda_tree_upload: the kept device copy of `root`, if there is one.

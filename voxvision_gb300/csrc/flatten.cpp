@@ -54,7 +54,11 @@ void parallel_for(size_t n, F f)
         for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
     };
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nt; t++) pool.emplace_back(run);
+    try {
+        for (size_t t = 1; t < nt; t++) pool.emplace_back(run);
+    } catch (...) {
+        // fewer threads: the work is dealt dynamically, the rest do it all
+    }
     run();
     for (auto &th : pool) th.join();
 }

@@ -25,11 +25,12 @@
 #include <vector>
 
 #include "internal.h"
+#include "abi_guard.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
 extern "C" struct vox_node *vox_make_tree_host(vox_dot set[], size_t n);
-void dropin_keep_prebuilt(const vox_node *root, vox_cuda_tree *t);
+void dropin_keep_prebuilt(const vox_node *root, vox_cuda_tree *t) noexcept;
 
 namespace {
 
@@ -61,7 +62,11 @@ void parallel_for(size_t n, F f)
         for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
     };
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nt; t++) pool.emplace_back(run);
+    try {
+        for (size_t t = 1; t < nt; t++) pool.emplace_back(run);
+    } catch (...) {
+        // fewer threads: the work is dealt dynamically, the rest do it all
+    }
     run();
     for (auto &th : pool) th.join();
 }
@@ -91,6 +96,7 @@ vox_node *tree_from_image(const std::vector<uint4_host> &u, const std::vector<ui
     const size_t nodes = rec_of_id.size();
     constexpr size_t CHUNK = 4096;
     const size_t nchunk = (nodes + CHUNK - 1) / CHUNK;
+    pre.reserve(nodes);   // every allocation that may throw comes before the nodes'
     std::vector<uint32_t> id_of_rec(u.size(), 0xFFFFFFFFu);
     for (size_t id = 0; id < nodes; id++) id_of_rec[rec_of_id[id]] = (uint32_t)id;
     std::vector<vox_node *> nd(nodes, nullptr);
@@ -158,26 +164,30 @@ vox_node *tree_from_image(const std::vector<uint4_host> &u, const std::vector<ui
     return nd[0];
 }
 
+// NULL (and nothing left allocated) if any step fails or throws.
 vox_node *make_on_gpu(vox_dot set[], size_t n)
 {
     std::vector<float> order(3 * n);
     HostTreeExtras x;
     x.order = order.data();
-    vox_cuda_tree *t = nullptr;
-    if (build_for_host_tree(&set[0][0], n, &t, &x) != VOX_CUDA_OK) return nullptr;
+    struct Owned {
+        vox_cuda_tree *t = nullptr;
+        ~Owned() { if (t) vox_cuda_tree_free(t); }
+    } own;
+    if (build_for_host_tree(&set[0][0], n, &own.t, &x) != VOX_CUDA_OK) return nullptr;
     size_t nu = 0, ni = 0;
-    vox_cuda_tree_image(t, nullptr, 0, nullptr, 0, &nu, &ni);
+    vox_cuda_tree_image(own.t, nullptr, 0, nullptr, 0, &nu, &ni);
     std::vector<uint4_host> units(nu);
     std::vector<uint32_t> recs(ni);
     std::vector<const vox_node *> pre;
     vox_node *root = nullptr;
     if (ni == x.dots_of_id.size() &&
-        vox_cuda_tree_image(t, units.data(), nu, recs.data(), ni, nullptr, nullptr) == VOX_CUDA_OK)
+        vox_cuda_tree_image(own.t, units.data(), nu, recs.data(), ni, nullptr, nullptr) == VOX_CUDA_OK)
         root = tree_from_image(units, recs, x.dots_of_id, pre);
-    if (!root) {
-        vox_cuda_tree_free(t);
-        return nullptr;
-    }
+    if (!root) return nullptr;
+    // nothing below throws
+    vox_cuda_tree *t = own.t;
+    own.t = nullptr;
     t->flat.preorder = std::move(pre);
     dropin_keep_prebuilt(root, t);
     std::memcpy(set, order.data(), 12 * n);
@@ -189,10 +199,16 @@ vox_node *make_on_gpu(vox_dot set[], size_t n)
 EXPORT size_t vox_cuda_make_tree_gpu_min(size_t n) { return g_gpu_min.exchange(n); }
 
 EXPORT struct vox_node *vox_make_tree(vox_dot set[], size_t n)
-{
+try {
     if (n == 0) return nullptr;
     if (set && n >= g_gpu_min.load() && n <= 0x7FFFFFFFull && have_gpu()) {
-        if (vox_node *root = make_on_gpu(set, n)) return root;
+        vox_node *root = nullptr;
+        try {
+            root = make_on_gpu(set, n);
+        } catch (...) {
+            root = nullptr;   // host memory ran short: the host build may still fit
+        }
+        if (root) return root;
     }
     return vox_make_tree_host(set, n);
-}
+} VOX_ABI_FAIL_NULL

@@ -111,7 +111,11 @@ int fill_rays(vox_rnd_ctx *c)
     };
     unsigned int nt = std::min(std::max(1u, std::thread::hardware_concurrency()), std::max(1u, c->h / 16));
     std::vector<std::thread> pool;
-    for (unsigned int i = 1; i < nt; i++) pool.emplace_back(rows);
+    try {
+        for (unsigned int i = 1; i < nt; i++) pool.emplace_back(rows);
+    } catch (...) {
+        // fewer threads: rows are dealt dynamically, the rest draw them all
+    }
     rows();
     for (auto &th : pool) th.join();
     if (cudaMemcpyAsync(c->d_rays, c->h_rays, n * sizeof(float), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)

@@ -37,6 +37,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -44,6 +45,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "abi_guard.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -158,6 +160,8 @@ struct vox_cuda_server {
     uint32_t inflight_reqs = 0;
     uint32_t building = 0;          // launches being built outside the lock
     bool stop = false;
+    bool failed = false;            // the worker stopped on a failure: requests are refused
+    std::atomic<int> inject{0};     // host-side fault for the next launch (vox_cuda_server_inject)
     std::thread worker;
 };
 
@@ -236,17 +240,31 @@ void release_launch(vox_cuda_server *s, Launch *L)
 // them meanwhile.
 Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cudaStream_t st)
 {
-    Launch *L = new Launch();
+    const int inj = s->inject.exchange(0);
+    if (inj == VOX_CUDA_INJECT_WORKER_FAILURE) throw std::bad_alloc();
+    // every allocation that may throw, before any work is enqueued
+    std::unique_ptr<Launch> own(new Launch());
+    Launch *L = own.get();
     L->srv = s;
     L->stream = st;
     uint64_t t = now_ns();
     std::vector<vox_cuda_frame_job> jobs;
     std::vector<Request *> frames;
     std::vector<size_t> frame_at;   // offset of each frame in the launch's device frames
+    L->reqs.reserve(batch.size());
+    L->host_free.reserve(batch.size());
+    jobs.reserve(batch.size());
+    frames.reserve(batch.size());
+    frame_at.reserve(batch.size());
     size_t frame_bytes = 0;
+    own.release();
     for (Request *r : batch) {
         r->t_launch = t;
         L->reqs.push_back(r);
+        if (inj == VOX_CUDA_INJECT_REQUEST_ERROR) {   // as if this launch's enqueue had failed
+            r->status = VOX_CUDA_ECUDA;
+            continue;
+        }
         size_t out_bytes = r->kind == FRAME ? (size_t)r->w * r->h * 4 : (size_t)r->n;
         r->res_bytes = out_bytes;
         r->h_res = s->pinned.get(out_bytes, &r->h_cls);
@@ -339,11 +357,60 @@ void admit(vox_cuda_server *s)
     }
 }
 
+// The worker met a failure it cannot recover from (an allocation that threw):
+// once every stream's work has ended, each request not yet done ends with
+// VOX_CUDA_ENOMEM -- those of launches that were fully enqueued keep their
+// results -- the budgets are given back, and later submissions are refused.
+void stop_on_failure(vox_cuda_server *s, std::vector<Request *> &batch)
+{
+    for (cudaStream_t st : s->streams) cudaStreamSynchronize(st);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->failed = true;
+    uint64_t t = now_ns();
+    auto end = [&](Request *r, bool charged, bool keep_status) {
+        if (r->done) return;
+        if (!keep_status) r->status = VOX_CUDA_ENOMEM;
+        if (charged) {
+            s->used -= r->dev_bytes;
+            s->host_used -= r->host_bytes;
+            s->inflight_reqs--;
+        }
+        r->t_done = t;
+        r->done = true;
+        s->completed++;
+    };
+    for (Launch *L : s->inflight) {
+        for (Request *r : L->reqs) end(r, true, true);
+        L->finished.store(true);
+    }
+    for (Request *r : batch) end(r, true, false);     // taken for a launch that was never enqueued
+    batch.clear();
+    if (s->building) s->building--;
+    for (Request *r : s->admitted) end(r, true, false);
+    s->admitted.clear();
+    for (Request *r : s->pending) end(r, false, false);
+    s->pending.clear();
+    s->cv_done.notify_all();
+}
+
+void serve(vox_cuda_server *s, std::vector<Launch *> &retired, std::vector<Request *> &batch);
+
 void worker_loop(vox_cuda_server *s)
 {
     cudaSetDevice(s->device);
     std::vector<Launch *> retired;
     std::vector<Request *> batch;
+    try {
+        retired.reserve(s->cfg.max_launches);
+        batch.reserve(s->cfg.max_batch);
+        serve(s, retired, batch);
+    } catch (...) {
+        stop_on_failure(s, batch);
+    }
+}
+
+void serve(vox_cuda_server *s, std::vector<Launch *> &retired, std::vector<Request *> &batch)
+{
     for (;;) {
         cudaStream_t st = nullptr;
         bool quit = false;
@@ -396,7 +463,7 @@ uint64_t request_host_bytes(Kind k, uint64_t a, uint64_t b)
 
 EXPORT int vox_cuda_server_create(const vox_cuda_server_config *config, const uint8_t *texture,
                                   vox_cuda_server **out)
-{
+try {
     if (!out || !texture) return VOX_CUDA_EINVAL;
     *out = nullptr;
     vox_cuda_server_config cfg = {40ull << 30, 16ull << 30, 1024, 256, 4, 8};
@@ -428,29 +495,38 @@ EXPORT int vox_cuda_server_create(const vox_cuda_server_config *config, const ui
         }
         s->streams.push_back(st);
     }
-    s->worker = std::thread(worker_loop, s);
+    try {
+        // the worker's vectors never grow past these while it runs
+        s->admitted.reserve(cfg.max_batch);
+        s->inflight.reserve(cfg.max_launches);
+        s->worker = std::thread(worker_loop, s);
+    } catch (...) {
+        vox_cuda_server_destroy(s);
+        return VOX_CUDA_ENOMEM;
+    }
     *out = s;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_add_tree(vox_cuda_server *s, const vox_cuda_tree *tree, uint32_t *tree_id)
-{
+try {
     if (!s || !tree || !tree_id) return VOX_CUDA_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
     vox_cuda_tree_info info;
     vox_cuda_tree_get_info(tree, &info);
     if (s->used + info.device_bytes > s->cfg.budget_bytes) return VOX_CUDA_EBUDGET;
+    s->trees.push_back(tree);
     s->used += info.device_bytes;          // resident trees count against the budget
     s->tree_bytes += info.device_bytes;
     s->peak = std::max(s->peak, s->used);
-    *tree_id = (uint32_t)s->trees.size();
-    s->trees.push_back(tree);
+    *tree_id = (uint32_t)(s->trees.size() - 1);
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 static int submit(vox_cuda_server *s, Request *r, uint64_t *ticket)
 {
     std::lock_guard<std::mutex> lk(s->mu);
+    if (s->failed) { delete r; return VOX_CUDA_ENOMEM; }
     if (r->tree >= s->trees.size()) { delete r; return VOX_CUDA_EINVAL; }
     if (s->tree_bytes + r->dev_bytes > s->cfg.budget_bytes || r->host_bytes > s->cfg.host_budget_bytes) {
         s->rejected++;
@@ -459,8 +535,19 @@ static int submit(vox_cuda_server *s, Request *r, uint64_t *ticket)
     }
     r->ticket = s->next_ticket++;
     r->t_submit = now_ns();
-    s->reqs[r->ticket] = r;
-    s->pending.push_back(r);
+    try {
+        s->reqs.emplace(r->ticket, r);
+    } catch (...) {
+        delete r;
+        throw;
+    }
+    try {
+        s->pending.push_back(r);
+    } catch (...) {
+        s->reqs.erase(r->ticket);
+        delete r;
+        throw;
+    }
     s->submitted++;
     *ticket = r->ticket;
     s->cv_work.notify_one();
@@ -469,7 +556,7 @@ static int submit(vox_cuda_server *s, Request *r, uint64_t *ticket)
 
 EXPORT int vox_cuda_server_submit_frame(vox_cuda_server *s, uint32_t tree_id, const vox_cuda_camera *camera,
                                         uint32_t w, uint32_t h, uint64_t *ticket)
-{
+try {
     if (!s || !camera || !ticket) return VOX_CUDA_EINVAL;
     if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
     if (camera->kind != VOX_CUDA_CAMERA_SIMPLE && camera->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
@@ -483,11 +570,11 @@ EXPORT int vox_cuda_server_submit_frame(vox_cuda_server *s, uint32_t tree_id, co
     r->dev_bytes = request_bytes(FRAME, w, h);
     r->host_bytes = request_host_bytes(FRAME, w, h);
     return submit(s, r, ticket);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_submit_balls(vox_cuda_server *s, uint32_t tree_id, const float *centres,
                                         const float *radii, uint32_t n, uint64_t *ticket)
-{
+try {
     if (!s || !ticket || n == 0 || !centres || !radii) return VOX_CUDA_EINVAL;
     Request *r = new (std::nothrow) Request();
     if (!r) return VOX_CUDA_ENOMEM;
@@ -499,10 +586,10 @@ EXPORT int vox_cuda_server_submit_balls(vox_cuda_server *s, uint32_t tree_id, co
     r->dev_bytes = request_bytes(BALLS, n, 0);
     r->host_bytes = request_host_bytes(BALLS, n, 0);
     return submit(s, r, ticket);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_wait(vox_cuda_server *s, uint64_t ticket, uint32_t timeout_ms)
-{
+try {
     if (!s) return VOX_CUDA_EINVAL;
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
@@ -511,11 +598,11 @@ EXPORT int vox_cuda_server_wait(vox_cuda_server *s, uint64_t ticket, uint32_t ti
     if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [r] { return r->done; }))
         return VOX_CUDA_ETIMEOUT;
     return r->status;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_result(vox_cuda_server *s, uint64_t ticket, const void **data, size_t *bytes,
                                   uint64_t *times_ns)
-{
+try {
     if (!s) return VOX_CUDA_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
@@ -530,10 +617,10 @@ EXPORT int vox_cuda_server_result(vox_cuda_server *s, uint64_t ticket, const voi
         times_ns[2] = r->t_done;
     }
     return r->status;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_release(vox_cuda_server *s, uint64_t ticket)
-{
+try {
     if (!s) return VOX_CUDA_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
@@ -544,10 +631,18 @@ EXPORT int vox_cuda_server_release(vox_cuda_server *s, uint64_t ticket)
     s->reqs.erase(it);
     delete r;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
+
+EXPORT int vox_cuda_server_inject(vox_cuda_server *s, int what)
+try {
+    if (!s || (what != VOX_CUDA_INJECT_REQUEST_ERROR && what != VOX_CUDA_INJECT_WORKER_FAILURE))
+        return VOX_CUDA_EINVAL;
+    s->inject.store(what);
+    return VOX_CUDA_OK;
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_get_stats(vox_cuda_server *s, vox_cuda_server_stats *st)
-{
+try {
     if (!s || !st) return VOX_CUDA_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
     st->submitted = s->submitted;
@@ -561,10 +656,10 @@ EXPORT int vox_cuda_server_get_stats(vox_cuda_server *s, vox_cuda_server_stats *
     st->host_bytes_in_use = s->host_used;
     st->host_peak_bytes = s->host_peak;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_server_destroy(vox_cuda_server *s)
-{
+try {
     if (!s) return VOX_CUDA_EINVAL;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -572,6 +667,8 @@ EXPORT int vox_cuda_server_destroy(vox_cuda_server *s)
     }
     s->cv_work.notify_one();
     if (s->worker.joinable()) s->worker.join();
+    for (Launch *L : s->inflight) release_launch(s, L);   // left by a worker stopped on a failure
+    s->inflight.clear();
     for (cudaStream_t st : s->streams) {
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
@@ -583,7 +680,7 @@ EXPORT int vox_cuda_server_destroy(vox_cuda_server *s)
     cudaFree(s->d_tex);
     delete s;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 /* ---------------------------------------------------------------------------
  * Trace replay: a request trace submitted at its arrival times from a native
@@ -595,7 +692,7 @@ EXPORT int vox_cuda_server_destroy(vox_cuda_server *s)
 
 EXPORT int vox_cuda_server_replay(vox_cuda_server *s, const vox_cuda_replay_request *reqs, uint32_t n,
                                   uint32_t collectors, vox_cuda_replay_result *out)
-{
+try {
     if (!s || (n && (!reqs || !out)) || collectors == 0 || collectors > 64) return VOX_CUDA_EINVAL;
     for (uint32_t i = 0; i < n; i++) {
         const vox_cuda_replay_request &q = reqs[i];
@@ -632,7 +729,11 @@ EXPORT int vox_cuda_server_replay(vox_cuda_server *s, const vox_cuda_replay_requ
         }
     };
     std::vector<std::thread> pool;
-    for (uint32_t c = 0; c < collectors; c++) pool.emplace_back(collect);
+    try {
+        for (uint32_t c = 0; c < collectors; c++) pool.emplace_back(collect);
+    } catch (...) {
+        // fewer collectors; with none, this thread collects after submitting
+    }
     const uint64_t t0 = now_ns();
     for (uint32_t i = 0; i < n; i++) {
         const vox_cuda_replay_request &q = reqs[i];
@@ -648,6 +749,7 @@ EXPORT int vox_cuda_server_replay(vox_cuda_server *s, const vox_cuda_replay_requ
         if (rc) submit_rc[i].store(rc);
         else tickets[i].store(tk, std::memory_order_release);
     }
+    if (pool.empty()) collect();
     for (auto &th : pool) th.join();
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT

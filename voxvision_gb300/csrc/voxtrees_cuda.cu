@@ -31,6 +31,7 @@
 #include "pool_layout.h"
 #include "traverse.cuh"
 #include "../../include/voxtrees_cuda.h"
+#include "abi_guard.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -652,7 +653,7 @@ void frame_rect_of(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t 
 // ======================================================================== API
 
 EXPORT const char *vox_cuda_strerror(int code)
-{
+try {
     switch (code) {
     case VOX_CUDA_OK: return "ok";
     case VOX_CUDA_EINVAL: return "invalid argument";
@@ -669,7 +670,7 @@ EXPORT const char *vox_cuda_strerror(int code)
     case VOX_CUDA_ERANGE: return "a search met an index outside the uploaded tree (checked build)";
     default: return "unknown error";
     }
-}
+} VOX_ABI_FAIL_NULL
 
 EXPORT const char *vox_cuda_version(void) { return "voxtrees_cuda 0.1 (sm_103a)"; }
 
@@ -828,7 +829,7 @@ bool tree_fits_now(const vox_cuda_tree *t)
 }
 
 EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out)
-{
+try {
     if (!out) return VOX_CUDA_EINVAL;
     if (root) {
         if (vox_cuda_tree *t = dropin_take_prebuilt(root)) {   // built on the GPU by vox_make_tree
@@ -837,7 +838,7 @@ EXPORT int vox_cuda_tree_upload(const struct vox_node *root, vox_cuda_tree **out
         }
     }
     return tree_upload_flat(root, out);
-}
+} VOX_ABI_FAIL_INT
 
 int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
 {
@@ -861,15 +862,15 @@ int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
 }
 
 EXPORT int vox_cuda_tree_refresh(vox_cuda_tree *t, const struct vox_node *root)
-{
+try {
     if (!t) return VOX_CUDA_EINVAL;
     // kernels in flight on any stream may still read the old image
     if (cudaDeviceSynchronize() != cudaSuccess) return VOX_CUDA_ECUDA;
     return load_tree(t, root);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info *info)
-{
+try {
     if (!info) return VOX_CUDA_EINVAL;
     FlatTree f;
     int rc = vox_flatten(root, vox_voxel, &f);
@@ -884,10 +885,10 @@ EXPORT int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info
     info->depth = f.depth;
     info->device_bytes = (f.units.size() ? f.units.size() : VOXP_REC_UNITS) * 16 + 4 * f.preorder.size() + 4;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_free(vox_cuda_tree *t)
-{
+try {
     if (!t) return VOX_CUDA_EINVAL;
     int cur = 0;
     cudaGetDevice(&cur);
@@ -898,10 +899,10 @@ EXPORT int vox_cuda_tree_free(vox_cuda_tree *t)
     if (cur != t->device) cudaSetDevice(cur);
     delete t;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_get_info(const vox_cuda_tree *t, vox_cuda_tree_info *info)
-{
+try {
     if (!t || !info) return VOX_CUDA_EINVAL;
     info->nodes = t->n_nodes;
     info->inner = t->flat.n_inner;
@@ -911,11 +912,11 @@ EXPORT int vox_cuda_tree_get_info(const vox_cuda_tree *t, vox_cuda_tree_info *in
     info->depth = t->flat.depth;
     info->device_bytes = t->pool_bytes + 4 * t->n_nodes + 4;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_image(const vox_cuda_tree *t, void *units, size_t units_cap, uint32_t *rec_of_id,
                                size_t ids_cap, size_t *n_units, size_t *n_ids)
-{
+try {
     if (!t) return VOX_CUDA_EINVAL;
     if (n_units) *n_units = t->n_units;
     if (n_ids) *n_ids = t->n_nodes;
@@ -928,16 +929,16 @@ EXPORT int vox_cuda_tree_image(const vox_cuda_tree *t, void *units, size_t units
         cudaMemcpy(rec_of_id, t->d_rec_of_id, t->n_nodes * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
         return VOX_CUDA_ECUDA;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *t, uint32_t id)
-{
+try {
     if (!t || id >= t->flat.preorder.size()) return nullptr;
     return t->flat.preorder[id];
-}
+} VOX_ABI_FAIL_NULL
 
 EXPORT int vox_cuda_tree_node_id(const vox_cuda_tree *t, const struct vox_node *node, uint32_t *id)
-{
+try {
     if (!t || !id) return VOX_CUDA_EINVAL;
     vox_cuda_tree *m = const_cast<vox_cuda_tree *>(t);
     std::lock_guard<std::mutex> lock(m->index_mu);
@@ -951,20 +952,20 @@ EXPORT int vox_cuda_tree_node_id(const vox_cuda_tree *t, const struct vox_node *
     if (it == m->index.end() || it->first != node) return VOX_CUDA_EINVAL;
     *id = it->second;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_ray_batch_device(const vox_cuda_tree *t, const float *o, const float *d,
                                      const uint32_t *roots, size_t n, uint32_t *leaf, uint8_t *slot,
                                      float *pts, void *stream)
-{
+try {
     if (!t || (n && (!o || !d || !leaf))) return VOX_CUDA_EINVAL;
     return status_of(launch_rays<false>(t, o, d, roots, n, leaf, slot, pts, nullptr, as_stream(stream)));
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_ray_batch(const vox_cuda_tree *t, const float *o, const float *d,
                               const uint32_t *roots, size_t n, uint32_t *leaf, uint8_t *slot,
                               float *pts, void *stream)
-{
+try {
     if (!t || (n && (!o || !d || !leaf))) return VOX_CUDA_EINVAL;
     if (n == 0) return VOX_CUDA_OK;
     cudaStream_t s = as_stream(stream);
@@ -991,18 +992,18 @@ EXPORT int vox_cuda_ray_batch(const vox_cuda_tree *t, const float *o, const floa
     if (e == cudaSuccess && pts) e = cudaMemcpyAsync(pts, d_pts, n * 12, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return VOX_CUDA_ECUDA;
     return check_tree_status(t, s);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_ball_batch_device(const vox_cuda_tree *t, const float *c, const float *r, size_t n,
                                       uint8_t *hit, void *stream)
-{
+try {
     if (!t || (n && (!c || !r || !hit))) return VOX_CUDA_EINVAL;
     return status_of(launch_balls<false>(t, c, r, n, hit, nullptr, as_stream(stream)));
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_ball_batch(const vox_cuda_tree *t, const float *c, const float *r, size_t n,
                                uint8_t *hit, void *stream)
-{
+try {
     if (!t || (n && (!c || !r || !hit))) return VOX_CUDA_EINVAL;
     if (n == 0) return VOX_CUDA_OK;
     cudaStream_t s = as_stream(stream);
@@ -1019,7 +1020,7 @@ EXPORT int vox_cuda_ball_batch(const vox_cuda_tree *t, const float *c, const flo
     if (e == cudaSuccess) e = cudaMemcpyAsync(hit, d_h, n, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return VOX_CUDA_ECUDA;
     return check_tree_status(t, s);
-}
+} VOX_ABI_FAIL_INT
 
 static int check_render_args(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                              const uint8_t *tex, const uint32_t *argb)
@@ -1032,11 +1033,11 @@ static int check_render_args(const vox_cuda_tree *t, const vox_cuda_camera *cam,
 
 EXPORT int vox_cuda_render_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                                   const uint8_t *tex, uint32_t *argb, void *stream)
-{
+try {
     int rc = check_render_args(t, cam, w, h, tex, argb);
     if (rc) return rc;
     return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true));
-}
+} VOX_ABI_FAIL_INT
 
 // The device's address of a host buffer that the GPU can write in place:
 // page-locked host memory (cudaHostAlloc, cudaHostRegister, torch pinned
@@ -1233,7 +1234,7 @@ static int host_call_finish(HostCallState *hc, const vox_cuda_tree *t, cudaStrea
 // and copied out.
 EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                            const uint8_t *tex, uint32_t *argb, void *stream)
-{
+try {
     int rc = check_render_args(t, cam, w, h, tex, argb);
     if (rc) return rc;
     cudaStream_t s = as_stream(stream);
@@ -1248,7 +1249,7 @@ EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, hc->d_tex, d_argb, nullptr, s);
     if (e == cudaSuccess && !in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
     return host_call_finish(hc, t, s, e);
-}
+} VOX_ABI_FAIL_INT
 
 // Host-buffer frames of one tree: the texture copied in once; all frames
 // drawn by one persistent launch into device frames, one after another, each
@@ -1278,7 +1279,7 @@ static int wait_announced(const volatile uint32_t *flag, uint32_t epoch, cudaStr
 
 EXPORT int vox_cuda_render_frames(const vox_cuda_tree *t, const vox_cuda_camera *cams, uint32_t n, uint32_t w,
                                   uint32_t h, const uint8_t *tex, uint32_t *const *frames, void *stream)
-{
+try {
     if (!t || (n && (!cams || !frames))) return VOX_CUDA_EINVAL;
     if (n == 0) return VOX_CUDA_OK;
     for (uint32_t i = 0; i < n; i++) {
@@ -1327,59 +1328,59 @@ EXPORT int vox_cuda_render_frames(const vox_cuda_tree *t, const vox_cuda_camera 
     if (e == cudaSuccess) e = e2;
     int rf = host_call_finish(hc, t, s, e);
     return rc ? rc : rf;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_render_counts_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
                                          uint32_t h, uint64_t *counts, void *stream)
-{
+try {
     if (!t || !cam || !counts) return VOX_CUDA_EINVAL;
     if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
     return status_of(launch_render<true>(t, *cam, w, h, nullptr, nullptr,
                                          reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_ray_counts_device(const vox_cuda_tree *t, const float *o, const float *d, size_t n,
                                       uint64_t *counts, void *stream)
-{
+try {
     if (!t || !counts || (n && (!o || !d))) return VOX_CUDA_EINVAL;
     return status_of(launch_rays<true>(t, o, d, nullptr, n, nullptr, nullptr, nullptr,
                                        reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_ball_counts_device(const vox_cuda_tree *t, const float *c, const float *r, size_t n,
                                        uint64_t *counts, void *stream)
-{
+try {
     if (!t || !counts || (n && (!c || !r))) return VOX_CUDA_EINVAL;
     return status_of(launch_balls<true>(t, c, r, n, nullptr,
                                         reinterpret_cast<unsigned long long *>(counts), as_stream(stream)));
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_frame_rect(const float *bbox, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                                uint32_t *rect)
-{
+try {
     if (!bbox || !cam || !rect) return VOX_CUDA_EINVAL;
     if (cam->kind != VOX_CUDA_CAMERA_SIMPLE && cam->kind != VOX_CUDA_CAMERA_DOOM) return VOX_CUDA_EINVAL;
     if (w == 0 || h == 0 || (w & 0xF) || (h & 0x3)) return VOX_CUDA_EGEOMETRY;
     double c[2];
     frame_rect(bbox, *cam, w, h, rect, c);
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_render_set_config(const vox_cuda_render_config *cfg)
-{
+try {
     if (!cfg || cfg->cull > 1 || cfg->overlap > 1) return VOX_CUDA_EINVAL;
     g_render_cull.store(cfg->cull);
     g_render_overlap.store(cfg->overlap);
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_render_get_config(vox_cuda_render_config *cfg)
-{
+try {
     if (!cfg) return VOX_CUDA_EINVAL;
     cfg->cull = g_render_cull.load();
     cfg->overlap = g_render_overlap.load();
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 static bool valid_quality(unsigned int q)
 {
@@ -1413,16 +1414,16 @@ static int render_any_device(const vox_cuda_tree *t, const vox_cuda_camera *cam,
 EXPORT int vox_cuda_render_quality_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
                                           uint32_t h, unsigned int quality, const uint8_t *tex, uint32_t *argb,
                                           void *stream)
-{
+try {
     return render_any_device(t, cam, w, h, quality, tex, nullptr, argb, stream);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_render_lit_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                                       unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights,
                                       uint32_t *argb, void *stream)
-{
+try {
     return render_any_device(t, cam, w, h, quality, tex, lights, argb, stream);
-}
+} VOX_ABI_FAIL_INT
 
 /* vox_render for a camera class the device cannot compute (renderer.c:200-319
  * with camera->iface->screen2world run by the caller): each pixel's direction
@@ -1432,7 +1433,7 @@ EXPORT int vox_cuda_render_lit_device(const vox_cuda_tree *t, const vox_cuda_cam
 EXPORT int vox_cuda_render_rays_device(const vox_cuda_tree *t, const float *origin, const float *dirs, uint32_t w,
                                        uint32_t h, unsigned int quality, const uint8_t *tex,
                                        const vox_cuda_lights *lights, uint32_t *argb, void *stream)
-{
+try {
     if (!origin || !dirs) return VOX_CUDA_EINVAL;
     vox_cuda_camera cam;
     std::memset(&cam, 0, sizeof cam);
@@ -1443,7 +1444,7 @@ EXPORT int vox_cuda_render_rays_device(const vox_cuda_tree *t, const float *orig
     if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
     return status_of(launch_render_squares(t, cam, w, h, quality, tex, argb, as_stream(stream),
                                            lights ? &lights->dev : nullptr, dirs));
-}
+} VOX_ABI_FAIL_INT
 
 static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                            unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights, uint32_t *argb,
@@ -1474,21 +1475,21 @@ static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
 
 EXPORT int vox_cuda_render_quality(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                                    unsigned int quality, const uint8_t *tex, uint32_t *argb, void *stream)
-{
+try {
     return render_any_host(t, cam, w, h, quality, tex, nullptr, argb, stream);
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_render_lit(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
                                unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights, uint32_t *argb,
                                void *stream)
-{
+try {
     return render_any_host(t, cam, w, h, quality, tex, lights, argb, stream);
-}
+} VOX_ABI_FAIL_INT
 
 // ------------------------------------------------------------------ lights
 
 EXPORT int vox_cuda_lights_upload(const struct vox_light_manager *lm, vox_cuda_lights **out)
-{
+try {
     if (!lm || !out) return VOX_CUDA_EINVAL;
     *out = nullptr;
     lights_image img;
@@ -1526,13 +1527,13 @@ EXPORT int vox_cuda_lights_upload(const struct vox_light_manager *lm, vox_cuda_l
     }
     *out = l;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_lights_free(vox_cuda_lights *l)
-{
+try {
     if (!l) return VOX_CUDA_EINVAL;
     cudaFree(l->d_nodes);
     cudaFree(l->d_spheres);
     delete l;
     return VOX_CUDA_OK;
-}
+} VOX_ABI_FAIL_INT
