@@ -158,6 +158,17 @@ int vox_cuda_read_raw_data(const char *filename, const unsigned dim[3], unsigned
  * VOX_CUDA_EINVAL.  For tests, tools and serialisation. */
 int vox_cuda_tree_image(const vox_cuda_tree *tree, void *units, size_t units_cap, uint32_t *rec_of_id,
                         size_t ids_cap, size_t *n_units, size_t *n_ids);
+/* The same image made on the host only (no GPU is used): what
+ * vox_cuda_tree_upload would copy to the device for `root` at the current
+ * vox_voxel.  Sizes and buffers as vox_cuda_tree_image; VOX_CUDA_ETOOBIG when
+ * the tree exceeds the image limits. */
+int vox_cuda_tree_flatten_host(const struct vox_node *root, void *units, size_t units_cap,
+                               uint32_t *rec_of_id, size_t ids_cap, size_t *n_units, size_t *n_ids);
+/* The check every upload makes before copying an image (no GPU is used):
+ * every offset a search can follow from the root record stays inside the
+ * n_units units, every kind is known, leaf ids are below n_nodes, and each of
+ * the n_nodes nodes is reached exactly once.  VOX_CUDA_OK or VOX_CUDA_EINVAL. */
+int vox_cuda_image_check(const void *units, size_t n_units, size_t n_nodes);
 /* Pre-order index -> host node (NULL when out of range). */
 const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *tree, uint32_t id);
 /* Host node -> pre-order index; VOX_CUDA_EINVAL when the node is not in the tree. */

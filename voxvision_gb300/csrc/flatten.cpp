@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "pool_layout.h"
+#include "parallel.h"
 
 namespace {
 
@@ -39,29 +40,6 @@ inline uint32_t fbits(float f)
 }
 
 inline bool is_inner(const vox_node *n) { return !(n->flags & VOX_LEAF_MASK); }
-
-// Runs f(i) for i in [0, n) on up to all host threads.
-template <typename F>
-void parallel_for(size_t n, F f)
-{
-    size_t nt = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
-    if (nt <= 1) {
-        for (size_t i = 0; i < n; i++) f(i);
-        return;
-    }
-    std::atomic<size_t> next{0};
-    auto run = [&]() {
-        for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
-    };
-    std::vector<std::thread> pool;
-    try {
-        for (size_t t = 1; t < nt; t++) pool.emplace_back(run);
-    } catch (...) {
-        // fewer threads: the work is dealt dynamically, the rest do it all
-    }
-    run();
-    for (auto &th : pool) th.join();
-}
 
 struct Sizes {
     uint64_t nodes = 0, units = 0, inner = 0, leaf = 0, dense = 0, dots = 0, depth = 0;

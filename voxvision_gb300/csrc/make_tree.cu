@@ -26,6 +26,7 @@
 
 #include "internal.h"
 #include "abi_guard.h"
+#include "parallel.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -47,28 +48,6 @@ bool have_gpu()
         }
     });
     return count > 0;
-}
-
-template <typename F>
-void parallel_for(size_t n, F f)
-{
-    size_t nt = std::min<size_t>(n, std::max(1u, std::thread::hardware_concurrency()));
-    if (nt <= 1) {
-        for (size_t i = 0; i < n; i++) f(i);
-        return;
-    }
-    std::atomic<size_t> next{0};
-    auto run = [&]() {
-        for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
-    };
-    std::vector<std::thread> pool;
-    try {
-        for (size_t t = 1; t < nt; t++) pool.emplace_back(run);
-    } catch (...) {
-        // fewer threads: the work is dealt dynamically, the rest do it all
-    }
-    run();
-    for (auto &th : pool) th.join();
 }
 
 inline float fl(uint32_t u)

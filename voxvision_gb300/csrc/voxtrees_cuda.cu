@@ -931,6 +931,31 @@ try {
     return VOX_CUDA_OK;
 } VOX_ABI_FAIL_INT
 
+EXPORT int vox_cuda_tree_flatten_host(const struct vox_node *root, void *units, size_t units_cap,
+                                      uint32_t *rec_of_id, size_t ids_cap, size_t *n_units, size_t *n_ids)
+try {
+    FlatTree flat;
+    int rc = vox_flatten(root, vox_voxel, &flat);
+    if (rc) return VOX_CUDA_ETOOBIG;
+    const size_t nu = flat.units.size(), ni = flat.preorder.size();
+    if (n_units) *n_units = nu;
+    if (n_ids) *n_ids = ni;
+    if ((units && units_cap < nu) || (rec_of_id && ids_cap < ni)) return VOX_CUDA_EINVAL;
+    if (units && nu) std::memcpy(units, flat.units.data(), nu * 16);
+    if (rec_of_id && ni) std::memcpy(rec_of_id, flat.rec_of_id.data(), ni * 4);
+    return VOX_CUDA_OK;
+} VOX_ABI_FAIL_INT
+
+EXPORT int vox_cuda_image_check(const void *units, size_t n_units, size_t n_nodes)
+try {
+    if (!units && n_units) return VOX_CUDA_EINVAL;
+    FlatTree f;
+    const uint4_host *u = static_cast<const uint4_host *>(units);
+    if (n_units) f.units.assign(u, u + n_units);
+    f.preorder.assign(n_nodes, nullptr);
+    return vox_flatten_validate(f) == 0 ? VOX_CUDA_OK : VOX_CUDA_EINVAL;
+} VOX_ABI_FAIL_INT
+
 EXPORT const struct vox_node *vox_cuda_tree_node(const vox_cuda_tree *t, uint32_t id)
 try {
     if (!t || id >= t->flat.preorder.size()) return nullptr;
