@@ -29,6 +29,9 @@ diagonal (665.1) at 20 degrees elevation around (128, 128, 128); texture
          bandwidth; a measured L2 copy bandwidth is reported beside it.
   cpu_baseline  the CPU oracle (C restatement of the reference's search and
          render loop) on all host cores over a bounded sample of orbit frames.
+  quality  (extras) the same orbit's frames in every vox_render quality
+         (BEST, FAST, ADAPTIVE with and without ray merging), Mpixels/s per
+         quality on the GPU and of the oracle on the host cores.
 
 --impl reference times that CPU implementation on the full orbit instead.
 Under torchrun each rank renders its own replica of the workload (the path
@@ -284,6 +287,47 @@ def measure_incoherent(torch, vg, dt, flush):
             "ball_hit_fraction": float(hit.float().mean().item()),
             "inputs": "rays: origins U[-128,384)^3 seed 3, dirs uniform on S^2; balls: centres U[0,256)^3, "
                       "r U[0.5,8] seed 4"}
+
+
+QUALITIES = {"best": 0, "fast": 1, "adaptive": 2, "adaptive_ray_merge": 2 | 4,
+             "adaptive_ray_merge_accurate": 2 | 8}
+
+
+def measure_quality(torch, vg, dt, ht_ptr, states, tex, d_tex, flush, cpu=True, nframes=24):
+    """The orbit at 1080p (every 5th frame) in every quality vox_render offers,
+    through vox_cuda_render_quality_device (BEST: the frame kernel; FAST and
+    ADAPTIVE: one thread per 4x4 square, renderer.c:215-318), one launch per
+    frame back to back, in pixels per second.  Frame 0 of each quality is
+    checked against the oracle, and the oracle's restatement of the same loop
+    on every host core times a few frames of each for comparison."""
+    from oracle import oracle as orc
+    sp = torch.cuda.current_stream().cuda_stream
+    picked = list(range(0, NFRAMES, max(1, NFRAMES // nframes)))[:nframes]
+    cams = [vg.camera_struct(states[f]) for f in picked]
+    out = torch.empty((len(cams), H * W), dtype=torch.int32, device="cuda")   # 199 MB of frames: > L2
+    res = {"frames": len(cams), "resolution": f"{W}x{H}", "unit": "Mpixels/s"}
+    for name, q in QUALITIES.items():
+        def run():
+            for i, c in enumerate(cams):
+                dt.render_quality_device(c, W, H, q, d_tex, out[i], stream=sp)
+        for _ in range(3):
+            run()
+        _, mean_ms = timed_reps(torch, run, 5, flush)
+        e = {"quality": q, "ms_per_frame": mean_ms / len(cams),
+             "value": len(cams) * W * H / (mean_ms * 1e-3) / 1e6}
+        ref, _ = orc.render_quality(ht_ptr, states[picked[0]], W, H, q, tex)
+        e["frame0_identical"] = bool(np.array_equal(out[0].cpu().numpy().view(np.uint32).reshape(H, W), ref))
+        if cpu:
+            n, t0, k = orc.nthreads_default(), time.perf_counter(), 0
+            for f in picked[:3]:
+                orc.render_quality(ht_ptr, states[f], W, H, q, tex, nthreads=n)
+                k += 1
+            cpu_s = time.perf_counter() - t0
+            e["cpu_value"] = k * W * H / cpu_s / 1e6
+            e["cpu_cores"] = n
+            e["vs_cpu"] = e["value"] / e["cpu_value"]
+        res[name] = e
+    return res
 
 
 def measure_editing(vg, vox, edits=1000, seed=16):
@@ -755,6 +799,8 @@ def run_ours(args):
             "config": dict(workload_config(info, len(vox)), frames_per_step=nf, rays_per_step=rays_step), "roofline": roofline, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk}
     if not args.no_extras:
+        line["quality"] = measure_quality(torch, vg, dt, ht.ptr, states, tex, d_tex, flush,
+                                          cpu=not args.no_cpu_baseline)
         line["incoherent"] = measure_incoherent(torch, vg, dt, flush)
         btrees = build_batch_trees(vg)
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)

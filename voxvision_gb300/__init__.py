@@ -265,6 +265,12 @@ class DeviceTree:
         check(lib().vox_cuda_render_device(self.h, C.byref(camera), w, h, _dptr(texture), _dptr(argb),
                                            stream), "vox_cuda_render_device")
 
+    def render_quality_device(self, camera: CameraStruct, w: int, h: int, quality: int, texture, argb,
+                              stream=None):
+        """vox_cuda_render_quality_device: a frame of any quality into device memory."""
+        check(lib().vox_cuda_render_quality_device(self.h, C.byref(camera), w, h, quality, _dptr(texture),
+                                                   _dptr(argb), stream), "vox_cuda_render_quality_device")
+
     def render_rays_device(self, origin, dirs, w: int, h: int, quality: int, texture, argb,
                            lights: "DeviceLights | None" = None, stream=None):
         """vox_cuda_render_rays_device: a frame from each pixel's direction
