@@ -224,61 +224,103 @@ __device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const floa
     }
 }
 
+// FAST and ADAPTIVE frames in two launches.  In renderer.c a pixel's leaf is
+// either the previous pixel's leaf, when the ray meets a voxel there (the
+// search from the leaf, :297), or what the search from the root finds for
+// the pixel's own ray (:299, and every corner and BEST pixel); the second
+// never depends on the square's earlier pixels.  So the first launch makes
+// the root search of every pixel at once, one thread a pixel like the BEST
+// kernel (warps of 8x4 pixels), and the second walks each square's 16 pixels
+// in the reference's order and decisions, one thread a square, with only the
+// searches from a leaf (one leaf's voxels) left to make; wherever the
+// reference searches from the root it takes the pixel's result of the first
+// launch.  The results are the reference's by construction: the same
+// searches of the same rays, the same choices between them.
+
+// Root search of every pixel: {leaf record or VOXP_EMPTY, intersection point}.
+// Pixels outside [x0, x1) x [y0, y1) miss the tree's box (the rectangle of
+// frame_rect) and are written as misses without a search.
+template <int CAP, bool RAYS>
+__global__ void __launch_bounds__(128) root_hits_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
+                                                        uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                                                        const float *__restrict__ rays, uint4 *__restrict__ hits,
+                                                        uint32_t *__restrict__ status)
+{
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t px = blockIdx.x * TILE_W + (warp & 1) * 8 + (lane & 7);
+    uint32_t py = blockIdx.y * TILE_H + (warp >> 1) * 4 + (lane >> 3);
+    if (px >= w || py >= h) return;
+    uint4 res = make_uint4(VOXP_EMPTY, 0u, 0u, 0u);
+    if (t.root != VOXP_EMPTY && px >= x0 && px < x1 && py >= y0 && py < y1) {
+        float dx, dy, dz;
+        pixel_dir<RAYS>(cam, rays, w, (int)px, (int)py, dx, dy, dz);
+        Counts c{0, 0, 0};
+        RayHit hh;
+        bool overflow = false;
+        if (vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1], cam.position[2], dx, dy, dz,
+                                       hh, c, overflow))
+            res = make_uint4(hh.rec, __float_as_uint(hh.x), __float_as_uint(hh.y), __float_as_uint(hh.z));
+        if (overflow) atomicOr(status, 1u);
+    }
+    hits[(size_t)py * w + px] = res;
+}
+
+// renderer.c:215-318 per 4x4 square over the root searches of root_hits_kernel.
 template <int CAP, bool RAYS>
 __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
                                                              uint32_t h, unsigned int quality,
                                                              const uint8_t *__restrict__ tex,
                                                              uint32_t *__restrict__ argb,
                                                              uint32_t *__restrict__ status, vox::DevLights lights,
-                                                             const float *__restrict__ rays)
+                                                             const float *__restrict__ rays,
+                                                             const uint4 *__restrict__ hits)
 {
-    const int order[16] = {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15};   // renderer.c:23-25
+    // renderer.c:23-25 rendering order {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}, a nibble each
+    constexpr uint64_t ORDER = 0xFEBADC9876325410ull;
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t sx = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);     // square coordinates
     uint32_t sy = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
     uint32_t ws = w >> 2, hs = h >> 2;
     if (sx >= ws || sy >= hs) return;
-    int xstart = (int)sx * 4, ystart = (int)sy * 4;
+    const int xstart = (int)sx * 4, ystart = (int)sy * 4;
     const float ox = cam.position[0], oy = cam.position[1], oz = cam.position[2];
     const int rnd_mode = quality & VOX_CUDA_QUALITY_MODE_MASK;
     const int merge_mode = quality & VOX_CUDA_QUALITY_RM_MASK;
+    const uint4 *sq = hits + (size_t)ystart * w + xstart;             // the square's root searches
     uint32_t out[16];
 #pragma unroll
     for (int i = 0; i < 16; i++) out[i] = 0u;
     Counts c{0, 0, 0};
     bool overflow = false;
-    bool have_leaf = false;
+    bool have_leaf = false;      // `leaf != NULL` of renderer.c
     uint32_t leaf_rec = 0;
     float ix = 0.f, iy = 0.f, iz = 0.f;       // inter1
     int block_mode = rnd_mode;
     int istart = 0, iend = 16;
     bool block_merge = false;
-    bool empty = t.root == VOXP_EMPTY;
 
-    if (block_mode == VOX_CUDA_QUALITY_ADAPTIVE) {
+    if (block_mode == VOX_CUDA_QUALITY_ADAPTIVE) {              // renderer.c:240-282
         block_merge = (merge_mode == VOX_CUDA_QUALITY_RAY_MERGE);
         istart = 1;
-        float d1x, d1y, d1z;
-        pixel_dir<RAYS>(cam, rays, w, xstart, ystart, d1x, d1y, d1z);
-        RayHit h1;
-        bool c1 = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d1x, d1y, d1z, h1, c, overflow);
+        const uint4 h1 = sq[0];
         block_mode = VOX_CUDA_QUALITY_FAST;
-        have_leaf = c1;
-        if (c1) {
-            leaf_rec = h1.rec;
-            ix = h1.x; iy = h1.y; iz = h1.z;
+        have_leaf = h1.x != VOXP_EMPTY;
+        if (have_leaf) {
+            leaf_rec = h1.x;
+            ix = __uint_as_float(h1.y); iy = __uint_as_float(h1.z); iz = __uint_as_float(h1.w);
             iend = 15;
-            out[0] = vox::hit_color(tex, t, lights, h1.x, h1.y, h1.z, overflow);
-            float d2x, d2y, d2z;
-            pixel_dir<RAYS>(cam, rays, w, xstart + 3, ystart + 3, d2x, d2y, d2z);
-            RayHit h2;
-            bool c2 = vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, d2x, d2y, d2z, h2, c, overflow);
-            if (c2) {
-                out[15] = vox::hit_color(tex, t, lights, h2.x, h2.y, h2.z, overflow);
-                float d1 = sqr3(h1.x, h1.y, h1.z, ox, oy, oz);
+            out[0] = vox::hit_color(tex, t, lights, ix, iy, iz, overflow);
+            const uint4 h2 = sq[3 * (size_t)w + 3];
+            if (h2.x != VOXP_EMPTY) {
+                const float jx = __uint_as_float(h2.y), jy = __uint_as_float(h2.z), jz = __uint_as_float(h2.w);
+                out[15] = vox::hit_color(tex, t, lights, jx, jy, jz, overflow);
+                float d1x, d1y, d1z, d2x, d2y, d2z;
+                pixel_dir<RAYS>(cam, rays, w, xstart, ystart, d1x, d1y, d1z);
+                pixel_dir<RAYS>(cam, rays, w, xstart + 3, ystart + 3, d2x, d2y, d2z);
+                float d1 = sqr3(ix, iy, iz, ox, oy, oz);
                 float d2 = sqr3(d1x, d1y, d1z, 0.f, 0.f, 0.f);
                 float criteria = __fmul_rn(__fdiv_rn(d1, d2), sqr3(d1x, d1y, d1z, d2x, d2y, d2z));
-                float dist = sqr3(h1.x, h1.y, h1.z, h2.x, h2.y, h2.z);
+                float dist = sqr3(ix, iy, iz, jx, jy, jz);
                 if ((double)__fdiv_rn(dist, criteria) > 1.69)          // LENGTH_THRESHOLD, renderer.c:197
                     block_mode = VOX_CUDA_QUALITY_BEST;
                 if (d1 > 22500.0f)                                       // MAX_DIST^2, renderer.c:198
@@ -291,27 +333,29 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
     }
 
     int prev_p = 0;
-    for (int i = istart; i < iend; i++) {
-        int p = order[i];
-        int py = p >> 2, px = p & 3;
-        bool merge = block_merge && (i & 1);
-        float dx, dy, dz;
-        pixel_dir<RAYS>(cam, rays, w, px + xstart, py + ystart, dx, dy, dz);
+    for (int i = istart; i < iend; i++) {                       // renderer.c:286-315
+        const int p = (int)((ORDER >> (4 * i)) & 15u);
+        const int py = p >> 2, px = p & 3;
+        const bool merge = block_merge && (i & 1);
         if (!merge) {
-            RayHit hh;
-            if (block_mode == VOX_CUDA_QUALITY_FAST) {
-                if (have_leaf)
-                    have_leaf = vox::trace_ray<CAP, false>(t, leaf_rec, ox, oy, oz, dx, dy, dz, hh, c, overflow);
-                if (!have_leaf)
-                    have_leaf = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, dx, dy, dz, hh, c,
-                                                                     overflow);
-            } else {
-                have_leaf = !empty && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, dx, dy, dz, hh, c,
-                                                                 overflow);
+            bool from_root = true;
+            if (block_mode == VOX_CUDA_QUALITY_FAST && have_leaf) {
+                float dx, dy, dz;
+                pixel_dir<RAYS>(cam, rays, w, px + xstart, py + ystart, dx, dy, dz);
+                RayHit hh;
+                if (vox::trace_ray<CAP, false>(t, leaf_rec, ox, oy, oz, dx, dy, dz, hh, c, overflow)) {
+                    leaf_rec = hh.rec;
+                    ix = hh.x; iy = hh.y; iz = hh.z;
+                    from_root = false;
+                }
             }
-            if (have_leaf) {
-                leaf_rec = hh.rec;
-                ix = hh.x; iy = hh.y; iz = hh.z;
+            if (from_root) {
+                const uint4 hr = sq[(size_t)py * w + px];
+                have_leaf = hr.x != VOXP_EMPTY;
+                if (have_leaf) {
+                    leaf_rec = hr.x;
+                    ix = __uint_as_float(hr.y); iy = __uint_as_float(hr.z); iz = __uint_as_float(hr.w);
+                }
             }
         }
         if (have_leaf) out[p] = merge ? out[prev_p] : vox::hit_color(tex, t, lights, ix, iy, iz, overflow);
@@ -429,25 +473,51 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
     return cudaGetLastError();
 }
 
-// FAST / ADAPTIVE frames, and with a ray buffer frames of every quality.
+// FAST / ADAPTIVE frames, and with a ray buffer frames of every quality: the
+// root searches of every pixel, then the squares.
 cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s,
                                   const vox::DevLights *lights = nullptr, const float *rays = nullptr)
 {
-    uint32_t ws = w / 4, hs = h / 4;
-    dim3 block(128), grid((ws + 15) / 16, (hs + 7) / 8);
     vox::DevLights L{};
     if (lights) L = *lights;
-    void (*kern)(DevTree, vox_cuda_camera, uint32_t, uint32_t, unsigned int, const uint8_t *, uint32_t *,
-                 uint32_t *, vox::DevLights, const float *);
+    // the rectangle where rays can meet the tree's box (a camera class the
+    // device does not know: the whole frame)
+    uint32_t x0 = 0, y0 = 0, x1 = w, y1 = h;
+    if (!rays) {
+        FramePlan p;
+        plan_frame(t, cam, w, h, g_render_cull.load() != 0, p);
+        x0 = p.x0; y0 = p.y0; x1 = p.x1; y1 = p.y1;
+    }
+    uint4 *hits = nullptr;
+    cudaError_t e = cudaMallocAsync(&hits, (size_t)w * h * sizeof(uint4), s);
+    if (e != cudaSuccess) return e;
     const int cap = t->cap_class;
-    if (rays) kern = cap == 0 ? render_squares_kernel<CAP0, true>
-                   : cap == 1 ? render_squares_kernel<CAP1, true> : render_squares_kernel<CAP2, true>;
-    else kern = cap == 0 ? render_squares_kernel<CAP0, false>
-              : cap == 1 ? render_squares_kernel<CAP1, false> : render_squares_kernel<CAP2, false>;
-    kern<<<grid, block, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status, L, rays);
+    void (*roots)(DevTree, vox_cuda_camera, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
+                  const float *, uint4 *, uint32_t *);
+    void (*squares)(DevTree, vox_cuda_camera, uint32_t, uint32_t, unsigned int, const uint8_t *, uint32_t *,
+                    uint32_t *, vox::DevLights, const float *, const uint4 *);
+    if (rays) {
+        roots = cap == 0 ? root_hits_kernel<CAP0, true> : cap == 1 ? root_hits_kernel<CAP1, true>
+                                                                   : root_hits_kernel<CAP2, true>;
+        squares = cap == 0 ? render_squares_kernel<CAP0, true>
+                : cap == 1 ? render_squares_kernel<CAP1, true> : render_squares_kernel<CAP2, true>;
+    } else {
+        roots = cap == 0 ? root_hits_kernel<CAP0, false> : cap == 1 ? root_hits_kernel<CAP1, false>
+                                                                    : root_hits_kernel<CAP2, false>;
+        squares = cap == 0 ? render_squares_kernel<CAP0, false>
+                : cap == 1 ? render_squares_kernel<CAP1, false> : render_squares_kernel<CAP2, false>;
+    }
+    roots<<<dim3((w + TILE_W - 1) / TILE_W, (h + TILE_H - 1) / TILE_H), 128, 0, s>>>(
+        t->dev, cam, w, h, x0, y0, x1, y1, rays, hits, t->d_status);
     count_launch();
-    return cudaGetLastError();
+    const uint32_t ws = w / 4, hs = h / 4;
+    squares<<<dim3((ws + 15) / 16, (hs + 7) / 8), 128, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status,
+                                                               L, rays, hits);
+    count_launch();
+    e = cudaGetLastError();
+    cudaFreeAsync(hits, s);
+    return e;
 }
 
 
