@@ -296,8 +296,9 @@ QUALITIES = {"best": 0, "fast": 1, "adaptive": 2, "adaptive_ray_merge": 2 | 4,
 def measure_quality(torch, vg, dt, ht_ptr, states, tex, d_tex, flush, cpu=True, nframes=24):
     """The orbit at 1080p (every 5th frame) in every quality vox_render offers,
     through vox_cuda_render_quality_device (BEST: the frame kernel; FAST and
-    ADAPTIVE: one thread per 4x4 square, renderer.c:215-318), one launch per
-    frame back to back, in pixels per second.  Frame 0 of each quality is
+    ADAPTIVE: every pixel's root search, then each 4x4 square's sequence of
+    renderer.c:215-318), one call per frame back to back, in pixels per
+    second.  Frame 0 of each quality is
     checked against the oracle, and the oracle's restatement of the same loop
     on every host core times a few frames of each for comparison."""
     from oracle import oracle as orc

@@ -198,11 +198,10 @@ __global__ void __launch_bounds__(128, MINB) render_kernel(DevTree t, vox_cuda_c
     if (COUNT) add_counts(counts, c);
 }
 
-// vox_render in FAST / ADAPTIVE quality (renderer.c:215-318): one thread per
-// 4x4 square, its 16 pixels in the reference's Z-order, reusing the previous
-// pixel's leaf as the search root (FAST) and choosing the mode per square
-// from the two corner rays (ADAPTIVE), with optional ray merging.  A warp
-// covers 8x4 squares (32x16 pixels).
+// vox_render in FAST / ADAPTIVE quality (renderer.c:215-318): each 4x4
+// square's 16 pixels in the reference's Z-order, reusing the previous pixel's
+// leaf as the search root (FAST) and choosing the mode per square from the
+// two corner rays (ADAPTIVE), with optional ray merging.
 __device__ __forceinline__ float sqr3(float ax, float ay, float az, float bx, float by, float bz)
 {
     float x = __fsub_rn(ax, bx), y = __fsub_rn(ay, by), z = __fsub_rn(az, bz);
