@@ -83,6 +83,8 @@ def parse_args():
     p.add_argument("--tree-build", type=int, default=0, metavar="N",
                    help="only time the device tree build of the N^3 noise volume (profiling runs)")
     p.add_argument("--reps", type=int, default=5, help="timed repetitions of --tree-build")
+    p.add_argument("--quality", type=int, default=0, metavar="N",
+                   help="only time every vox_render quality on N orbit frames (profiling runs)")
     return p.parse_args()
 
 
@@ -856,6 +858,18 @@ def main():
         vg.set_voxel_size((1, 1, 1))
         size = {256: (256, 2, 0.08), 512: (512, 3, 0.10)}.get(args.tree_build, (args.tree_build, 2, 0.08))
         print(json.dumps({"tree_build": measure_tree_build(vg, (size,), reps=args.reps)}), flush=True)
+        return
+    if args.quality:
+        import torch
+
+        import voxvision_gb300 as vg
+        vg.set_voxel_size((1, 1, 1))
+        vox, ht, tex = make_workload(vg.HostTree.from_voxels)
+        dt = vg.DeviceTree(ht.ptr)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        q = measure_quality(torch, vg, dt, ht.ptr, orbit_states(), tex, torch.from_numpy(tex).cuda(), flush,
+                            cpu=not args.no_cpu_baseline, nframes=args.quality)
+        print(json.dumps({"quality": q}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)
