@@ -802,12 +802,14 @@ def run_ours(args):
             "config": dict(workload_config(info, len(vox)), frames_per_step=nf, rays_per_step=rays_step), "roofline": roofline, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk}
     if not args.no_extras:
+        # the request server first: its latencies are the extras most easily
+        # disturbed by what ran before in the process
+        btrees = build_batch_trees(vg)
+        line["served"] = measure_served(vg, btrees, tex)
         line["quality"] = measure_quality(torch, vg, dt, ht.ptr, states, tex, d_tex, flush,
                                           cpu=not args.no_cpu_baseline)
         line["incoherent"] = measure_incoherent(torch, vg, dt, flush)
-        btrees = build_batch_trees(vg)
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
-        line["served"] = measure_served(vg, btrees, tex)
         line["editing"] = measure_editing(vg, vox)
         line["tree_build"] = measure_tree_build(vg)
     if not args.no_cpu_baseline and world >= 1:
