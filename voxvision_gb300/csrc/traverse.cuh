@@ -149,8 +149,8 @@ struct RayHit {
  * ray_step() runs one iteration.  Every iteration makes one 16..48-byte load
  * (a node record, or one voxel of the leaf being scanned) and one box test,
  * so the lanes of a warp stay in step whatever mix of nodes and voxels they
- * are on, and a lane whose search ended can start another between any two
- * iterations (the refill render kernel does).  The box test of a node is
+ * are on, and a lane whose search ended could start another between any
+ * two iterations.  The box test of a node is
  * search.c:22-23; of a voxel, the leaf loop's test at :55.  When an inner
  * node's box is entered, its plane crossings (:105-148) are computed at once:
  * the children behind the crossings are pushed in visiting order and the
