@@ -300,10 +300,9 @@ def measure_quality(torch, vg, dt, ht_ptr, states, tex, d_tex, flush, cpu=True, 
     through vox_cuda_render_quality_device (BEST: the frame kernel; FAST and
     ADAPTIVE: every pixel's root search, then each 4x4 square's sequence of
     renderer.c:215-318), one call per frame back to back, in pixels per
-    second.  Frame 0 of each quality is
-    checked against the oracle, and the oracle's restatement of the same loop
-    on every host core times a few frames of each for comparison."""
-    from oracle import oracle as orc
+    second.  With the CPU-baseline leg on (no --no-cpu-baseline), frame 0 of
+    each quality is checked against the oracle and the oracle's restatement
+    of the same loop times a few frames of each on every host core."""
     sp = torch.cuda.current_stream().cuda_stream
     picked = list(range(0, NFRAMES, max(1, NFRAMES // nframes)))[:nframes]
     cams = [vg.camera_struct(states[f]) for f in picked]
@@ -318,9 +317,10 @@ def measure_quality(torch, vg, dt, ht_ptr, states, tex, d_tex, flush, cpu=True, 
         _, mean_ms = timed_reps(torch, run, 5, flush)
         e = {"quality": q, "ms_per_frame": mean_ms / len(cams),
              "value": len(cams) * W * H / (mean_ms * 1e-3) / 1e6}
-        ref, _ = orc.render_quality(ht_ptr, states[picked[0]], W, H, q, tex)
-        e["frame0_identical"] = bool(np.array_equal(out[0].cpu().numpy().view(np.uint32).reshape(H, W), ref))
-        if cpu:
+        if cpu:   # the CPU-baseline leg: the oracle checks frame 0 and is timed beside the GPU
+            from oracle import oracle as orc
+            ref, _ = orc.render_quality(ht_ptr, states[picked[0]], W, H, q, tex)
+            e["frame0_identical"] = bool(np.array_equal(out[0].cpu().numpy().view(np.uint32).reshape(H, W), ref))
             n, t0, k = orc.nthreads_default(), time.perf_counter(), 0
             for f in picked[:3]:
                 orc.render_quality(ht_ptr, states[f], W, H, q, tex, nthreads=n)
