@@ -50,6 +50,17 @@ void vox_use_camera_methods(struct vox_camera *camera, const struct vox_camera_i
 /* camera.h:160 */
 void vox_init_camera(struct vox_camera *camera);
 
+/* vect-ops.h:13-64: the vector helpers libvoxrnd exports for camera modules
+ * (declared there under VOXRND_SOURCE), so that a camera class built against
+ * the reference links against this library.  vox_rotate_vector_q rotates the
+ * vector part of `vector` into res[1..3] and leaves res[0] alone. */
+void vox_quat_mul(const vox_quat q1, const vox_quat q2, vox_quat res);
+void vox_rotate_vector(const vox_quat base, const vox_dot vector, vox_dot res);
+void vox_rotate_vector_q(const vox_quat base, const vox_quat vector, vox_quat res);
+void vox_quat_normalize(vox_quat quat);
+void vox_dot_normalize(vox_dot dot);
+void vox_quat_set_identity(vox_quat quat);
+
 /* renderer.h quality flags */
 #define VOX_QUALITY_BEST 0x0
 #define VOX_QUALITY_FAST 0x1

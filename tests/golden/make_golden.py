@@ -6,6 +6,7 @@ Run in a container that has the reference sources (default /root/reference):
                                   # camera sources into oracle/_ref/
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py edits    # the tree-editing fixtures only
+    python tests/golden/make_golden.py vectops  # the vector-helper fixture only
 
 Every expected value here comes from the reference's compiled code:
 vox_make_tree, vox_insert_voxel, vox_delete_voxel, vox_ray_tree_intersection,
@@ -289,6 +290,41 @@ def camera_cases():
     print("cameras:", len(recs))
 
 
+def vectops_case():
+    """The vector helpers of vect-ops.c (exported by the reference's camera
+    plugins) on random and special inputs: quaternion products, rotations of
+    vectors and of quaternions' vector parts, normalisation."""
+    lib = C.CDLL(os.path.join(REF, "libsimplecam_ref.so"))
+    for name in ("vox_quat_mul", "vox_rotate_vector", "vox_rotate_vector_q"):
+        getattr(lib, name).argtypes = [vp, vp, vp]
+    for name in ("vox_quat_normalize", "vox_dot_normalize", "vox_quat_set_identity"):
+        getattr(lib, name).argtypes = [vp]
+    rng = np.random.default_rng(90)
+    n = 2000
+    q1 = rng.normal(0, 1, (n, 4)).astype(np.float32)
+    q2 = rng.normal(0, 3, (n, 4)).astype(np.float32)
+    v = rng.uniform(-500, 500, (n, 3)).astype(np.float32)
+    special = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1], [0, 0, 0, 0],
+                        [0.5, 0.5, 0.5, 0.5], [-0.0, 0, 0, 0], [4, 1, 2, 3], [2, 0, 2, 0]], np.float32)
+    q1[:len(special)] = special
+    q2[:len(special)] = special[::-1]
+    with np.errstate(invalid="ignore"):        # the zero quaternion
+        unit = np.nan_to_num(q1 / np.linalg.norm(q1, axis=1, keepdims=True)).astype(np.float32)
+    prod = np.zeros_like(q1); rot = np.zeros_like(v); rotq = np.full_like(q1, 7.0)
+    qn = q1.copy(); dn = v.copy()
+    for i in range(n):
+        lib.vox_quat_mul(P(q1[i]), P(q2[i]), P(prod[i]))
+        lib.vox_rotate_vector(P(unit[i]), P(v[i]), P(rot[i]))
+        lib.vox_rotate_vector_q(P(unit[i]), P(q2[i]), P(rotq[i]))
+        lib.vox_quat_normalize(P(qn[i]))
+        lib.vox_dot_normalize(P(dn[i]))
+    ident = np.full(4, 9.0, np.float32)
+    lib.vox_quat_set_identity(P(ident))
+    np.savez_compressed(os.path.join(OUT, "vectops.npz"), q1=q1, q2=q2, unit=unit, v=v, prod=prod, rot=rot,
+                        rotq=rotq, qn=qn, dn=dn, identity=ident)
+    print("vectops:", n)
+
+
 def render_case():
     """Config-1 workload (64^3 blobs, 256x256, camera at (160,-96,112) looking at
     (32,32,32)): per-pixel rays from the reference simple camera, hits from the
@@ -479,11 +515,14 @@ def main():
 
     camera_cases()
     render_case()
+    vectops_case()
 
 
 if __name__ == "__main__":
     if sys.argv[1:] == ["edits"]:
         edit_cases()
+    elif sys.argv[1:] == ["vectops"]:
+        vectops_case()
     else:
         main()
         edit_cases()

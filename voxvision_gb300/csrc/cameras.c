@@ -79,6 +79,35 @@ static void set_identity(float *q)
     q[0] = 1; q[1] = 0; q[2] = 0; q[3] = 0;
 }
 
+/* The vector helpers libvoxrnd exports for camera modules (vect-ops.h:13-64,
+ * vect-ops.c:17-70), so that a camera class built against the reference
+ * links against this library too.  The same arithmetic as the built-in
+ * cameras use. */
+EXPORT void vox_quat_mul(const vox_quat q1, const vox_quat q2, vox_quat res) { quat_mul(q1, q2, res); }
+
+EXPORT void vox_rotate_vector(const vox_quat base, const vox_dot vector, vox_dot res)
+{
+    rotate3(base, vector, res);
+}
+
+/* The vector part of `vector` rotated into res[1..3]; res[0] is left as it is. */
+EXPORT void vox_rotate_vector_q(const vox_quat base, const vox_quat vector, vox_quat res)
+{
+    rotate3(base, vector + 1, res + 1);
+}
+
+EXPORT void vox_quat_normalize(vox_quat quat) { normalize4(quat); }
+
+EXPORT void vox_dot_normalize(vox_dot dot)
+{
+    float s = 0;
+    for (int i = 0; i < 3; i++) s += dot[i] * dot[i];
+    float n = sqrtf(s);
+    for (int i = 0; i < 3; i++) dot[i] /= n;
+}
+
+EXPORT void vox_quat_set_identity(vox_quat quat) { set_identity(quat); }
+
 /* set_window_size of both classes (simple-camera.c:120-136) */
 static void window_params(float fov, int w, int h, float *xsub, float *ysub, float *mul)
 {
