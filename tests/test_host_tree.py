@@ -103,6 +103,50 @@ def test_camera_reference_expectations():
         np.testing.assert_allclose(cam.position(), [-1, 0, 0], atol=1e-5)
 
 
+def test_camera_look_at_reference_expectations():
+    """tests.c:712-733: after look_at, the centre ray of either class passes
+    through the target (the reference's hit_dot at approx_check 0.5)."""
+    for kind in (0, 1):
+        cam = HostCamera(kind)
+        cam.set_window_size(100, 100)
+        pos, target = np.array([-100, 20, -20], np.float32), np.zeros(3, np.float32)
+        cam.set_position(pos)
+        cam.look_at(target)
+        d = cam.screen2world(50, 50)
+        t = np.float32((target[0] - pos[0]) / d[0])
+        assert t >= 0
+        hit = np.array([target[0], d[1] * t + pos[1], d[2] * t + pos[2]], np.float32)
+        assert np.max(np.abs(hit - target)) <= 0.5
+
+
+def test_camera_look_at_then_move():
+    """tests.c:735-759: looking at the default direction and moving by (1, 0, 0)
+    lands at (1, 0, 0), twice in a row."""
+    cam = HostCamera(0)
+    for _ in range(2):
+        cam.set_position((0, 0, 0))
+        cam.look_at(np.array([0, 1, 0], np.float32))
+        cam.move((1, 0, 0))
+        np.testing.assert_allclose(cam.position(), [1, 0, 0], atol=1e-5)
+
+
+def test_camera_copy_construction():
+    """tests.c:761-776: construct_camera(camera) copies the camera's state."""
+    import ctypes as C
+    from voxvision_gb300 import lib
+    from voxvision_gb300.cameras import CONS, DOTM, DESTROY
+    cam = HostCamera(0)
+    cam.set_position((10, 110, 1110))
+    cam.set_window_size(100, 100)
+    tbl = C.cast(lib().vox_camera_methods(b"simple-camera"), C.POINTER(C.c_void_p * 10)).contents
+    copy = CONS(tbl[8])(cam.obj)
+    assert copy
+    pos = np.zeros(3, np.float32)
+    DOTM(tbl[6])(copy, pos.ctypes.data_as(C.c_void_p))
+    np.testing.assert_allclose(pos, [10, 110, 1110], atol=1e-5)
+    DESTROY(tbl[9])(copy)
+
+
 @pytest.mark.parametrize("case", BUILT + ["g676d50c"])
 def test_flattened_image_is_sound(case):
     """vox_cuda_tree_measure flattens the tree on the host, walks the device
