@@ -59,6 +59,14 @@ struct vox_node *vox_make_tree_host(vox_dot set[], size_t n);
 void vox_destroy_tree(struct vox_node *tree);
 /* tree.h:72 */
 size_t vox_voxels_in_tree(const struct vox_node *tree);
+/* tree.h:130 -- print the tree to stdout, node by node (the reference's text). */
+void vox_dump_tree(const struct vox_node *tree);
+/* geom.h:59-73 -- L1 distance, squared distance, squared norm (summed in axis order). */
+float vox_abs_metric(const vox_dot dot1, const vox_dot dot2);
+float vox_sqr_metric(const vox_dot dot1, const vox_dot dot2);
+float vox_sqr_norm(const vox_dot dot);
+/* geom.h:87 -- octant of `dot` around `center` (bit i: center[i] > dot[i]). */
+int get_subspace_idx(const vox_dot center, const vox_dot dot);
 /* tree.h:77 */
 void vox_bounding_box(const struct vox_node *tree, struct vox_box *box);
 /* tree.h:140 */
@@ -118,6 +126,8 @@ void vox_mtree_destroy(struct vox_mtree_node *root);
 struct vox_mtree_node *vox_mtree_contains_sphere(const struct vox_mtree_node *root, const struct vox_sphere *s);
 /* mtree.h:110 -- number of spheres. */
 unsigned int vox_mtree_items(const struct vox_mtree_node *root);
+/* mtree.h:98 -- print the M-tree to stdout, node by node (the reference's text). */
+void vox_mtree_dump(const struct vox_mtree_node *root);
 /* mtree.h:138-140 -- call callback(s, arg) for every sphere containing dot. */
 void vox_mtree_spheres_containing_f(const struct vox_mtree_node *root, const vox_dot dot,
                                     void (*callback)(const struct vox_sphere *s, void *arg), void *arg);

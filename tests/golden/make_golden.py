@@ -7,6 +7,7 @@ Run in a container that has the reference sources (default /root/reference):
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py edits    # the tree-editing fixtures only
     python tests/golden/make_golden.py vectops  # the vector-helper fixture only
+    python tests/golden/make_golden.py geom     # the metrics and tree-dump fixture only
 
 Every expected value here comes from the reference's compiled code:
 vox_make_tree, vox_insert_voxel, vox_delete_voxel, vox_ray_tree_intersection,
@@ -325,6 +326,62 @@ def vectops_case():
     print("vectops:", n)
 
 
+def capture_stdout(fn):
+    """What fn() prints through the C library's stdout."""
+    import tempfile
+    libc = C.CDLL(None)
+    libc.fflush.argtypes = [vp]
+    sys.stdout.flush()
+    libc.fflush(None)
+    saved = os.dup(1)
+    with tempfile.TemporaryFile() as f:
+        os.dup2(f.fileno(), 1)
+        try:
+            fn()
+            libc.fflush(None)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+        f.seek(0)
+        return f.read().decode()
+
+
+def geom_case():
+    """geom.c's exported metrics and subspace index on random and special
+    inputs, and tree.c's vox_dump_tree text of a small tree (pointers other
+    than NULL masked)."""
+    import re
+    for name in ("vox_abs_metric", "vox_sqr_metric"):
+        getattr(ref, name).argtypes = [vp, vp]
+        getattr(ref, name).restype = C.c_float
+    ref.vox_sqr_norm.argtypes = [vp]; ref.vox_sqr_norm.restype = C.c_float
+    ref.get_subspace_idx.argtypes = [vp, vp]; ref.get_subspace_idx.restype = C.c_int
+    ref.vox_dump_tree.argtypes = [vp]
+    rng = np.random.default_rng(95)
+    n = 3000
+    a = rng.uniform(-1e3, 1e3, (n, 3)).astype(np.float32)
+    b = rng.uniform(-1e3, 1e3, (n, 3)).astype(np.float32)
+    b[:n // 4] = a[:n // 4] + rng.integers(-2, 3, (n // 4, 3)).astype(np.float32)   # ties and near ties
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-40, -1e-40, 3e38, -3e38], np.float32)
+    k = len(special)
+    a[n // 4:n // 4 + k * k, 0] = np.repeat(special, k)
+    b[n // 4:n // 4 + k * k, 0] = np.tile(special, k)
+    absm = np.array([ref.vox_abs_metric(P(a[i]), P(b[i])) for i in range(n)], np.float32)
+    sqrm = np.array([ref.vox_sqr_metric(P(a[i]), P(b[i])) for i in range(n)], np.float32)
+    norm = np.array([ref.vox_sqr_norm(P(a[i])) for i in range(n)], np.float32)
+    sub = np.array([ref.get_subspace_idx(P(a[i]), P(b[i])) for i in range(n)], np.int32)
+    set_voxel((1.0, 1.0, 1.0))
+    cube = np.mgrid[0:8, 0:8, 0:8].reshape(3, -1).T.astype(np.float32)
+    holes = np.concatenate([cube[(cube.sum(1) % 5) != 0], np.tile([[20, 3, 3]], (9, 1))]).astype(np.float32)
+    t = ref_tree_from_voxels(holes)
+    text = capture_stdout(lambda: ref.vox_dump_tree(t))
+    ref.vox_destroy_tree(t)
+    text = re.sub(r"0x[0-9a-f]+", "PTR", text)
+    np.savez_compressed(os.path.join(OUT, "geom.npz"), a=a, b=b, abs_metric=absm, sqr_metric=sqrm, sqr_norm=norm,
+                        subspace=sub, dump_voxels=holes, dump_text=np.array(text))
+    print("geom:", n, "dump lines:", text.count("\n"))
+
+
 def render_case():
     """Config-1 workload (64^3 blobs, 256x256, camera at (160,-96,112) looking at
     (32,32,32)): per-pixel rays from the reference simple camera, hits from the
@@ -516,13 +573,15 @@ def main():
     camera_cases()
     render_case()
     vectops_case()
+    geom_case()
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["edits"]:
-        edit_cases()
-    elif sys.argv[1:] == ["vectops"]:
-        vectops_case()
+    parts = {"edits": edit_cases, "vectops": vectops_case, "geom": geom_case}
+    if sys.argv[1:] and sys.argv[1] not in parts:
+        sys.exit(f"unknown fixture set {sys.argv[1]!r}; one of {sorted(parts)} or none for everything")
+    if sys.argv[1:]:
+        parts[sys.argv[1]]()
     else:
         main()
         edit_cases()

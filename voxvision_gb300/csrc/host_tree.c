@@ -11,6 +11,7 @@
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -210,6 +211,69 @@ EXPORT void vox_destroy_tree(struct vox_node *tree)
 EXPORT size_t vox_voxels_in_tree(const struct vox_node *tree)
 {
     return tree ? tree->dots_num : 0;
+}
+
+/* geom.c:125-147: distances summed axis by axis from 0, in axis order. */
+EXPORT float vox_abs_metric(const vox_dot dot1, const vox_dot dot2)
+{
+    float r = 0;
+    for (int i = 0; i < 3; i++) r += fabsf(dot1[i] - dot2[i]);
+    return r;
+}
+
+EXPORT float vox_sqr_metric(const vox_dot dot1, const vox_dot dot2)
+{
+    float r = 0;
+    for (int i = 0; i < 3; i++) {
+        float d = dot1[i] - dot2[i];
+        r += d * d;
+    }
+    return r;
+}
+
+EXPORT float vox_sqr_norm(const vox_dot dot)
+{
+    float r = 0;
+    for (int i = 0; i < 3; i++) r += dot[i] * dot[i];
+    return r;
+}
+
+/* geom.c:44-51: octant of `dot` around `center`, bit i set when center[i] > dot[i]. */
+EXPORT int get_subspace_idx(const vox_dot center, const vox_dot dot)
+{
+    int r = 0;
+    for (int i = 0; i < 3; i++) r |= (center[i] > dot[i]) << i;
+    return r;
+}
+
+/* tree.c:868-918: the tree printed node by node, depth first (the text the
+ * reference prints, for the same debugging use). */
+EXPORT void vox_dump_tree(const struct vox_node *tree)
+{
+    if (!tree) return;
+    const int inner = !(tree->flags & VOX_LEAF_MASK);
+    printf("Node %p %s\n", (const void *)tree,
+           (tree->flags & VOX_LEAF) ? "LEAF" : (tree->flags & VOX_DENSE_LEAF) ? "DENSE LEAF" : "INNER");
+    printf("Bounding box min <%f, %f, %f>\n", tree->bounding_box.min[0], tree->bounding_box.min[1],
+           tree->bounding_box.min[2]);
+    printf("Bounding box max <%f, %f, %f>\n", tree->bounding_box.max[0], tree->bounding_box.max[1],
+           tree->bounding_box.max[2]);
+    printf("Number of voxels %u\n", tree->dots_num);
+    if (tree->flags & VOX_LEAF) {
+        printf("Dots:\n");
+        for (unsigned i = 0; i < tree->dots_num; i++)
+            printf("<%f, %f, %f>\n", tree->data.dots[i][0], tree->data.dots[i][1], tree->data.dots[i][2]);
+    } else if (inner) {
+        printf("Center <%f, %f, %f>\n", tree->data.inner.center[0], tree->data.inner.center[1],
+               tree->data.inner.center[2]);
+        printf("Children:\n");
+        for (int i = 0; i < 8; i++) printf("%p\n", (void *)tree->data.inner.children[i]);
+    }
+    printf("------Node ends here------\n");
+    if (inner) {
+        for (int i = 0; i < 8; i++) vox_dump_tree(tree->data.inner.children[i]);
+        printf("=======Node and children end here=======\n");
+    }
 }
 
 EXPORT void vox_bounding_box(const struct vox_node *tree, struct vox_box *box)

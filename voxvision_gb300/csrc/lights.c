@@ -13,6 +13,7 @@
  * as in the reference's scalar build.
  */
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -280,6 +281,33 @@ EXPORT void vox_mtree_destroy(struct vox_mtree_node *n)
         for (unsigned i = 0; i < n->num; i++) vox_mtree_destroy(n->data.children[i]);
     }
     free(n);
+}
+
+/* mtree.c:384-416: the M-tree printed node by node, depth first (the text
+ * the reference prints, for the same debugging use). */
+EXPORT void vox_mtree_dump(const struct vox_mtree_node *node)
+{
+    printf("Node %p ", (const void *)node);
+    if (!node) {
+        printf("empty node\n");
+        return;
+    }
+    printf("%s, parent=%p\n", node->leaf ? "leaf" : "inner node", (void *)node->parent);
+    printf("Bounding sphere: <%7.4f, %7.4f, %7.4f>, %7.4f\n", node->bounding_sphere.center[0],
+           node->bounding_sphere.center[1], node->bounding_sphere.center[2], node->bounding_sphere.radius);
+    if (node->leaf) {
+        printf("Leaf content (%u spheres):\n", node->num);
+        for (unsigned i = 0; i < node->num; i++)
+            printf("<%7.4f, %7.4f, %7.4f>, %7.4f\n", node->data.spheres[i].center[0],
+                   node->data.spheres[i].center[1], node->data.spheres[i].center[2],
+                   node->data.spheres[i].radius);
+        printf("==========\n");
+    } else {
+        printf("Node children\n");
+        for (unsigned i = 0; i < node->num; i++) printf("%p ", (void *)node->data.children[i]);
+        printf("\n==========\n");
+        for (unsigned i = 0; i < node->num; i++) vox_mtree_dump(node->data.children[i]);
+    }
 }
 
 EXPORT unsigned int vox_mtree_items(const struct vox_mtree_node *n)
