@@ -42,8 +42,21 @@ struct vox_camera {
     struct vox_camera_interface *iface;
 };
 
-/* camera.h:175: methods of a camera class by name ("simple-camera",
- * "doom-camera"); NULL for any other name. */
+/* modules.h:15-54: a module is `<name>.so` whose module_init() returns its
+ * class and methods; it is looked for in $VOXVISION_MODULES (and in the
+ * module directory the library was built with, VOX_MODULE_PATH, if any).
+ * NULL when it is not found, cannot be opened or is of another class. */
+#define CAMERA_MODULE 0
+struct vox_module_methods;
+struct vox_module {
+    int type;
+    struct vox_module_methods *methods;
+};
+struct vox_module_methods *vox_load_module(const char *name, int type);
+
+/* camera.h:175: methods of a camera class by name: the built-in
+ * "simple-camera" and "doom-camera" (which the GPU computes itself), or the
+ * camera module of that name (which vox_render asks for every ray). */
 struct vox_camera_interface *vox_camera_methods(const char *name);
 /* camera.h:146 */
 void vox_use_camera_methods(struct vox_camera *camera, const struct vox_camera_interface *iface);

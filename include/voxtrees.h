@@ -59,6 +59,11 @@ struct vox_node *vox_make_tree_host(vox_dot set[], size_t n);
 void vox_destroy_tree(struct vox_node *tree);
 /* tree.h:72 */
 size_t vox_voxels_in_tree(const struct vox_node *tree);
+/* datareader.h:40-53 -- `filename` as given, else in the data directory the
+ * library was built with (VOX_DATA_PATH, if any), else in $VOXVISION_DATA
+ * ($HOME/.voxvision when unset); the path found goes to `fullpath` (PATH_MAX
+ * bytes).  1 if found. */
+int vox_find_data_file(const char *filename, char *fullpath);
 /* tree.h:130 -- print the tree to stdout, node by node (the reference's text). */
 void vox_dump_tree(const struct vox_node *tree);
 /* geom.h:59-73 -- L1 distance, squared distance, squared norm (summed in axis order). */

@@ -34,7 +34,7 @@ CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-fvisibility=hidden", "-ffp-contract=
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall"]
 
 CUDA_SOURCES = ["voxtrees_cuda.cu", "batch.cu", "server.cu", "build.cu", "raysort.cu", "make_tree.cu"]
-C_SOURCES = ["host_tree.c", "cameras.c", "lights.c"]
+C_SOURCES = ["host_tree.c", "cameras.c", "lights.c", "modules.c"]
 CXX_SOURCES = ["flatten.cpp", "dropin_search.cpp", "renderer.cpp"]
 
 
@@ -102,7 +102,7 @@ def build(verbose: bool = False, force: bool = False, checked: bool = False) -> 
         raise RuntimeError(f"compilation failed: {failed}")
     if jobs or not os.path.exists(lib):
         tmp = lib + ".tmp"
-        cmd = [nvcc, ARCH, "-shared", "-o", tmp, *objs, "-Xlinker", "-Bsymbolic", "-lpthread"]
+        cmd = [nvcc, ARCH, "-shared", "-o", tmp, *objs, "-Xlinker", "-Bsymbolic", "-lpthread", "-ldl"]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode:
             sys.stdout.write(r.stdout)

@@ -383,12 +383,14 @@ static struct vox_camera *doom_construct(const struct vox_camera *old)
     return (struct vox_camera *)c;
 }
 
+/* camera.c:43-48: the methods of a camera class by name -- the two built-in
+ * classes, or a camera module of that name (modules.c). */
 EXPORT struct vox_camera_interface *vox_camera_methods(const char *name)
 {
     if (!name) return NULL;
     if (strcmp(name, "simple-camera") == 0) return &simple_methods;
     if (strcmp(name, "doom-camera") == 0) return &doom_methods;
-    return NULL;
+    return (struct vox_camera_interface *)vox_load_module(name, CAMERA_MODULE);
 }
 
 /* For the renderer: the vox_cuda_camera state of a built-in camera, or -1
