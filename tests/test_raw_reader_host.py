@@ -4,7 +4,6 @@ reference's error strings."""
 import ctypes as C
 
 import numpy as np
-import pytest
 
 import voxvision_gb300 as vg
 from voxvision_gb300._lib import RawTest
