@@ -1481,7 +1481,7 @@ EXPORT int vox_cuda_tree_build_raw(const void *samples, const unsigned dim[3], u
 try {
     int rc = check_raw_args(dim, samplesize, test);
     if (rc) return rc;
-    if (!samples && (uint64_t)dim[0] * dim[1] * dim[2]) return VOX_CUDA_EINVAL;
+    if (!samples && (uint64_t)dim[0] * dim[1] * dim[2] != 0) return VOX_CUDA_EINVAL;
     return new_tree(out, [&](vox_cuda_tree *t, cudaStream_t s) {
         return raw_build(t, samples, dim, samplesize, test, s);
     });
