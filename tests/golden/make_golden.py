@@ -11,8 +11,9 @@ Run in a container that has the reference sources (default /root/reference):
 
 Every expected value here comes from the reference's compiled code:
 vox_make_tree, vox_insert_voxel, vox_delete_voxel, vox_ray_tree_intersection,
-vox_tree_ball_collidep (src/voxtrees/tree.c, search.c, geom.c) and the
-simple-camera / doom-camera plugins (src/voxrnd/*-camera.c, vect-ops.c).
+vox_tree_ball_collidep, the geom.c metrics and vox_dump_tree
+(src/voxtrees/tree.c, search.c, geom.c) and the simple-camera / doom-camera
+plugins with their vector helpers (src/voxrnd/*-camera.c, vect-ops.c).
 The oracle library is used only to serialise the reference-built trees
 (orc_dump / orc_preorder walk the same struct layout).  The fixtures are
 small .npz files that the tests read on any host; this script is the only
