@@ -48,8 +48,8 @@ def test_refresh_after_edits(lib):
     img, ref = _frame(vg, dt, root, cam, tex)
     assert np.array_equal(img, ref)
     rng = np.random.default_rng(12)
-    for rnd in range(3):
-        n_ins = (200, 3000, 100)[rnd]                  # round 2 grows the tree past its old pool
+    for batch in range(3):
+        n_ins = (200, 3000, 100)[batch]                # the second batch grows the tree past its old pool
         for _ in range(n_ins):
             a = rng.integers(-8, 72, 3).astype(np.float32)
             L.vox_insert_voxel(C.byref(root), a.ctypes.data_as(C.c_void_p))
@@ -58,7 +58,7 @@ def test_refresh_after_edits(lib):
             L.vox_delete_voxel(C.byref(root), a.ctypes.data_as(C.c_void_p))
         vg.check(L.vox_cuda_tree_refresh(dt.h, root), "vox_cuda_tree_refresh")
         img, ref = _frame(vg, dt, root, cam, tex)
-        assert np.array_equal(img, ref), f"round {rnd}: {(img != ref).sum()} pixels differ"
+        assert np.array_equal(img, ref), f"batch {batch}: {(img != ref).sum()} pixels differ"
         # rays through the batch entry point report the edited tree's leaves
         o = np.tile(np.float32([150, -90, 100]), (500, 1))
         d = (rng.uniform(-1, 1, (500, 3)) + np.float32([-0.7, 0.8, -0.45])).astype(np.float32)
