@@ -43,7 +43,6 @@ import argparse
 import json
 import math
 import os
-import re
 import subprocess
 import sys
 import tempfile
@@ -62,7 +61,7 @@ CENTRE = (128.0, 128.0, 128.0)
 RADIUS = 1.5 * 256 * math.sqrt(3.0)
 METRIC = "Mrays/s at 1080p on 256^3"
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
-TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "batch_orbit_1080p_256.md")
+TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "batch_orbit_1080p_256.json")
 
 
 def parse_args():
@@ -111,29 +110,94 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def workload_config(info=None, voxels=None):
-    cfg = {"workload": "orbit-1080p-256^3-best", "volume": "256^3 u8 value noise, seed 2, band ~8% solid",
-           "frames_per_step": NFRAMES, "resolution": f"{W}x{H}", "quality": "BEST",
-           "camera": "simple-camera fov 1.0, orbit r=665.1 elev 20deg",
-           "rays_per_step": NFRAMES * W * H, "l2": "flushed between steps (256 MiB write)"}
-    if voxels is not None:
-        cfg["voxels"] = int(voxels)
-    if info:
-        cfg.update({"tree_nodes": info["nodes"], "tree_depth": info["depth"],
-                    "tree_bytes": info["device_bytes"]})
-    return cfg
+def workload_config(voxels, nframes=NFRAMES):
+    """The workload as both arms name it (the same dict in both lines)."""
+    return {"workload": "orbit-1080p-256^3-best", "volume": "256^3 u8 value noise, seed 2, band ~8% solid",
+            "voxels": int(voxels), "frames_per_step": nframes, "resolution": f"{W}x{H}", "quality": "BEST",
+            "camera": "simple-camera fov 1.0, orbit r=665.1 elev 20deg",
+            "rays_per_step": nframes * W * H, "l2": "flushed between steps (256 MiB write)"}
+
+
+def workloads():
+    """The seeded workload generators (voxvision_gb300/workloads.py, numpy
+    only), loaded from their file so that the reference arm imports nothing
+    of the library package."""
+    import importlib.util
+    mod = sys.modules.get("_orbit_workloads")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("_orbit_workloads",
+                                                      os.path.join(ROOT, "voxvision_gb300", "workloads.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        sys.modules["_orbit_workloads"] = mod
+    return mod
 
 
 def make_workload(build_tree):
-    from voxvision_gb300 import workloads as wl
+    wl = workloads()
     vox = wl.voxels_from_mask(wl.noise_volume(VOLUME, SEED, SOLID))
     tree = build_tree(vox)
     return vox, tree, wl.texture32(7)
 
 
 def orbit_states():
+    """The library's simple-camera set up for every orbit frame."""
     from voxvision_gb300.cameras import orbit_camera
     return [orbit_camera(f, NFRAMES, W, H, CENTRE, RADIUS).state() for f in range(NFRAMES)]
+
+
+def oracle_orbit_states():
+    """The same cameras set up by the oracle's restatement of simple-camera.c
+    (bit-identical to the library's: tests/test_oracle_golden.py)."""
+    from oracle import oracle as orc
+    wl = workloads()
+    return [orc.camera_simple(wl.orbit_pose(f, NFRAMES, CENTRE, RADIUS, 20.0), CENTRE, W, H, 1.0)
+            for f in range(NFRAMES)]
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu), or what /proc/cpuinfo says."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_reference_details(tree_ptr, states, tex, cores):
+    """Beside the all-core figure: the CPU model, one core's Mrays/s (the
+    oracle's BEST render on one thread over two orbit frames), and the same
+    frames drawn by the restatement compiled with floating-point contraction
+    on (the compiler's default in the reference's release build): its speed
+    and how many pixels differ from the contraction-off frames."""
+    from oracle import oracle as orc
+    picked = [0, 61]
+    t0 = time.perf_counter()
+    off = [orc.render_best(tree_ptr, states[f], W, H, tex, nthreads=1)[0] for f in picked]
+    single = len(picked) * W * H / (time.perf_counter() - t0) / 1e6
+    t0 = time.perf_counter()
+    on = [orc.render_best_contracted(tree_ptr, states[f], W, H, tex, nthreads=cores)[0] for f in picked]
+    fc_value = len(picked) * W * H / (time.perf_counter() - t0) / 1e6
+    t0 = time.perf_counter()
+    for f in picked:
+        orc.render_best(tree_ptr, states[f], W, H, tex, nthreads=cores)
+    off_value = len(picked) * W * H / (time.perf_counter() - t0) / 1e6
+    differ = int(sum(int((a != b).sum()) for a, b in zip(off, on)))
+    return {"cpu_model": cpu_model(), "single_core_value": single,
+            "single_core_sample": f"orbit frames {picked} at {W}x{H}, BEST, 1 thread",
+            "fp_contract_fast": {"value": fc_value, "value_contract_off": off_value, "cores": cores,
+                                 "pixels_differing": differ, "pixels": len(picked) * W * H,
+                                 "what": "the restatement compiled with -ffp-contract=fast (liboracle_fc.so), "
+                                         "same tree and frames"}}
 
 
 class ClockSampler:
@@ -197,14 +261,16 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def traffic_per_launch():
-    """dram bytes per render launch from the committed ncu summary, if any."""
+def traffic_per_launch(nframes):
+    """DRAM bytes (read + write) per batch launch of `nframes` orbit frames,
+    from the committed ncu figures of the kernel (scaled by frames, which the
+    reads of tree misses and the frame stores both follow), if any."""
     try:
-        txt = open(TRAFFIC_SUMMARY).read()
-    except OSError:
+        with open(TRAFFIC_SUMMARY) as f:
+            p = json.load(f)
+        return float(p["traffic_bytes_per_launch"]) * nframes / float(p["frames_per_launch"])
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
-    return float(m.group(1)) if m else None
 
 
 def l2_copy_gbs(torch):
@@ -243,6 +309,32 @@ def cpu_baseline_sample(tree_ptr, states, tex, budget_s=3.0):
             "sample": f"{frames} of the {NFRAMES} orbit frames at {W}x{H}, BEST, {dt:.2f} s wall"}
 
 
+
+
+def oracle_check_orbit(frames_dev, vox, lib_tree_ptr, tex, nf):
+    """Every frame of the timed batch launch against the oracle: the tree
+    built by the oracle's restatement of tree.c from the same voxels (and
+    compared node for node with the library's), the cameras set up by its
+    restatement of simple-camera.c, each frame drawn by its BEST loop."""
+    from oracle import oracle as orc
+    orc.set_voxel((1, 1, 1))
+    t0 = time.perf_counter()
+    ot = orc.OracleTree.from_voxels(vox)
+    a, b = orc.dump_tree(lib_tree_ptr), ot.dump()
+    tree_same = a.keys() == b.keys() and all(np.array_equal(a[k], b[k]) for k in a)
+    states = oracle_orbit_states()
+    host = frames_dev.cpu().numpy().view(np.uint32)
+    n = orc.nthreads_default()
+    bad = []
+    for f in range(nf):
+        ref, _ = orc.render_best(ot.ptr, states[f], W, H, tex, nthreads=n)
+        if not np.array_equal(host[f].reshape(H, W), ref):
+            bad.append(f)
+    return {"frames_checked": nf, "frames_identical_oracle": not bad, "frames_differing": bad[:10],
+            "tree_identical_oracle": bool(tree_same), "oracle_tree_nodes": int(ot.node_count()),
+            "check_s": time.perf_counter() - t0,
+            "what": "every frame of the timed batch launch vs the oracle's BEST render over the oracle-built "
+                    "tree with oracle-set-up cameras; the library's tree vs the oracle's, node for node"}
 
 
 def timed_reps(torch, fn, reps, flush):
@@ -773,7 +865,7 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     mean_launch_s = float(np.mean(step_ms)) * 1e-3
     achieved = traced_bytes_step / mean_launch_s / 1e9
-    traffic = traffic_per_launch()
+    traffic = traffic_per_launch(nf)
     l2 = l2_copy_gbs(torch)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
@@ -799,8 +891,9 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sum(step_ms) / len(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(workload_config(info, len(vox)), frames_per_step=nf, rays_per_step=rays_step), "roofline": roofline, "e2e": e2e,
-            "gpu_launches": int(launches), "clocks": clk}
+            "config": workload_config(len(vox), nf), "roofline": roofline, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk,
+            "tree": {"nodes": info["nodes"], "depth": info["depth"], "device_bytes": info["device_bytes"]}}
     if not args.no_extras:
         # the request server first: its latencies are the extras most easily
         # disturbed by what ran before in the process
@@ -812,8 +905,13 @@ def run_ours(args):
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
         line["editing"] = measure_editing(vg, vox)
         line["tree_build"] = measure_tree_build(vg)
-    if not args.no_cpu_baseline and world >= 1:
-        line["cpu_baseline"] = cpu_baseline_sample(ht.ptr, states, tex)
+    if not args.no_cpu_baseline:
+        # the CPU leg: the oracle checks every timed frame (the last launch's
+        # nf device frames) over its own tree and cameras, then is timed
+        line["parity"] = oracle_check_orbit(frames_dev, vox, ht.ptr, tex, nf)
+        cb = cpu_baseline_sample(ht.ptr, states, tex)
+        cb.update(cpu_reference_details(ht.ptr, states, tex, cb["cores"]))
+        line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -828,7 +926,7 @@ def run_reference(args):
     from oracle import oracle as orc
     orc.set_voxel((1, 1, 1))
     vox, tree, tex = make_workload(orc.OracleTree.from_voxels)
-    states = orbit_states()
+    states = oracle_orbit_states()
     n = orc.nthreads_default()
 
     def step():
@@ -845,10 +943,12 @@ def run_reference(args):
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(None, len(vox)), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": n, "kind": "port",
-                             "sample": f"full {NFRAMES}-frame orbit per step, {W}x{H}, BEST, "
-                                       f"C restatement of search.c/renderer.c on {n} threads"},
+            "config": workload_config(len(vox)), "impl": "reference",
+            "cpu_baseline": dict({"value": value, "unit": "Mrays/s", "cores": n, "kind": "port",
+                                  "sample": f"full {NFRAMES}-frame orbit per step, {W}x{H}, BEST, "
+                                            f"C restatement of tree.c/search.c/renderer.c/simple-camera.c "
+                                            f"on {n} threads"},
+                                 **cpu_reference_details(tree.ptr, states, tex, n)),
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

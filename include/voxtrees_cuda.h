@@ -164,6 +164,40 @@ int vox_cuda_tree_image(const vox_cuda_tree *tree, void *units, size_t units_cap
  * the tree exceeds the image limits. */
 int vox_cuda_tree_flatten_host(const struct vox_node *root, void *units, size_t units_cap,
                                uint32_t *rec_of_id, size_t ids_cap, size_t *n_units, size_t *n_ids);
+
+/* ---- vox_dot layouts -------------------------------------------------------
+ * A voxvision built with SSE_INTRIN (its default on x86, CMakeLists.txt:19)
+ * has a 16-byte vox_dot -- float[4] aligned to 16 bytes -- so its struct
+ * vox_box is 32 bytes and its struct vox_node 128 (voxvision.h.in:45-57,
+ * tree.h:22-38).  Without SSE_INTRIN vox_dot is float[3] and struct vox_node
+ * 112 bytes: the layout include/voxtrees.h declares, the only one on aarch64,
+ * and the one the calls above read.  The *_layout calls read a tree of either
+ * layout (VOX_CUDA_LAYOUT_*); `voxel` is the voxel size to embed (3 floats,
+ * NULL: this library's vox_voxel).  A tree of the SSE layout gives the image,
+ * and so every result, that the scalar layout of the same nodes gives;
+ * vox_cuda_tree_node returns the caller's own (SSE-layout) nodes.  Replace:
+ * nothing in the reference (its searches read its own layout in place). */
+#define VOX_CUDA_LAYOUT_SCALAR 0
+#define VOX_CUDA_LAYOUT_SSE    1
+int vox_cuda_tree_upload_layout(const struct vox_node *root, int layout, const float *voxel, vox_cuda_tree **out);
+int vox_cuda_tree_refresh_layout(vox_cuda_tree *tree, const struct vox_node *root, int layout, const float *voxel);
+int vox_cuda_tree_flatten_host_layout(const struct vox_node *root, int layout, const float *voxel, void *units,
+                                      size_t units_cap, uint32_t *rec_of_id, size_t ids_cap, size_t *n_units,
+                                      size_t *n_ids);
+/* Code compiled against a voxvision.h with SSE_INTRIN defined (which makes
+ * its vox_dot 16 bytes) that includes this header gets the SSE reading under
+ * the plain names, with its own vox_voxel, as its voxvision.h picks its
+ * vox_dot.  Define VOX_CUDA_KEEP_SCALAR_NAMES to turn this off. */
+#if defined(SSE_INTRIN) && !defined(VOX_CUDA_KEEP_SCALAR_NAMES)
+#define vox_cuda_tree_upload(root, out) \
+    vox_cuda_tree_upload_layout((root), VOX_CUDA_LAYOUT_SSE, vox_voxel, (out))
+#define vox_cuda_tree_refresh(tree, root) \
+    vox_cuda_tree_refresh_layout((tree), (root), VOX_CUDA_LAYOUT_SSE, vox_voxel)
+#define vox_cuda_tree_flatten_host(root, units, units_cap, rec_of_id, ids_cap, n_units, n_ids)             \
+    vox_cuda_tree_flatten_host_layout((root), VOX_CUDA_LAYOUT_SSE, vox_voxel, (units), (units_cap), (rec_of_id), \
+                                      (ids_cap), (n_units), (n_ids))
+#endif
+
 /* The check every upload makes before copying an image (no GPU is used):
  * every offset a search can follow from the root record stays inside the
  * n_units units, every kind is known, leaf ids are below n_nodes, and each of
@@ -380,8 +414,12 @@ int vox_cuda_batch_free(vox_cuda_batch *batch);
  * until exit.  Frames are bit-identical to vox_cuda_render_device's.
  * More than VOX_CUDA_NOALLOC_MAX_JOBS jobs: VOX_CUDA_ECAPACITY.  All calls
  * share the array: calls whose work overlaps on the GPU race and must be
- * ordered (same stream, or synchronised).  The first call on a device looks
- * up the array's address; make it before starting any stream capture. */
+ * ordered (same stream, or synchronised).  The job table reaches the GPU as
+ * a kernel argument, so the call neither copies from host memory nor waits
+ * for earlier work on `stream`.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and caches it for the process: make
+ * that first call before starting any stream capture, and do not call this
+ * after cudaDeviceReset on that device. */
 #define VOX_CUDA_NOALLOC_MAX_JOBS 64
 int vox_cuda_render_frames_noalloc(const vox_cuda_frame_job *jobs, uint32_t njobs, void *stream);
 

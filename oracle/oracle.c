@@ -570,6 +570,69 @@ void orc_screen2world(const orc_camera *cam, int sx, int sy, float *ray)
     for (int i = 0; i < 3; i++) ray[i] = v[i] + cam->rotation[0] * t[i] + t2[i];
 }
 
+/* vect-ops.c:16-24 vox_quat_mul: res = q1 * q2 (res may alias either). */
+static void quat_mul(const float *q1, const float *q2, float *res)
+{
+    float e1 = q1[0], i1 = q1[1], j1 = q1[2], k1 = q1[3];
+    float e2 = q2[0], i2 = q2[1], j2 = q2[2], k2 = q2[3];
+    res[0] = e1 * e2 - i1 * i2 - j1 * j2 - k1 * k2;
+    res[1] = j1 * k2 - k1 * j2 + i1 * e2 + e1 * i2;
+    res[2] = k1 * i2 - i1 * k2 + j1 * e2 + e1 * j2;
+    res[3] = i1 * j2 - j1 * i2 + k1 * e2 + e1 * k2;
+}
+
+/* vect-ops.c:38-46 vox_rotate_vector_q: the vector part of `v` rotated by
+ * `q` into res[1..3]; res[0] is left alone. */
+static void rotate_vector_q(const float *q, const float *v, float *res)
+{
+    float t[3], t2[3];
+    cross(q + 1, v + 1, t);
+    for (int i = 0; i < 3; i++) t[i] = t[i] * 2.0f;
+    cross(q + 1, t, t2);
+    for (int i = 0; i < 3; i++) res[i + 1] = v[i + 1] + q[0] * t[i] + t2[i];
+}
+
+/* A simple-camera as vox_simple_camera_construct, set_property_number("fov"),
+ * set_window_size, set_property_dot("position") and look_at leave it
+ * (simple-camera.c:139-159, :161-165, :120-136, :167-170, :106-118 with
+ * simple_rotate_camera :50-99 and vect-ops.c:48-58 vox_quat_normalize).
+ * Host-side set-up only: the renderer reads the resulting fields. */
+void orc_camera_simple(orc_camera *cam, const float position[3], const float target[3], int w, int h, float fov)
+{
+    memset(cam, 0, sizeof *cam);
+    cam->kind = 0;
+    if (w > h) {                                  /* simple-camera.c:124-135 */
+        cam->xsub = fov;
+        cam->ysub = fov * h / w;
+        cam->mul = fov * 2 / w;
+    } else {
+        cam->ysub = fov;
+        cam->xsub = fov * w / h;
+        cam->mul = fov * 2 / h;
+    }
+    for (int i = 0; i < 3; i++) cam->position[i] = position[i];
+    float *q = cam->rotation;
+    q[0] = 1.0f; q[1] = q[2] = q[3] = 0.0f;       /* vox_quat_set_identity */
+    float sub[3], rot[3];
+    for (int i = 0; i < 3; i++) sub[i] = target[i] - cam->position[i];
+    rot[0] = atan2f(sub[2], hypotf(sub[0], sub[1]));
+    rot[1] = 0;
+    rot[2] = -atan2f(sub[0], sub[1]);
+    static const float orts[3][4] = {{0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+    for (int i = 2; i >= 0; i--) {                /* z, then y, then x axis of the camera */
+        float r[4];
+        rotate_vector_q(q, orts[i], r);
+        float s = sinf(rot[i] / 2), c = cosf(rot[i] / 2);
+        for (int j = 0; j < 3; j++) r[j + 1] = s * r[j + 1];
+        r[0] = c;
+        quat_mul(r, q, q);
+    }
+    float sum = 0;
+    for (int i = 0; i < 4; i++) sum += q[i] * q[i];
+    float norm = sqrtf(sum);
+    for (int i = 0; i < 4; i++) q[i] /= norm;
+}
+
 /* ------------------------------------------------------------------ */
 /* light manager and its M-tree (src/voxrnd/lights.c,                  */
 /* src/voxtrees/mtree.c), restated recursively as the reference has it  */

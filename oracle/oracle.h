@@ -102,6 +102,12 @@ int orc_ray_counts_per_ray(const struct orc_node *root, size_t n, const float *o
 
 void orc_screen2world(const orc_camera *cam, int sx, int sy, float *ray);
 
+/* A simple-camera of field of view `fov` (horizontal when w > h) for a w x h
+ * window at `position`, looking at `target`: the fields that
+ * set_property_number("fov"), set_window_size, set_property_dot("position")
+ * and look_at leave in the reference's camera (simple-camera.c:106-170). */
+void orc_camera_simple(orc_camera *cam, const float position[3], const float target[3], int w, int h, float fov);
+
 /* vox_render, quality BEST (renderer.c:200-319, branch :308) into a linear
  * ARGB8888 framebuffer; misses stay 0 (vox_redraw clears, renderer.c:324). */
 int orc_render_best(const struct orc_node *tree, const orc_camera *cam,

@@ -16,9 +16,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+LIB_FC_PATH = os.path.join(HERE, "_build", "liboracle_fc.so")   # the same with FP contraction on
 REF_DIR = os.path.join(HERE, "_ref")
 
 _lib = None
+_lib_fc = None
 
 
 def build(force: bool = False) -> str:
@@ -27,6 +29,30 @@ def build(force: bool = False) -> str:
             os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     return LIB_PATH
+
+
+def render_best_contracted(tree_ptr, state: dict, w: int, h: int, texture: np.ndarray, nthreads=None):
+    """render_best by the restatement compiled with floating-point contraction
+    on (liboracle_fc.so): what a build with the compiler's default
+    contraction draws, for the CPU baseline's comparison only."""
+    global _lib_fc
+    if _lib_fc is None:
+        build()
+        if not os.path.exists(LIB_FC_PATH):
+            subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+        L = C.CDLL(LIB_FC_PATH)
+        L.orc_render_best.argtypes = [C.c_void_p, C.POINTER(OrcCamera), C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_int]
+        L.orc_render_best.restype = C.c_int
+        _lib_fc = L
+    tex = np.ascontiguousarray(texture, dtype=np.uint8)
+    out = np.zeros(w * h, np.uint32)
+    cnt = np.zeros(3, np.uint64)
+    rc = _lib_fc.orc_render_best(tree_ptr, C.byref(camera(state)), w, h, _p(tex), _p(out), _p(cnt),
+                                 nthreads or nthreads_default())
+    if rc != 0:
+        raise ValueError("bad geometry: width must be a multiple of 16 and height of 4")
+    return out.reshape(h, w), cnt
 
 
 class OrcCamera(C.Structure):
@@ -51,6 +77,7 @@ def lib():
         L.orc_ray_batch.argtypes = [vp, vp, sz, fp, fp, vp, vp, fp, vp, C.c_int]
         L.orc_ball_batch.argtypes = [vp, sz, fp, fp, vp, vp, C.c_int]
         L.orc_screen2world.argtypes = [C.POINTER(OrcCamera), C.c_int, C.c_int, fp]
+        L.orc_camera_simple.argtypes = [C.POINTER(OrcCamera), fp, fp, C.c_int, C.c_int, C.c_float]
         L.orc_render_best.argtypes = [vp, C.POINTER(OrcCamera), C.c_int, C.c_int, vp, vp, vp, C.c_int]
         L.orc_render_best.restype = C.c_int
         L.orc_render_quality.argtypes = [vp, C.POINTER(OrcCamera), C.c_int, C.c_int, C.c_uint, vp, vp,
@@ -178,6 +205,19 @@ def camera(state: dict) -> OrcCamera:
         cam.rays = rays.ctypes.data
         cam.rays_w = rays.shape[1]
     return cam
+
+
+def camera_simple(position, target, w: int, h: int, fov: float = 1.0) -> dict:
+    """The state of a simple-camera set up for a w x h window at `position`
+    looking at `target` (the oracle's restatement of simple-camera.c's
+    set-up), as a camera-state dict for render_best and friends."""
+    cam = OrcCamera()
+    pos = np.ascontiguousarray(np.asarray(position, np.float32).reshape(3))
+    tgt = np.ascontiguousarray(np.asarray(target, np.float32).reshape(3))
+    lib().orc_camera_simple(C.byref(cam), _p(pos), _p(tgt), int(w), int(h), float(fov))
+    return dict(kind=0, position=np.array(cam.position[:], np.float32),
+                rotation=np.array(cam.rotation[:], np.float32), mul=np.float32(cam.mul),
+                xsub=np.float32(cam.xsub), ysub=np.float32(cam.ysub), fov=np.float32(fov))
 
 
 def screen2world(state: dict, sx: int, sy: int) -> np.ndarray:

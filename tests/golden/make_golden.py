@@ -1,13 +1,17 @@
 """Generate the golden vectors under tests/golden/ from the reference itself.
 
-Run in a container that has the reference sources (default /root/reference):
+Run where the reference sources are present (REF = the voxvision source tree):
 
-    make -C oracle ref            # compiles the reference's own voxtrees and
+    make -C oracle ref REF=...    # compiles the reference's own voxtrees and
                                   # camera sources into oracle/_ref/
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py edits    # the tree-editing fixtures only
     python tests/golden/make_golden.py vectops  # the vector-helper fixture only
     python tests/golden/make_golden.py geom     # the metrics and tree-dump fixture only
+    make -C oracle ref-sse REF=... && python tests/golden/make_golden.py sse
+                                                # the SSE-layout trees (x86 hosts only)
+    make -C oracle ref-lights REF=... && python tests/golden/make_golden.py lights
+                                                # the light manager and its M-tree
 
 Every expected value here comes from the reference's compiled code:
 vox_make_tree, vox_insert_voxel, vox_delete_voxel, vox_ray_tree_intersection,
@@ -511,6 +515,230 @@ def edit_cases():
     edit_case("edit_voxsize", v, start, edit_ops(rng, 500, -2, 12, v, start))
 
 
+# ---------------------------------------------------------------- SSE layout
+
+class Node16(C.Structure):
+    """struct vox_node of a voxvision built with SSE_INTRIN (tree.h:28-38 with
+    the 16-byte aligned float[4] vox_dot of voxvision.h.in:45-57): box 32
+    bytes, flags and dots_num, 8 bytes of padding, the union at byte 48
+    (a dots pointer, or the centre and 8 children): 128 bytes."""
+    _fields_ = [("bmin", C.c_float * 4), ("bmax", C.c_float * 4), ("flags", C.c_uint), ("dots_num", C.c_uint),
+                ("pad", C.c_uint * 2), ("u", C.c_float * 4), ("children", vp * 8)]
+
+
+assert C.sizeof(Node16) == 128
+
+
+def f4(a):
+    """(n, 3) floats as (n, 4) rows of a 16-byte aligned array (vox_dot of the SSE build)."""
+    a = np.asarray(a, np.float32).reshape(-1, 3)
+    buf = np.zeros(a.shape[0] * 4 + 4, np.float32)
+    off = (-buf.ctypes.data % 16) // 4
+    out = buf[off: off + a.shape[0] * 4].reshape(-1, 4)
+    out[:, :3] = a
+    assert out.ctypes.data % 16 == 0
+    return out
+
+
+def dump16(root):
+    """Pre-order dump (the oracle's dump fields) of an SSE-layout tree, and
+    the node pointers in that order."""
+    flags, dnum, boxes, centers, mask, doff, dots, ptrs = [], [], [], [], [], [], [], []
+    stack = [root] if root else []
+    nd = 0
+    while stack:
+        p = stack.pop()
+        n = Node16.from_address(p)
+        ptrs.append(p)
+        flags.append(n.flags); dnum.append(n.dots_num)
+        boxes.append(list(n.bmin[:3]) + list(n.bmax[:3]))
+        doff.append(nd)
+        c, m = [0.0, 0.0, 0.0], 0
+        if n.flags & 2:
+            pass
+        elif n.flags & 1:
+            base = C.c_void_p.from_address(p + 48).value
+            arr = (C.c_float * (4 * n.dots_num)).from_address(base)
+            d = np.frombuffer(arr, np.float32).reshape(-1, 4)[:, :3]
+            dots.append(d.copy())
+            nd += n.dots_num
+        else:
+            c = list(n.u[:3])
+            for o in range(7, -1, -1):
+                if n.children[o]:
+                    m |= 1 << o
+                    stack.append(n.children[o])
+        centers.append(c); mask.append(m)
+    d = dict(flags=np.asarray(flags, np.uint32), dots_num=np.asarray(dnum, np.uint32),
+             boxes=np.asarray(boxes, np.float32).reshape(-1, 6), centers=np.asarray(centers, np.float32).reshape(-1, 3),
+             child_mask=np.asarray(mask, np.uint8), dot_offset=np.asarray(doff, np.uint64),
+             dots=np.concatenate(dots).astype(np.float32) if dots else np.zeros((0, 3), np.float32))
+    return d, ptrs
+
+
+def sse_layout_case():
+    """Trees built by the reference compiled with SSE_INTRIN on (the 16-byte
+    vox_dot and 128-byte struct vox_node of its default x86 build), dumped in
+    pre-order with their SSE build's own ray and ball answers: the fixture of
+    the SSE-layout upload (tests/test_sse_layout.py).  Needs an x86 host
+    (make -C oracle ref-sse)."""
+    sse = C.CDLL(os.path.join(REF, "libvoxtrees_ref_sse.so"))
+    sse.vox_make_tree.argtypes = [vp, C.c_size_t]; sse.vox_make_tree.restype = vp
+    sse.vox_destroy_tree.argtypes = [vp]
+    sse.vox_ray_tree_intersection.argtypes = [vp, vp, vp, vp]; sse.vox_ray_tree_intersection.restype = vp
+    sse.vox_tree_ball_collidep.argtypes = [vp, vp, C.c_float]; sse.vox_tree_ball_collidep.restype = C.c_int
+    sse.vox_set_voxel_size.argtypes = [C.c_float] * 3
+    g = np.mgrid[-12:12, -12:12, -12:12].reshape(3, -1).T
+    ball = g[(g ** 2).sum(1) < 144].astype(np.float32)
+    rng = np.random.default_rng(71)
+    cloud = np.unique(rng.integers(0, 48, (3000, 3)), axis=0).astype(np.float32)
+    rng.shuffle(cloud)
+    dup = np.concatenate([np.tile([[3, 3, 3]], (12, 1)), np.mgrid[0:3, 0:3, 0:2].reshape(3, -1).T,
+                          [[9, 1, 4], [9, 2, 4], [10, 2, 4]]]).astype(np.float32)
+    v = (0.5, 1.0, 2.0)
+    gg = np.mgrid[-8:8, -8:8, -8:8].reshape(3, -1).T
+    vv = (gg[((gg ** 2).sum(1) < 64) & ((gg[:, 0] + gg[:, 1]) % 3 != 0)] * np.asarray(v)).astype(np.float32)
+    blob = wl.voxels_from_mask(wl.blobs_volume(64, 20, 1, 0.20))
+    cases = [("ball", ball, (1.0, 1.0, 1.0)), ("cloud", cloud, (1.0, 1.0, 1.0)), ("overflow", dup, (1.0, 1.0, 1.0)),
+             ("voxsize", vv, v), ("blob64", blob, (1.0, 1.0, 1.0))]
+    out = {"cases": np.array([c[0] for c in cases])}
+    for k, (name, vox, voxel) in enumerate(cases):
+        sse.vox_set_voxel_size(*voxel)
+        s4 = f4(vox)
+        t = sse.vox_make_tree(P(s4), s4.shape[0])
+        d, ptrs = dump16(t)
+        pmap = {p: i for i, p in enumerate(ptrs)}
+        bmin, bmax = d["boxes"][0][:3], d["boxes"][0][3:]
+        o, dr = edge_rays(bmin, bmax, 3000, 80 + k, np.asarray(voxel, np.float64))
+        leaf = np.full(len(o), 0xFFFFFFFF, np.uint32)
+        pts = np.zeros((len(o), 3), np.float32)
+        o4, d4, r4 = f4(o), f4(dr), f4(np.zeros((1, 3)))
+        for i in range(len(o)):
+            r = sse.vox_ray_tree_intersection(t, o4[i].ctypes.data, d4[i].ctypes.data, r4[0].ctypes.data)
+            if r:
+                leaf[i] = pmap[int(r)]
+                pts[i] = r4[0, :3]
+        c, rad = edge_balls(bmin, bmax, 1500, 90 + k)
+        c4 = f4(c)
+        hit = np.array([sse.vox_tree_ball_collidep(t, c4[i].ctypes.data, C.c_float(float(rad[i])))
+                        for i in range(len(c))], np.uint8)
+        out.update({f"{name}_voxel": np.asarray(voxel, np.float32), f"{name}_voxels": np.asarray(vox, np.float32),
+                    f"{name}_ray_origins": o, f"{name}_ray_dirs": dr, f"{name}_ray_leaf": leaf,
+                    f"{name}_ray_points": pts, f"{name}_ball_centres": c, f"{name}_ball_radii": rad,
+                    f"{name}_ball_hit": hit})
+        out.update({f"{name}_tree_{key}": val for key, val in d.items()})
+        print(f"sse {name}: nodes={len(ptrs)} rays hit={np.mean(leaf != 0xFFFFFFFF):.3f}")
+        sse.vox_destroy_tree(t)
+    sse.vox_set_voxel_size(1.0, 1.0, 1.0)
+    path = os.path.join(OUT, "sse_layout.npz")
+    np.savez_compressed(path, **out)
+    print(f"sse_layout: {os.path.getsize(path)} B")
+
+
+# ---------------------------------------------------------------- lights
+
+from tests.helpers import mtree_walk  # noqa: E402
+
+
+def light_ops(seed, n, kind):
+    """A random call sequence for a light manager: insertions (valid and
+    invalid colours, radii <= 0, duplicates of live lights), removals (of
+    live lights and of missing ones) and ambient changes."""
+    rng = np.random.default_rng(seed)
+    ops, live = [], []
+    for _ in range(n):
+        u = rng.random()
+        if u < 0.62:
+            if kind == "overlap":          # tests.c:856-882: many large overlapping spheres
+                c = np.floor(rng.uniform(0, 100, 3)); r = float(70 + np.floor(rng.uniform(0, 30)))
+            elif kind == "float":
+                c = rng.uniform(-40, 40, 3); r = float(rng.uniform(-1, 25))
+            else:
+                c = np.floor(rng.uniform(0, 64, 3)); r = float(np.floor(rng.uniform(-2, 20)))
+            col = rng.uniform(-0.05, 1.05, 3)
+            if live and rng.random() < 0.08:
+                c, r = live[int(rng.integers(len(live)))]
+            ops.append(("insert", np.asarray(c, np.float32), np.float32(r), np.asarray(col, np.float32)))
+            live.append((np.asarray(c, np.float32), np.float32(r)))
+        elif u < 0.96:
+            if live and rng.random() < 0.85:
+                c, r = live.pop(int(rng.integers(len(live))))
+            else:
+                c, r = np.floor(rng.uniform(0, 64, 3)).astype(np.float32), np.float32(5)
+            ops.append(("delete", c, r, None))
+        else:
+            ops.append(("ambient", None, None, rng.uniform(-0.05, 1.05, 3).astype(np.float32)))
+    return ops
+
+
+def lights_case():
+    """The reference's own light manager and M-tree (lights.c, mtree.c with
+    the block-typed search cut out: make -C oracle ref-lights) driven through
+    three call sequences; every 20 calls the whole M-tree (pre-order walk,
+    float bits), the light count and vox_get_light at sample points (lights.c:
+    104-116, the sum the renderer colours a hit with) are recorded."""
+    L = C.CDLL(os.path.join(REF, "liblights_ref.so"))
+    L.vox_make_light_manager.restype = vp
+    L.vox_destroy_light_manager.argtypes = [vp]
+    L.vox_insert_shadowless_light.argtypes = [vp, vp, C.c_float, vp]; L.vox_insert_shadowless_light.restype = C.c_int
+    L.vox_delete_shadowless_light.argtypes = [vp, vp, C.c_float]; L.vox_delete_shadowless_light.restype = C.c_int
+    L.vox_set_ambient_light.argtypes = [vp, vp]; L.vox_set_ambient_light.restype = C.c_int
+    L.vox_shadowless_lights_number.argtypes = [vp]; L.vox_shadowless_lights_number.restype = C.c_int
+    L.vox_get_light.argtypes = [vp, vp, vp]
+    out = {}
+    seqs = [("int", 11, 400), ("float", 12, 400), ("overlap", 13, 300)]
+    out["sequences"] = np.array([s[0] for s in seqs])
+    for kind, seed, n in seqs:
+        ops = light_ops(seed, n, kind)
+        lm = L.vox_make_light_manager()
+        rng = np.random.default_rng(seed + 100)
+        codes, args = [], []
+        snaps = {"at": [], "count": [], "nodes": [], "node_split": [], "spheres": [], "sphere_split": [],
+                 "points": [], "light": []}
+        for i, (op, c, r, col) in enumerate(ops):
+            if op == "insert":
+                rc = L.vox_insert_shadowless_light(lm, P(c), C.c_float(r), P(col))
+                codes.append(0); args.append(np.concatenate([c, [r], col]))
+            elif op == "delete":
+                rc = L.vox_delete_shadowless_light(lm, P(c), C.c_float(r))
+                codes.append(1); args.append(np.concatenate([c, [r], [0, 0, 0]]))
+            else:
+                rc = L.vox_set_ambient_light(lm, P(col))
+                codes.append(2); args.append(np.concatenate([[0, 0, 0, 0], col]))
+            args[-1] = np.concatenate([args[-1], [rc]]).astype(np.float32)
+            if (i + 1) % 20 == 0 or i + 1 == len(ops):
+                root = C.c_void_p.from_address(lm + 16).value      # lights.c:11-14: ambient, then the tree
+                nodes, spheres = mtree_walk(root)
+                live = [a for code, a in zip(codes, args) if code == 0]
+                pts = np.asarray([a[:3] for a in live[-24:]] if live else [[0, 0, 0]], np.float32)
+                pts = np.concatenate([pts, pts + rng.normal(0, 4, pts.shape), rng.uniform(-40, 100, (40, 3))])
+                pts = np.ascontiguousarray(pts.astype(np.float32))
+                light = np.zeros_like(pts)
+                for k in range(len(pts)):
+                    L.vox_get_light(lm, P(pts[k]), P(light[k]))
+                snaps["at"].append(i + 1); snaps["count"].append(L.vox_shadowless_lights_number(lm))
+                snaps["nodes"].append(nodes); snaps["node_split"].append(len(nodes))
+                snaps["spheres"].append(spheres); snaps["sphere_split"].append(len(spheres))
+                snaps["points"].append(pts); snaps["light"].append(light)
+        L.vox_destroy_light_manager(lm)
+        out[f"{kind}_op"] = np.array(codes, np.uint8)
+        out[f"{kind}_args"] = np.array(args, np.float32)
+        out[f"{kind}_snap_at"] = np.array(snaps["at"], np.int32)
+        out[f"{kind}_snap_count"] = np.array(snaps["count"], np.int32)
+        out[f"{kind}_nodes"] = np.concatenate(snaps["nodes"]).astype(np.uint32)
+        out[f"{kind}_node_split"] = np.array(snaps["node_split"], np.int64)
+        out[f"{kind}_spheres"] = np.concatenate(snaps["spheres"]).astype(np.uint32)
+        out[f"{kind}_sphere_split"] = np.array(snaps["sphere_split"], np.int64)
+        out[f"{kind}_point_split"] = np.array([len(p) for p in snaps["points"]], np.int64)
+        out[f"{kind}_points"] = np.concatenate(snaps["points"]).astype(np.float32)
+        out[f"{kind}_light"] = np.concatenate(snaps["light"]).astype(np.float32)
+        print(f"lights {kind}: {len(ops)} calls, {len(snaps['at'])} snapshots, final count {snaps['count'][-1]}, "
+              f"nodes {snaps['node_split'][-1]}")
+    path = os.path.join(OUT, "lights.npz")
+    np.savez_compressed(path, **out)
+    print(f"lights: {os.path.getsize(path)} B")
+
+
 def main():
     # 1. ball of radius 12 (the reference's own tree fixture, tests.c:214-237, scaled down)
     set_voxel((1.0, 1.0, 1.0))
@@ -578,7 +806,8 @@ def main():
 
 
 if __name__ == "__main__":
-    parts = {"edits": edit_cases, "vectops": vectops_case, "geom": geom_case}
+    parts = {"edits": edit_cases, "vectops": vectops_case, "geom": geom_case, "sse": sse_layout_case,
+             "lights": lights_case}
     if sys.argv[1:] and sys.argv[1] not in parts:
         sys.exit(f"unknown fixture set {sys.argv[1]!r}; one of {sorted(parts)} or none for everything")
     if sys.argv[1:]:

@@ -1,6 +1,7 @@
 """The request server: requests from several threads, admitted by a memory
 budget and batched continuously; every result equals the same request run
-alone through the plain entry points (frames pixel-exact, ball hits exact)."""
+alone through the plain entry points and the oracle's answer over its own
+tree (frames pixel-exact, ball hits exact)."""
 import threading
 
 import numpy as np
@@ -19,11 +20,33 @@ def setup():
     import voxvision_gb300 as vg
     from voxvision_gb300 import workloads as wl
     vg.set_voxel_size((1, 1, 1))
-    hosts = [vg.HostTree.from_voxels(wl.voxels_from_mask(wl.blobs_volume(64, 20, 1, 0.20))),
-             vg.HostTree.from_voxels(wl.voxels_from_mask(wl.noise_volume(128, 8, 0.10)))]
+    from oracle import oracle as orc
+    orc.set_voxel((1, 1, 1))
+    vols = [wl.voxels_from_mask(wl.blobs_volume(64, 20, 1, 0.20)),
+            wl.voxels_from_mask(wl.noise_volume(128, 8, 0.10))]
+    hosts = [vg.HostTree.from_voxels(v) for v in vols]
     trees = [vg.DeviceTree(h.ptr) for h in hosts]
     tex = wl.texture32(7)
+    global _OTREES
+    _OTREES = [orc.OracleTree.from_voxels(v) for v in vols]   # the oracle's own trees of the same voxels
     return vg, wl, hosts, trees, tex
+
+
+_OTREES = None
+
+
+def _oracle(tex, req):
+    """The oracle's answer to a request: its BEST frame (camera state as the
+    library's camera class set it up, pinned separately to the reference's
+    camera plugins) or its ball answers, over the oracle-built tree."""
+    from oracle import oracle as orc
+    if req[0] == "frame":
+        _, ti, cam, w, h, state = req
+        ref, _ = orc.render_best(_OTREES[ti].ptr, state, w, h, tex)
+        return ref.ravel().view(np.uint8)
+    _, ti, c, r = req
+    hit, _ = orc.ball_batch(_OTREES[ti].ptr, c, r)
+    return hit
 
 
 def _requests(wl, n, seed):
@@ -40,7 +63,7 @@ def _requests(wl, n, seed):
             cam.set_position(wl.pose_position((side / 2,) * 3, 1.5 * side * 3 ** 0.5,
                                               rng.uniform(0, 2 * np.pi), rng.uniform(5, 45)))
             cam.look_at((side / 2,) * 3)
-            out.append(("frame", ti, cam.gpu_struct(), w, h))
+            out.append(("frame", ti, cam.gpu_struct(), w, h, cam.state()))
         else:
             k = int(rng.integers(1000, 20000))
             c, r = wl.balls(k, 0.0, float(side), 0.5, 8.0, seed * 1000 + i)
@@ -50,7 +73,7 @@ def _requests(wl, n, seed):
 
 def _alone(trees, tex, req):
     if req[0] == "frame":
-        _, ti, cam, w, h = req
+        _, ti, cam, w, h = req[:5]
         return trees[ti].render(cam, w, h, tex).ravel().view(np.uint8)
     _, ti, c, r = req
     return trees[ti].balls(c, r)
@@ -93,6 +116,7 @@ def test_mixed_requests_equal_requests_alone(setup):
     results, stats = _run_mixed(vg, trees, tex, reqs, cfg)
     for q, got in zip(reqs, results):
         assert np.array_equal(got, _alone(trees, tex, q)), q[0]
+        assert np.array_equal(got, _oracle(tex, q)), q[0]
     assert stats["completed"] == stats["submitted"] == len(reqs)
     assert stats["launches"] >= 1
 
@@ -115,6 +139,7 @@ def test_tight_budget_queues_but_stays_exact(setup):
     results, stats = _run_mixed(vg, trees, tex, reqs, cfg, nthreads=3)
     for q, got in zip(reqs, results):
         assert np.array_equal(got, _alone(trees, tex, q)), q[0]
+        assert np.array_equal(got, _oracle(tex, q)), q[0]
     assert 0 < stats["host_peak_bytes"] <= host_budget
 
 

@@ -30,8 +30,10 @@ def test_make_tree_render64_volume():
     assert ok, key
 
 
-@pytest.mark.parametrize("n,seed,solid", [(64, 10, 0.05), (128, 11, 0.10)])
+@pytest.mark.parametrize("n,seed,solid", [(256, 2, 0.08)] + list(wl.BATCH_TREES))
 def test_make_tree_matches_oracle_on_noise_volumes(n, seed, solid):
+    """The benchmark's trees: the 256^3 orbit volume and the four trees of the
+    mixed-camera batch (64^3 .. 512^3, 13.9 M voxels), node for node."""
     set_voxel_size((1, 1, 1))
     orc.set_voxel((1, 1, 1))
     vox = wl.voxels_from_mask(wl.noise_volume(n, seed, solid))

@@ -1,9 +1,12 @@
 """The light manager and its M-tree (host side, no GPU): the oracle's
 restatement satisfies the reference's own M-tree tests (tests/tests.c:
 779-900: invariants after every insertion and removal, duplicates refused,
-search counts equal to brute force), and the library's independent
-restatement answers every call of a random sequence exactly as the oracle
-does."""
+search counts equal to brute force), the library's independent restatement
+answers every call of a random sequence exactly as the oracle does, and both
+are pinned to the reference's own compiled lights.c and mtree.c: the
+library's M-tree node for node, the oracle's light sums bit for bit."""
+import os
+
 import numpy as np
 import pytest
 
@@ -89,3 +92,75 @@ def test_library_answers_like_the_oracle():
         assert L.verify() == 0
     M.clear()
     assert M.count() == 0
+
+
+# ---- pinned to the reference's own light manager and M-tree ---------------
+#
+# tests/golden/lights.npz: three call sequences run through the reference's
+# lights.c and mtree.c compiled here (make -C oracle ref-lights), with the
+# whole M-tree, the light count and vox_get_light at sample points recorded
+# every 20 calls (make_golden.py lights).
+
+LG = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lights.npz"))
+SEQUENCES = [str(s) for s in LG["sequences"]]
+
+
+def _replay(kind, manager, at_snapshot):
+    ops, args = LG[f"{kind}_op"], LG[f"{kind}_args"]
+    snaps = list(LG[f"{kind}_snap_at"])
+    k = 0
+    for i, (op, a) in enumerate(zip(ops, args)):
+        if op == 0:
+            rc = manager.insert(a[:3], a[3], a[4:7])
+        elif op == 1:
+            rc = manager.delete(a[:3], a[3])
+        else:
+            rc = manager.ambient(a[4:7])
+        assert int(rc) == int(a[7]), (kind, i, int(op))
+        if k < len(snaps) and i + 1 == snaps[k]:
+            at_snapshot(k)
+            k += 1
+    assert k == len(snaps)
+
+
+def _split(kind, name, k):
+    cut = np.concatenate([[0], np.cumsum(LG[f"{kind}_{name}_split"])])
+    return LG[f"{kind}_{name}s" if name != "point" else f"{kind}_points"][cut[k]:cut[k + 1]]
+
+
+@pytest.mark.parametrize("kind", SEQUENCES)
+def test_library_mtree_is_the_references(kind):
+    """The library's light manager returns what the reference's does for
+    every call, and its M-tree is the reference's node for node -- shape,
+    order, bounding spheres and stored spheres to the bit -- after every 20
+    calls (insertions with splits, removals with merges, refusals)."""
+    import ctypes as C
+    from tests.helpers import mtree_walk
+    M = vg.LightManager()
+
+    def check(k):
+        nodes, spheres = mtree_walk(C.c_void_p.from_address(M.ptr + 16).value)
+        assert np.array_equal(nodes, _split(kind, "node", k)), (kind, k)
+        assert np.array_equal(spheres, _split(kind, "sphere", k)), (kind, k)
+        assert M.count() == LG[f"{kind}_snap_count"][k]
+
+    _replay(kind, M, check)
+    M.close()
+
+
+@pytest.mark.parametrize("kind", SEQUENCES)
+def test_oracle_light_sums_are_the_references(kind):
+    """The oracle's light at every sample point -- ambient plus each
+    containing sphere's share, summed in M-tree order -- has the bits of the
+    reference's vox_get_light (lights.c:104-116) after every 20 calls."""
+    L = orc.OracleLights()
+    cut = np.concatenate([[0], np.cumsum(LG[f"{kind}_point_split"])])
+
+    def check(k):
+        pts = LG[f"{kind}_points"][cut[k]:cut[k + 1]]
+        ref = LG[f"{kind}_light"][cut[k]:cut[k + 1]]
+        got = np.array([L.light(p)[0] for p in pts], np.float32)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (kind, k)
+        assert L.count() == LG[f"{kind}_snap_count"][k]
+
+    _replay(kind, L, check)

@@ -121,3 +121,39 @@ def test_oracle_ray_buffer_camera_draws_its_directions():
         a, _ = orc.render_quality(t.ptr, st, w, h, q, tex, nthreads=2)
         b, _ = orc.render_quality(t.ptr, buf, w, h, q, tex, nthreads=2)
         assert np.array_equal(a, b), q
+
+
+def test_oracle_camera_setup_matches_reference_cameras():
+    """The oracle's simple-camera set-up (window size, position, look_at)
+    leaves the reference camera's fields bit for bit (cameras.npz: the
+    reference's simple-camera.c compiled here, driven through its vtable)."""
+    g = load("cameras")
+    checked = 0
+    for i in range(int(g["ncams"])):
+        if int(g[f"c{i}_kind"]) != 0 or np.isnan(g[f"c{i}_lookat"]).any():
+            continue
+        w, h = (int(x) for x in g[f"c{i}_wh"])
+        st = orc.camera_simple(g[f"c{i}_setpos"], g[f"c{i}_lookat"], w, h, float(g[f"c{i}_fov"]))
+        for k in ("position", "rotation", "mul", "xsub", "ysub"):
+            a = np.asarray(st[k], np.float32).view(np.uint32)
+            b = np.asarray(g[f"c{i}_{k}"], np.float32).view(np.uint32)
+            assert np.array_equal(a, b), (i, k)
+        checked += 1
+    assert checked == 5
+
+
+def test_oracle_orbit_cameras_match_library_cameras():
+    """The 120 orbit cameras of the 1080p benchmark set up by the oracle equal
+    the library's simple-camera set up the same way (both follow
+    simple-camera.c; the benchmark's reference arm uses the oracle's)."""
+    import math
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import orbit_camera
+    centre, radius = (128.0, 128.0, 128.0), 1.5 * 256 * math.sqrt(3.0)
+    for f in range(120):
+        lib_st = orbit_camera(f, 120, 1920, 1080, centre, radius).state()
+        orc_st = orc.camera_simple(wl.orbit_pose(f, 120, centre, radius, 20.0), centre, 1920, 1080, 1.0)
+        for k in ("position", "rotation", "mul", "xsub", "ysub"):
+            a = np.asarray(orc_st[k], np.float32).view(np.uint32)
+            b = np.asarray(lib_st[k], np.float32).view(np.uint32)
+            assert np.array_equal(a, b), (f, k)

@@ -7,10 +7,12 @@ shared by every call.
 Each frame must equal the one vox_cuda_render_device draws for the same tree,
 camera and size (ARGB pixels, compared exactly), on two calls in a row --
 the second with a different job list, so a stale job table or an unreset
-queue head from the first call would show.  This file is collected last so a
-failure here cannot hide the results of the other tests.
+queue head from the first call would show -- also when the two calls are
+issued back to back on one stream with no wait between them, behind a kernel
+that is still running.  This file is collected last so a failure here cannot
+hide the results of the other tests.
 """
-import ctypes as C
+import time
 
 import numpy as np
 import pytest
@@ -92,3 +94,28 @@ def test_noalloc_rejects_requests_beyond_its_capacity(scene):
     assert vg.lib().vox_cuda_strerror(-11).startswith(b"request exceeds")
     assert _call(vg, jobs[:cap], tex) == 0
     _check_against_plain(jobs[:cap], tex)
+
+
+def test_noalloc_calls_back_to_back_on_a_busy_stream(scene):
+    """Two calls with different job lists on one non-default stream, queued
+    behind a kernel that is still running and with no synchronisation between
+    them: both return before that kernel ends (the job table travels as a
+    kernel argument; nothing waits for the stream), and after one
+    synchronisation every frame of both lists equals the plain frame."""
+    vg, hosts, trees, tex, make_jobs = scene
+    s = torch.cuda.Stream()
+    a, b = make_jobs(7, 4), make_jobs(6, 5)
+    assert _call(vg, a[:1], tex, s.cuda_stream) == 0      # set-up done before timing
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        torch.cuda._sleep(400_000_000)                    # a busy kernel, ~0.2 s at 2 GHz
+    t0 = time.perf_counter()
+    assert _call(vg, a, tex, s.cuda_stream) == 0
+    assert _call(vg, b, tex, s.cuda_stream) == 0
+    returned_s = time.perf_counter() - t0
+    still_busy = not s.query()
+    s.synchronize()
+    _check_against_plain(a, tex)
+    _check_against_plain(b, tex)
+    assert still_busy, "the stream finished before the calls returned: they waited for it"
+    assert returned_s < 0.05

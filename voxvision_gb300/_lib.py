@@ -141,6 +141,10 @@ SIGNATURES = {
     "vox_cuda_tree_flatten_host": (C.c_int, [_vp, _vp, C.c_size_t, _vp, C.c_size_t, C.POINTER(C.c_size_t),
                                              C.POINTER(C.c_size_t)]),
     "vox_cuda_image_check": (C.c_int, [_vp, C.c_size_t, C.c_size_t]),
+    "vox_cuda_tree_upload_layout": (C.c_int, [_vp, C.c_int, _vp, C.POINTER(_vp)]),
+    "vox_cuda_tree_refresh_layout": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "vox_cuda_tree_flatten_host_layout": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_size_t, _vp, C.c_size_t,
+                                                    C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "vox_cuda_render_rays_device": (C.c_int, [_vp, _vp, _vp, _u32, _u32, C.c_uint, _vp, _vp, _vp, _vp]),
     "vox_cuda_batch_create": (C.c_int, [C.POINTER(FrameJob), _u32, C.POINTER(BatchConfig), C.POINTER(_vp)]),
     "vox_cuda_batch_set_camera": (C.c_int, [_vp, _u32, C.POINTER(CameraStruct)]),

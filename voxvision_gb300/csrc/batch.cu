@@ -530,10 +530,19 @@ try {
  * whose work overlaps on the GPU (different streams, or different host
  * threads without ordering) race on the array and give wrong frames.
  *
+ * Staging.  The job table travels as a kernel argument (by value, at most
+ * sizeof(NoallocStage) bytes, inside the 32,764-byte argument limit) to a
+ * one-block kernel that writes it into the array and zeroes the queue head;
+ * the frame kernel follows on the same stream.  No host memory is read by the
+ * GPU and nothing is copied by the host, so the call returns without waiting
+ * for earlier work on the stream.
+ *
  * Set-up.  Host code cannot use the array's name as a device address.  The
  * first call on each device looks its address up with cudaGetSymbolAddress
- * (with that device current) and caches it; make that first call before any
- * stream capture is started on the device.
+ * (with that device current) and caches it for the life of the process;
+ * make that first call before any stream capture is started on the device.
+ * The cached address does not survive cudaDeviceReset: a process that resets
+ * a device must not call this entry point on it afterwards.
  * ------------------------------------------------------------------------- */
 
 namespace {
@@ -546,6 +555,25 @@ static_assert(NOALLOC_BYTES <= 16384, "no-allocation scratch must stay within 16
 // [0, 4): work-queue head; [256, ...): job table (its head, then one entry
 // per frame).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// One call's job table, passed by value to noalloc_stage_kernel.
+struct NoallocStage {
+    BatchHead head;
+    BatchJobDev jobs[VOX_CUDA_NOALLOC_MAX_JOBS];
+};
+static_assert(sizeof(NoallocStage) + 2 * sizeof(void *) + sizeof(uint32_t) <= 32764,
+              "the job table must fit the kernel argument limit");
+static_assert(sizeof(NoallocStage) % 4 == 0 && alignof(NoallocStage) >= 4, "staged in 4-byte words");
+
+// Writes the first `words` 4-byte words of the staged table into the array
+// and zeroes the queue head.
+__global__ void __launch_bounds__(256) noalloc_stage_kernel(const __grid_constant__ NoallocStage st, uint32_t words,
+                                                           uint32_t *__restrict__ table, uint32_t *__restrict__ head)
+{
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&st);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) table[i] = src[i];
+    if (threadIdx.x == 0) *head = 0u;
+}
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 void *g_noalloc_addr[NOALLOC_MAX_DEVICES];
@@ -604,19 +632,19 @@ try {
         }
         order[k] = i;
     }
-    // head and table staged on the host stack, copied into the array
-    struct {
-        BatchHead head;
-        BatchJobDev jobs[VOX_CUDA_NOALLOC_MAX_JOBS];
-    } stage;
+    // head and table built on the host stack; they reach the GPU as the
+    // staging kernel's argument
+    NoallocStage stage;
+    std::memset(&stage, 0, sizeof stage);
     stage.head = BatchHead{njobs, 0u, 0u, 0u};
     for (uint32_t q = 0; q < njobs; q++) fill_job(stage.jobs[q], jobs[order[q]], 8, 4, stage.head);
     cudaStream_t s = as_stream(stream);
     uint32_t *head = reinterpret_cast<uint32_t *>(scratch);
     BatchHead *dtable = reinterpret_cast<BatchHead *>(scratch + NOALLOC_HEAD_BYTES);
-    if (cudaMemcpyAsync(dtable, &stage, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemsetAsync(head, 0, sizeof(uint32_t), s) != cudaSuccess)
-        return VOX_CUDA_ECUDA;
+    noalloc_stage_kernel<<<1, 256, 0, s>>>(stage, (uint32_t)(table_bytes(njobs) / 4),
+                                           reinterpret_cast<uint32_t *>(dtable), head);
+    count_launch();
+    if (cudaGetLastError() != cudaSuccess) return VOX_CUDA_ECUDA;
     switch (cap) {
     case 0: launch_noalloc<CAP0>(dtable, head, nsm, s); break;
     case 1: launch_noalloc<CAP1>(dtable, head, nsm, s); break;

@@ -1,6 +1,8 @@
 /*
  * flatten.cpp -- turn a host struct vox_node tree into the device pool image
- * described in pool_layout.h.
+ * described in pool_layout.h.  Trees of either vox_dot layout are read: the
+ * scalar one (float[3]) and the SSE one (float[4] aligned to 16, vox_node16);
+ * the image is the same for the same nodes.
  *
  * Layout.  Records are placed depth first: when a node is visited (in
  * pre-order: node, then children 0..7), its child block -- or its voxel run,
@@ -39,18 +41,20 @@ inline uint32_t fbits(float f)
     return u;
 }
 
-inline bool is_inner(const vox_node *n) { return !(n->flags & VOX_LEAF_MASK); }
-
 struct Sizes {
     uint64_t nodes = 0, units = 0, inner = 0, leaf = 0, dense = 0, dots = 0, depth = 0;
 };
 
+// Every walk below is a template over the node layout N (vox_node: scalar
+// vox_dot; vox_node16: the SSE layout); both have the same member names.
+
 // Nodes of the subtree, units it appends (child blocks and voxel runs), kinds,
 // and its depth in inner nodes.
-Sizes count(const vox_node *root)
+template <class N>
+Sizes count(const N *root)
 {
     Sizes s;
-    std::vector<std::pair<const vox_node *, uint32_t>> work{{root, 0}};
+    std::vector<std::pair<const N *, uint32_t>> work{{root, 0}};
     while (!work.empty()) {
         auto [n, d] = work.back();
         work.pop_back();
@@ -65,7 +69,7 @@ Sizes count(const vox_node *root)
             s.inner++;
             s.depth = std::max<uint64_t>(s.depth, d + 1);
             for (int o = 0; o < 8; o++)
-                if (const vox_node *ch = n->data.inner.children[o]) {
+                if (const N *ch = n->data.inner.children[o]) {
                     s.units += VOXP_REC_UNITS;
                     work.push_back({ch, d + 1});
                 }
@@ -76,8 +80,9 @@ Sizes count(const vox_node *root)
 
 // A subtree placed on its own: its root's record offset (in its parent's
 // child block), its first pre-order id and the start of its image region.
+template <class N>
 struct Task {
-    const vox_node *node;
+    const N *node;
     uint32_t rec, id, next;
 };
 
@@ -85,8 +90,9 @@ struct Task {
 // leaf, appends its child block or voxel run at *next.  Pushes the children
 // (in reverse octant order, so they are visited in pre-order) onto `work`.
 // Returns false if a leaf is too large for the record format.
-bool place(const vox_node *n, uint32_t rec, uint32_t id, uint32_t *next, uint4_host *u,
-           std::vector<std::pair<const vox_node *, uint32_t>> *work)
+template <class N>
+bool place(const N *n, uint32_t rec, uint32_t id, uint32_t *next, uint4_host *u,
+           std::vector<std::pair<const N *, uint32_t>> *work)
 {
     uint32_t meta, link;
     uint4_host extra{0u, 0u, 0u, 0u};
@@ -108,7 +114,7 @@ bool place(const vox_node *n, uint32_t rec, uint32_t id, uint32_t *next, uint4_h
         link = *next;
         *next += VOXP_REC_UNITS * (uint32_t)__builtin_popcount(mask);
         for (int o = 7; o >= 0; o--) {
-            const vox_node *ch = n->data.inner.children[o];
+            const N *ch = n->data.inner.children[o];
             if (!ch) continue;
             uint32_t rank = (uint32_t)__builtin_popcount(mask & ((1u << o) - 1u));
             work->push_back({ch, link + VOXP_REC_UNITS * rank});
@@ -117,7 +123,7 @@ bool place(const vox_node *n, uint32_t rec, uint32_t id, uint32_t *next, uint4_h
         const float *c = n->data.inner.center;
         extra = {fbits(c[0]), fbits(c[1]), fbits(c[2]), 0u};
     }
-    const vox_box &b = n->bounding_box;
+    const auto &b = n->bounding_box;
     u[rec] = {fbits(b.min[0]), fbits(b.min[1]), fbits(b.min[2]), fbits(b.max[0])};
     u[rec + 1] = {fbits(b.max[1]), fbits(b.max[2]), meta, link};
     u[rec + 2] = extra;
@@ -125,15 +131,16 @@ bool place(const vox_node *n, uint32_t rec, uint32_t id, uint32_t *next, uint4_h
 }
 
 // Places a whole subtree depth first from its task.
-bool place_subtree(const Task &t, FlatTree *out)
+template <class N>
+bool place_subtree(const Task<N> &t, FlatTree *out)
 {
-    std::vector<std::pair<const vox_node *, uint32_t>> work{{t.node, t.rec}};
+    std::vector<std::pair<const N *, uint32_t>> work{{t.node, t.rec}};
     uint32_t id = t.id, next = t.next;
     uint4_host *u = out->units.data();
     while (!work.empty()) {
         auto [n, rec] = work.back();
         work.pop_back();
-        out->preorder[id] = n;
+        out->preorder[id] = reinterpret_cast<const vox_node *>(n);
         out->rec_of_id[id] = rec;
         if (!place(n, rec, id, &next, u, &work)) return false;
         id++;
@@ -143,9 +150,8 @@ bool place_subtree(const Task &t, FlatTree *out)
 
 constexpr uint32_t CUT_DEPTH = 3;   // levels walked by one thread (up to 512 subtrees below)
 
-}  // namespace
-
-int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
+template <class N>
+int flatten_tree(const N *root, const float voxel[3], FlatTree *out)
 {
     out->units.clear();
     out->preorder.clear();
@@ -158,10 +164,10 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
 
     // 1. The subtrees at the cut depth, in pre-order, counted in parallel;
     //    the nodes above the cut counted here.
-    std::vector<const vox_node *> cut;
+    std::vector<const N *> cut;
     Sizes top;
     {
-        std::vector<std::pair<const vox_node *, uint32_t>> work{{root, 0}};
+        std::vector<std::pair<const N *, uint32_t>> work{{root, 0}};
         while (!work.empty()) {
             auto [n, d] = work.back();
             work.pop_back();
@@ -177,7 +183,7 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
                 top.inner++;
                 top.depth = std::max<uint64_t>(top.depth, d + 1);
                 for (int o = 7; o >= 0; o--)
-                    if (const vox_node *ch = n->data.inner.children[o]) {
+                    if (const N *ch = n->data.inner.children[o]) {
                         top.units += VOXP_REC_UNITS;
                         work.push_back({ch, d + 1});
                     }
@@ -202,10 +208,10 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
 
     // 2. The levels above the cut, depth first, reserving each cut subtree's
     //    id range and image region where the single walk would place it.
-    std::vector<Task> tasks;
+    std::vector<Task<N>> tasks;
     tasks.reserve(cut.size());
     {
-        std::vector<std::pair<const vox_node *, uint32_t>> work{{root, 0}}, kids;
+        std::vector<std::pair<const N *, uint32_t>> work{{root, 0}}, kids;
         std::vector<uint32_t> depth{0};
         uint32_t id = 0, next = VOXP_REC_UNITS;
         size_t k = 0;
@@ -222,7 +228,7 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
                 next += (uint32_t)z.units;
                 continue;
             }
-            out->preorder[id] = n;
+            out->preorder[id] = reinterpret_cast<const vox_node *>(n);
             out->rec_of_id[id] = rec;
             kids.clear();
             if (!place(n, rec, id, &next, u, &kids)) return -1;
@@ -240,6 +246,18 @@ int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
         if (!place_subtree(tasks[i], out)) ok = false;
     });
     return ok ? 0 : -1;
+}
+
+}  // namespace
+
+int vox_flatten(const vox_node *root, const float voxel[3], FlatTree *out)
+{
+    return flatten_tree(root, voxel, out);
+}
+
+int vox_flatten16(const vox_node16 *root, const float voxel[3], FlatTree *out)
+{
+    return flatten_tree(root, voxel, out);
 }
 
 namespace {

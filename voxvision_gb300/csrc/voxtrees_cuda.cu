@@ -750,10 +750,20 @@ EXPORT uint64_t vox_cuda_launch_count(void) { return g_launches.load(); }
 // Flattens `root` into t (host maps) and copies the image to the device,
 // reusing t's device buffers when they are large enough.  On failure t keeps
 // its previous contents when `keep` is set (a refresh), else is left empty.
-static int load_tree(vox_cuda_tree *t, const struct vox_node *root)
+// The image of `root` read in the given vox_dot layout, with `voxel` (NULL:
+// the library's vox_voxel) as the voxel size.
+static int flatten_as(const struct vox_node *root, int layout, const float *voxel, FlatTree *f)
+{
+    const float *v = voxel ? voxel : vox_voxel;
+    if (layout == VOX_CUDA_LAYOUT_SSE) return vox_flatten16(reinterpret_cast<const vox_node16 *>(root), v, f);
+    return vox_flatten(root, v, f);
+}
+
+static int load_tree(vox_cuda_tree *t, const struct vox_node *root, int layout = VOX_CUDA_LAYOUT_SCALAR,
+                     const float *voxel = nullptr)
 {
     FlatTree flat;
-    int rc = vox_flatten(root, vox_voxel, &flat);
+    int rc = flatten_as(root, layout, voxel, &flat);
     if (rc == -2 || rc == -1) return VOX_CUDA_ETOOBIG;
     if (vox_flatten_validate(flat) != 0) return VOX_CUDA_EINVAL;
     int cls = cap_class_for_depth(flat.depth);
@@ -798,11 +808,10 @@ static int load_tree(vox_cuda_tree *t, const struct vox_node *root)
         t->map_bytes = map_bytes;
     }
     t->cap_class = cls;
-    if (root) {
-        for (int i = 0; i < 3; i++) {
-            t->bbox[i] = root->bounding_box.min[i];
-            t->bbox[3 + i] = root->bounding_box.max[i];
-        }
+    if (root) {   // the root record: {min.xyz, max.x}, {max.yz, ...}
+        const uint4_host &a = flat.units[0], &b = flat.units[1];
+        const uint32_t bits[6] = {a.x, a.y, a.z, a.w, b.x, b.y};
+        for (int i = 0; i < 6; i++) std::memcpy(&t->bbox[i], &bits[i], 4);
     } else {
         for (int i = 0; i < 6; i++) t->bbox[i] = 0.0f;
     }
@@ -909,7 +918,7 @@ try {
     return tree_upload_flat(root, out);
 } VOX_ABI_FAIL_INT
 
-int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
+static int upload_as(const struct vox_node *root, int layout, const float *voxel, vox_cuda_tree **out)
 {
     if (!out) return VOX_CUDA_EINVAL;
     *out = nullptr;
@@ -918,7 +927,7 @@ int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
     vox_cuda_tree *t = new (std::nothrow) vox_cuda_tree();
     if (!t) return VOX_CUDA_ENOMEM;
     t->device = dev;
-    int rc = load_tree(t, root);
+    int rc = load_tree(t, root, layout, voxel);
     if (rc) {
         cudaFree(t->d_pool);
         cudaFree(t->d_rec_of_id);
@@ -930,12 +939,34 @@ int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
     return VOX_CUDA_OK;
 }
 
+int tree_upload_flat(const struct vox_node *root, vox_cuda_tree **out)
+{
+    return upload_as(root, VOX_CUDA_LAYOUT_SCALAR, nullptr, out);
+}
+
+static bool known_layout(int layout) { return layout == VOX_CUDA_LAYOUT_SCALAR || layout == VOX_CUDA_LAYOUT_SSE; }
+
+EXPORT int vox_cuda_tree_upload_layout(const struct vox_node *root, int layout, const float *voxel,
+                                       vox_cuda_tree **out)
+try {
+    if (!out || !known_layout(layout)) return VOX_CUDA_EINVAL;
+    return upload_as(root, layout, voxel, out);
+} VOX_ABI_FAIL_INT
+
 EXPORT int vox_cuda_tree_refresh(vox_cuda_tree *t, const struct vox_node *root)
 try {
     if (!t) return VOX_CUDA_EINVAL;
     // kernels in flight on any stream may still read the old image
     if (cudaDeviceSynchronize() != cudaSuccess) return VOX_CUDA_ECUDA;
     return load_tree(t, root);
+} VOX_ABI_FAIL_INT
+
+EXPORT int vox_cuda_tree_refresh_layout(vox_cuda_tree *t, const struct vox_node *root, int layout,
+                                        const float *voxel)
+try {
+    if (!t || !known_layout(layout)) return VOX_CUDA_EINVAL;
+    if (cudaDeviceSynchronize() != cudaSuccess) return VOX_CUDA_ECUDA;
+    return load_tree(t, root, layout, voxel);
 } VOX_ABI_FAIL_INT
 
 EXPORT int vox_cuda_tree_measure(const struct vox_node *root, vox_cuda_tree_info *info)
@@ -1003,8 +1034,17 @@ try {
 EXPORT int vox_cuda_tree_flatten_host(const struct vox_node *root, void *units, size_t units_cap,
                                       uint32_t *rec_of_id, size_t ids_cap, size_t *n_units, size_t *n_ids)
 try {
+    return vox_cuda_tree_flatten_host_layout(root, VOX_CUDA_LAYOUT_SCALAR, nullptr, units, units_cap, rec_of_id,
+                                             ids_cap, n_units, n_ids);
+} VOX_ABI_FAIL_INT
+
+EXPORT int vox_cuda_tree_flatten_host_layout(const struct vox_node *root, int layout, const float *voxel,
+                                             void *units, size_t units_cap, uint32_t *rec_of_id, size_t ids_cap,
+                                             size_t *n_units, size_t *n_ids)
+try {
+    if (!known_layout(layout)) return VOX_CUDA_EINVAL;
     FlatTree flat;
-    int rc = vox_flatten(root, vox_voxel, &flat);
+    int rc = flatten_as(root, layout, voxel, &flat);
     if (rc) return VOX_CUDA_ETOOBIG;
     const size_t nu = flat.units.size(), ni = flat.preorder.size();
     if (n_units) *n_units = nu;
