@@ -273,23 +273,42 @@ def traffic_per_launch(nframes):
         return None
 
 
-def l2_copy_gbs(torch):
-    """L2 bandwidth: 20 back-to-back 24 MiB -> 24 MiB device copies (both
-    buffers stay in the 129 MB L2), read + write bytes over the CUDA-event
-    time, best of 10."""
-    a = torch.ones(6 << 20, dtype=torch.float32, device="cuda")
-    b = torch.empty_like(a)
-    for _ in range(5):
-        b.copy_(a)
+def l2_read_gbs(L, mib=32, reps=1000):
+    """L2 read bandwidth: one kernel reading a 32 MiB buffer (inside the
+    129 MB L2) 1000 times over with L1-bypassing loads, CUDA-event timed
+    (vox_cuda_measure_l2_read); best of 3."""
+    import ctypes as C
     best = 0.0
-    for _ in range(10):
-        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(20):
-            b.copy_(a)
-        e1.record(); e1.synchronize()
-        best = max(best, 20 * 2 * a.numel() * 4 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    for _ in range(3):
+        g = C.c_float()
+        if L.vox_cuda_measure_l2_read(mib << 20, reps, C.byref(g)) == 0:
+            best = max(best, float(g.value))
     return best
+
+
+def issue_figures(nframes, traced_rays, launch_s, nsm, sm_mhz):
+    """The issue roofline of the kernel: its warp instructions per launch
+    (from the committed ncu summary of the 24-frame orbit, scaled to this
+    launch by frames) over the launch time measured here, against the issue
+    peak of the device (4 schedulers a SM, one warp instruction a cycle each,
+    at the SM clock sampled during the timed region); and the instructions
+    per traced ray."""
+    try:
+        with open(TRAFFIC_SUMMARY) as f:
+            p = json.load(f)
+        inst = float(p["warp_inst_per_launch"]) * nframes / float(p["frames_per_launch"])
+        achieved = inst / launch_s / 1e9
+        peak = nsm * 4 * sm_mhz * 1e6 / 1e9 if sm_mhz else None
+        return {"achieved_ginst_s": achieved, "peak_ginst_s": peak, "frac": achieved / peak if peak else None,
+                "unit": "G warp instructions/s",
+                "warp_inst_per_traced_ray": inst / traced_rays,
+                "thread_inst_per_traced_ray": inst * float(p["lanes_active_per_inst"]) / traced_rays,
+                "lanes_active_per_inst": float(p["lanes_active_per_inst"]),
+                "issue_slots_busy": float(p["issue_slots_busy"]),
+                "l2_throughput_pct_of_peak": float(p["l2_throughput_pct"]),
+                "source": "ncu --set full of batch_kernel on the 24-frame orbit, " + p.get("captured", "")}
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
+        return None
 
 
 def cpu_baseline_sample(tree_ptr, states, tex, budget_s=3.0):
@@ -866,7 +885,7 @@ def run_ours(args):
     mean_launch_s = float(np.mean(step_ms)) * 1e-3
     achieved = traced_bytes_step / mean_launch_s / 1e9
     traffic = traffic_per_launch(nf)
-    l2 = l2_copy_gbs(torch)
+    l2 = l2_read_gbs(L)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback 6.8 TB/s",
@@ -886,8 +905,14 @@ def run_ours(args):
                 "bytes_per_ray": traced_bytes_step / rays_step,
                 "visits_per_ray": {"nodes": nodes / rays_step, "inner": inner / rays_step,
                                    "voxels": voxels / rays_step},
-                "l2_gbs_measured": l2, "l2_frac": achieved / l2,
-                "l2_probe": "24 MiB device-to-device copy inside L2, read+write bytes"}
+                "traced_rays_per_launch": rays_step - culled,
+                "traced_mrays_s": (rays_step - culled) / mean_launch_s / 1e6,
+                "l2_gbs_measured": l2, "l2_frac": achieved / l2 if l2 else None,
+                "l2_probe": "vox_cuda_measure_l2_read: one kernel reading a 32 MiB buffer 1000 times, "
+                            "L1 bypassed (ld.global.cg)",
+                "issue": issue_figures(nf, rays_step - culled, mean_launch_s,
+                                       torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count,
+                                       clk["sm_mhz"] if clk else None)}
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sum(step_ms) / len(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

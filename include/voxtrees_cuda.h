@@ -527,6 +527,14 @@ int vox_cuda_server_replay(vox_cuda_server *srv, const vox_cuda_replay_request *
 const char *vox_cuda_version(void);
 uint64_t vox_cuda_launch_count(void);
 
+/* Measurement aid, no counterpart in the reference: the L2 read bandwidth of
+ * the current device in GB/s, from one kernel that reads a `bytes` buffer
+ * (small enough to stay in L2, e.g. 32 MiB) `reps` times over with loads that
+ * bypass L1, timed with CUDA events after a warm pass.  The roofline of the
+ * search kernels, whose tree mostly stays in L2, is set against it.
+ * Allocates and frees the buffer itself. */
+int vox_cuda_measure_l2_read(size_t bytes, uint32_t reps, float *gbs);
+
 /* 1 in the checked build (libvoxtrees_cuda_checked.so, compiled with
  * -DVOX_CUDA_CHECKED): every search load first checks its index against the
  * uploaded tree and light arrays, and a search that meets an index outside

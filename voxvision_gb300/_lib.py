@@ -141,6 +141,7 @@ SIGNATURES = {
     "vox_cuda_tree_flatten_host": (C.c_int, [_vp, _vp, C.c_size_t, _vp, C.c_size_t, C.POINTER(C.c_size_t),
                                              C.POINTER(C.c_size_t)]),
     "vox_cuda_image_check": (C.c_int, [_vp, C.c_size_t, C.c_size_t]),
+    "vox_cuda_measure_l2_read": (C.c_int, [C.c_size_t, _u32, C.POINTER(C.c_float)]),
     "vox_cuda_tree_upload_layout": (C.c_int, [_vp, C.c_int, _vp, C.POINTER(_vp)]),
     "vox_cuda_tree_refresh_layout": (C.c_int, [_vp, _vp, C.c_int, _vp]),
     "vox_cuda_tree_flatten_host_layout": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_size_t, _vp, C.c_size_t,

@@ -743,6 +743,69 @@ try {
 
 EXPORT const char *vox_cuda_version(void) { return "voxtrees_cuda 0.1 (sm_103a)"; }
 
+namespace {
+
+// Reads `n16` 16-byte units `reps` times over, bypassing L1 (ld.global.cg),
+// so that every load is served by L2 while the buffer fits it.  The xor of
+// everything read is stored only if it takes one particular value, which
+// keeps the loads without writing anything in practice.
+__global__ void __launch_bounds__(256) l2_read_kernel(const uint4 *__restrict__ buf, size_t n16, uint32_t reps,
+                                                      uint32_t *__restrict__ sink)
+{
+    uint32_t acc = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t first = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t r = 0; r < reps; r++) {
+        for (size_t i = first; i < n16; i += stride) {
+            uint4 v = __ldcg(buf + i);
+            acc ^= v.x ^ v.y ^ v.z ^ v.w;
+        }
+    }
+    if (acc == 0x9E3779B9u) sink[0] = acc;
+}
+
+}  // namespace
+
+EXPORT int vox_cuda_measure_l2_read(size_t bytes, uint32_t reps, float *gbs)
+try {
+    if (!gbs || bytes < 4096 || reps == 0) return VOX_CUDA_EINVAL;
+    *gbs = 0.0f;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return VOX_CUDA_ENODEV;
+    const size_t n16 = bytes / 16;
+    uint4 *buf = nullptr;
+    uint32_t *sink = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = VOX_CUDA_ECUDA;
+    if (cudaMalloc(&buf, n16 * 16) != cudaSuccess || cudaMalloc(&sink, 4) != cudaSuccess) {
+        rc = VOX_CUDA_ENOMEM;
+    } else if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+               cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
+               cudaMemsetAsync(buf, 0x5A, n16 * 16, s) == cudaSuccess) {
+        const dim3 grid(nsm * 8), block(256);
+        l2_read_kernel<<<grid, block, 0, s>>>(buf, n16, 2, sink);   // warm: the buffer into L2
+        count_launch();
+        cudaEventRecord(e0, s);
+        l2_read_kernel<<<grid, block, 0, s>>>(buf, n16, reps, sink);
+        count_launch();
+        cudaEventRecord(e1, s);
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0) {
+            *gbs = (float)((double)n16 * 16.0 * reps / (ms * 1e-3) / 1e9);
+            rc = VOX_CUDA_OK;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    cudaFree(buf);
+    cudaFree(sink);
+    return rc;
+} VOX_ABI_FAIL_INT
+
 EXPORT int vox_cuda_build_checked(void) { return vox::CHECKED ? 1 : 0; }
 
 EXPORT uint64_t vox_cuda_launch_count(void) { return g_launches.load(); }
