@@ -377,11 +377,14 @@ typedef struct {
 /* tile_w x tile_h pixels per warp tile: 8x4, 16x2, 32x1 (one ray per thread)
  * or 8x8, 16x4 (two rays per thread); tiles_per_grab: tiles a warp takes
  * from the queue at once (1..64); blocks_per_sm: resident 128-thread blocks
- * per SM (1..16). */
+ * per SM (1..16); stack_class: the traversal stack per ray, 0 = the smallest
+ * that holds the deepest tree of the batch (28 entries up to depth 9, 64 up
+ * to 21, 256 up to 85), 1 or 2 = at least 64 or 256 entries. */
 typedef struct {
     uint32_t tile_w, tile_h;
     uint32_t tiles_per_grab;
     uint32_t blocks_per_sm;
+    uint32_t stack_class;
 } vox_cuda_batch_config;
 
 typedef struct vox_cuda_batch vox_cuda_batch;
@@ -399,7 +402,9 @@ int vox_cuda_batch_launch(vox_cuda_batch *batch, void *stream);
 int vox_cuda_batch_get_config(const vox_cuda_batch *batch, vox_cuda_batch_config *config);
 int vox_cuda_batch_set_config(vox_cuda_batch *batch, const vox_cuda_batch_config *config);
 /* Time every candidate configuration (reps timed replays each, 0 = 3) on this
- * batch, keep the fastest and report it (chosen, best_ms may be NULL). */
+ * batch -- tile shapes, tiles per grab, blocks per SM, and the smallest stack
+ * class against the next larger one -- keep the fastest and report it
+ * (chosen, best_ms may be NULL). */
 int vox_cuda_batch_autotune(vox_cuda_batch *batch, void *stream, uint32_t reps,
                             vox_cuda_batch_config *chosen, float *best_ms);
 int vox_cuda_batch_free(vox_cuda_batch *batch);

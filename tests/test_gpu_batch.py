@@ -68,7 +68,8 @@ def test_batch_frames_equal_plain_frames(scene):
     b.close()
 
 
-@pytest.mark.parametrize("cfg", [(8, 4, 1, 4), (16, 2, 2, 8), (32, 1, 4, 4), (8, 8, 1, 8), (16, 4, 2, 4)])
+@pytest.mark.parametrize("cfg", [(8, 4, 1, 4), (16, 2, 2, 8), (32, 1, 4, 4), (8, 8, 1, 8), (16, 4, 2, 4),
+                                 (8, 4, 2, 8, 1), (8, 4, 2, 8, 2)])
 def test_every_config_gives_the_same_frames(scene, cfg):
     vg, hosts, devs, jobs, meta, tex = scene
     b = vg.FrameBatch(jobs, vg.BatchConfig(*cfg))
@@ -79,7 +80,8 @@ def test_every_config_gives_the_same_frames(scene, cfg):
     torch.cuda.synchronize()
     for j in jobs:
         assert np.array_equal(j[5].cpu().numpy(), _plain(vg, j))
-    assert b.config() == dict(zip(("tile_w", "tile_h", "tiles_per_grab", "blocks_per_sm"), cfg))
+    assert b.config() == dict(zip(("tile_w", "tile_h", "tiles_per_grab", "blocks_per_sm", "stack_class"),
+                                  cfg + (0,) * (5 - len(cfg))))
     b.close()
 
 

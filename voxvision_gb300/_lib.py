@@ -56,7 +56,7 @@ class FrameJob(C.Structure):
 class BatchConfig(C.Structure):
     """vox_cuda_batch_config (include/voxtrees_cuda.h)."""
     _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("tiles_per_grab", C.c_uint32),
-                ("blocks_per_sm", C.c_uint32)]
+                ("blocks_per_sm", C.c_uint32), ("stack_class", C.c_uint32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

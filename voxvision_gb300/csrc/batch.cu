@@ -267,7 +267,7 @@ bool valid_config(const vox_cuda_batch_config &c)
     bool shape = false;
     for (const Shape &s : kShapes) shape |= (s.tw == c.tile_w && s.th == c.tile_h);
     return shape && c.tiles_per_grab >= 1 && c.tiles_per_grab <= 64 && c.blocks_per_sm >= 1 &&
-           c.blocks_per_sm <= 16;
+           c.blocks_per_sm <= 16 && c.stack_class <= 2;
 }
 
 }  // namespace
@@ -283,7 +283,7 @@ struct vox_cuda_batch {
     unsigned char *h_stage = nullptr;         // pinned copy of head + table that the graph reads
     BatchHead *d_table = nullptr;             // device head + table
     uint32_t *d_counter = nullptr;            // work queue head (scratch)
-    vox_cuda_batch_config cfg{8, 4, 1, 4};
+    vox_cuda_batch_config cfg{8, 4, 1, 4, 0};
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -312,7 +312,7 @@ void stage_table(vox_cuda_batch *b)
 
 cudaError_t launch_kernel(vox_cuda_batch *b, cudaStream_t s)
 {
-    switch (b->cap_class) {
+    switch (std::max(b->cap_class, (int)b->cfg.stack_class)) {
     case 0: return launch_batch_cap<CAP0>(b->cfg, b->d_table, b->d_counter, b->nsm, s);
     case 1: return launch_batch_cap<CAP1>(b->cfg, b->d_table, b->d_counter, b->nsm, s);
     default: return launch_batch_cap<CAP2>(b->cfg, b->d_table, b->d_counter, b->nsm, s);
@@ -464,13 +464,17 @@ try {
     if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return VOX_CUDA_ECUDA; }
     const uint32_t grabs[] = {1, 2, 4};
     const uint32_t bpsm[] = {4, 8};
+    // the smallest stack class that holds the trees (0), and the next larger
+    const uint32_t stacks[] = {0u, (uint32_t)std::min(b->cap_class + 1, 2)};
+    const int nstacks = b->cap_class < 2 ? 2 : 1;
     vox_cuda_batch_config best = b->cfg;
     float best_t = 1e30f;
     int rc = VOX_CUDA_OK;
+    for (int si = 0; si < nstacks; si++)
     for (const Shape &sh : kShapes) {
         for (uint32_t g : grabs) {
             for (uint32_t k : bpsm) {
-                vox_cuda_batch_config c{sh.tw, sh.th, g, k};
+                vox_cuda_batch_config c{sh.tw, sh.th, g, k, stacks[si]};
                 if ((rc = vox_cuda_batch_set_config(b, &c)) != VOX_CUDA_OK) goto out;
                 if ((rc = vox_cuda_batch_launch(b, stream)) != VOX_CUDA_OK) goto out;   // warm-up
                 float tmin = 1e30f;
@@ -710,7 +714,7 @@ int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_t
     if (cudaMemcpyAsync(d_table, h_table, table_bytes(njobs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s) != cudaSuccess)
         return VOX_CUDA_ECUDA;
-    vox_cuda_batch_config c = cfg ? *cfg : vox_cuda_batch_config{8, 4, 1, 8};
+    vox_cuda_batch_config c = cfg ? *cfg : vox_cuda_batch_config{8, 4, 1, 8, 0};
     const BatchHead *dt = static_cast<const BatchHead *>(d_table);
     cudaError_t e;
     switch (cap) {
