@@ -557,21 +557,23 @@ def build_batch_trees(vg):
     return trees
 
 
-def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000), duration=1.0, seed=15):
+def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000), duration=1.0, seed=15,
+                   frames_on_device=False):
     """Served load: 256 clients with Poisson arrivals (merged: one Poisson
     stream at the aggregate rate); 70% frames (resolution uniform over
     320x240..3840x2160, tree uniform, random orbit pose), 30% batches of
     1k-64k ball queries; 4 resident trees under a 40 GB device budget.  The
     trace is replayed by the library's native replay (a submitting thread at
     the arrival times, 8 collector threads); latency = submission to result
-    in host memory, on the server's clock."""
+    in host memory (or, with frames_on_device, to the frame complete in the
+    server's device memory), on the server's clock."""
     import ctypes as C
     from voxvision_gb300 import workloads as wl
     from voxvision_gb300.cameras import HostCamera
     # 256 requests admitted at once (a few milliseconds of GPU work; more would
-    # only hold more pinned result memory), up to 64 per launch, 32 launches
-    # in flight on 16 streams
-    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 24 << 30, 256, 64, 16, 32))
+    # only hold more result memory), up to 32 per launch, 16 launches in
+    # flight on 8 streams (the best of the configurations tried on the box)
+    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 24 << 30, 256, 32, 8, 16, 1 if frames_on_device else 0))
     ids = [srv.add_tree(t[2]) for t in trees]
     rng = np.random.default_rng(seed)
     ball_pool = []
@@ -609,9 +611,13 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
         n = max(200, int(rate * duration))
         arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
         reqs = make_requests(n, arrivals)
+        st0 = srv.stats()
         res = srv.replay(reqs)
+        st1 = srv.stats()
         ok = res[:, 0] == 0
         lat = (res[:, 3] - res[:, 1]) * 1e-6
+        queued = (res[:, 2] - res[:, 1]) * 1e-6      # submission to launch
+        ran = (res[:, 3] - res[:, 2]) * 1e-6         # launch to result
         is_frame = np.array([q[0] == "frame" for q in reqs]) & ok
         is_ball = np.array([q[0] == "balls" for q in reqs]) & ok
         span = (res[ok, 3].max() - res[ok, 1].min()) * 1e-9
@@ -619,36 +625,63 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
         out[str(rate)] = {"requests": n, "errors": int((~ok).sum()),
                           "frame_p50_ms": float(np.percentile(lat[is_frame], 50)),
                           "frame_p99_ms": float(np.percentile(lat[is_frame], 99)),
+                          "frame_queue_p99_ms": float(np.percentile(queued[is_frame], 99)),
+                          "frame_run_p99_ms": float(np.percentile(ran[is_frame], 99)),
                           "ball_p50_ms": float(np.percentile(lat[is_ball], 50)) if is_ball.any() else None,
                           "ball_p99_ms": float(np.percentile(lat[is_ball], 99)) if is_ball.any() else None,
                           "error_codes": sorted({int(x) for x in res[~ok, 0]}),
                           "mrays_s": rays / span / 1e6, "offered_hz": rate,
-                          "achieved_hz": n / span}
+                          "achieved_hz": n / span,
+                          "worker": {k: st1[k] - st0[k] for k in ("worker_busy_ns", "host_pin_ns", "host_pins",
+                                                                  "device_alloc_ns", "frame_bytes_out")}}
     stats = srv.stats()
     srv.close()
-    # the plain path: the same kind of frames, one synchronous vox_cuda_render
-    # call at a time into a page-locked host frame
+    busy = {k: stats[k] for k in ("worker_busy_ns", "build_ns", "host_pin_ns", "host_pins", "device_alloc_ns",
+                                  "frame_bytes_out")}
+    # the plain path: the same kind of frames, one synchronous call at a time
+    # -- vox_cuda_render into a page-locked host frame, or with the frames on
+    # the device vox_cuda_render_device into a device frame, then wait
     import torch
     L = vg.lib()
     reqs = [q for q in make_requests(300, np.zeros(300)) if q[0] == "frame"][:150]
-    host = torch.empty(3840 * 2160, dtype=torch.int32).pin_memory()
     tex_c = np.ascontiguousarray(tex)
     tree_of = {ids[i]: trees[i][2] for i in range(len(trees))}
+    if frames_on_device:
+        dframe = torch.empty(3840 * 2160, dtype=torch.int32, device="cuda")
+        dtex = torch.from_numpy(tex_c).cuda()
+        stream = torch.cuda.current_stream()
+
+        def one(q):
+            rc = L.vox_cuda_render_device(tree_of[q[1]].h, C.byref(q[2]), q[3], q[4], C.c_void_p(dtex.data_ptr()),
+                                          C.c_void_p(dframe.data_ptr()), C.c_void_p(stream.cuda_stream))
+            stream.synchronize()
+            return rc
+        call = "vox_cuda_render_device into a device frame, then wait; one frame at a time"
+    else:
+        host = torch.empty(3840 * 2160, dtype=torch.int32).pin_memory()
+
+        def one(q):
+            return L.vox_cuda_render(tree_of[q[1]].h, C.byref(q[2]), q[3], q[4], tex_c.ctypes.data_as(C.c_void_p),
+                                     C.c_void_p(host.data_ptr()), None)
+        call = "vox_cuda_render, one frame at a time, page-locked host frame"
+    for q in reqs[:5]:
+        one(q)
     lat = []
     t_all = time.perf_counter()
     for q in reqs:
         t1 = time.perf_counter()
-        rc = L.vox_cuda_render(tree_of[q[1]].h, C.byref(q[2]), q[3], q[4], tex_c.ctypes.data_as(C.c_void_p),
-                               C.c_void_p(host.data_ptr()), None)
+        rc = one(q)
         if rc:
-            raise vg.VoxCudaError(rc, "vox_cuda_render")
+            raise vg.VoxCudaError(rc, "plain frame")
         lat.append((time.perf_counter() - t1) * 1e3)
     span = time.perf_counter() - t_all
     plain = {"frame_p50_ms": float(np.percentile(lat, 50)), "frame_p99_ms": float(np.percentile(lat, 99)),
-             "mrays_s": sum(q[3] * q[4] for q in reqs) / span / 1e6, "frames": len(reqs),
-             "call": "vox_cuda_render, one frame at a time, page-locked host frame"}
+             "mrays_s": sum(q[3] * q[4] for q in reqs) / span / 1e6, "frames": len(reqs), "call": call}
+    best = max(out.values(), key=lambda v: v["mrays_s"])
     return {"rates": out, "plain": plain, "budget_gb": 40, "clients": 256, "peak_bytes": stats["peak_bytes"],
-            "launches": stats["launches"], "replay": "vox_cuda_server_replay, 8 collector threads"}
+            "frames_on_device": bool(frames_on_device),
+            "speedup_vs_plain_sync": best["mrays_s"] / plain["mrays_s"],
+            "launches": stats["launches"], "replay": "vox_cuda_server_replay, 8 collector threads", "stats": busy}
 
 
 def measure_batched(torch, vg, flush, tex_dev, trees=None):
@@ -678,6 +711,23 @@ def measure_batched(torch, vg, flush, tex_dev, trees=None):
     for _ in range(3):
         plain()
     pb, pm = timed_reps(torch, plain, 5, flush)
+
+    # the plain path as a caller that waits for each frame sees it (what the
+    # drop-in vox_render does): one launch, then wait, per frame; host-timed
+    def plain_sync():
+        for dt, cam, w, h, tex, out in jobs:
+            dt.render_device(cam, w, h, tex, out, stream=sp)
+            torch.cuda.current_stream().synchronize()
+
+    plain_sync()
+    sync_ms = []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plain_sync()
+        sync_ms.append((time.perf_counter() - t0) * 1e3)
+    psm = float(np.median(sync_ms))
     batch = vg.FrameBatch(jobs)
     cfg, tune_ms = batch.autotune(stream=sp, reps=2)
     launch = lambda: batch.launch(stream=sp)
@@ -692,8 +742,11 @@ def measure_batched(torch, vg, flush, tex_dev, trees=None):
     batch.close()
     return {"frames": len(jobs), "rays": rays, "trees": [t[0] for t in trees],
             "plain_ms": pm, "plain_mrays_s": rays / (pm * 1e-3) / 1e6,
+            "plain_sync_ms": psm, "plain_sync_mrays_s": rays / (psm * 1e-3) / 1e6,
             "batched_ms": bm, "batched_mrays_s": rays / (bm * 1e-3) / 1e6,
-            "speedup": pm / bm, "autotuned": cfg, "frames_identical": same,
+            "speedup": pm / bm, "speedup_vs_sync": psm / bm, "autotuned": cfg, "frames_identical": same,
+            "plain": "64 vox_cuda_render_device launches back to back (consecutive kernels overlap)",
+            "plain_sync": "the same launches, each waited for before the next (host-timed)",
             "form": "persistent kernel, work queue, CUDA graph replay"}
 
 # ------------------------------------------------------------------ our arm
@@ -920,16 +973,15 @@ def run_ours(args):
             "gpu_launches": int(launches), "clocks": clk,
             "tree": {"nodes": info["nodes"], "depth": info["depth"], "device_bytes": info["device_bytes"]}}
     if not args.no_extras:
-        # the request server first: its latencies are the extras most easily
-        # disturbed by what ran before in the process
         btrees = build_batch_trees(vg)
-        line["served"] = measure_served(vg, btrees, tex)
         line["quality"] = measure_quality(torch, vg, dt, ht.ptr, states, tex, d_tex, flush,
                                           cpu=not args.no_cpu_baseline)
         line["incoherent"] = measure_incoherent(torch, vg, dt, flush)
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
         line["editing"] = measure_editing(vg, vox)
         line["tree_build"] = measure_tree_build(vg)
+        line["served"] = measure_served(vg, btrees, tex)
+        line["served_device"] = measure_served(vg, btrees, tex, frames_on_device=True)
     if not args.no_cpu_baseline:
         # the CPU leg: the oracle checks every timed frame (the last launch's
         # nf device frames) over its own tree and cameras, then is timed
@@ -937,6 +989,25 @@ def run_ours(args):
         cb = cpu_baseline_sample(ht.ptr, states, tex)
         cb.update(cpu_reference_details(ht.ptr, states, tex, cb["cores"]))
         line["cpu_baseline"] = cb
+    if not args.no_extras:
+        # compact summaries last, where a truncated log still shows them
+        b = line["batched"]
+        line["batched_summary"] = {"frames": b["frames"], "batched_mrays_s": round(b["batched_mrays_s"]),
+                                   "plain_mrays_s": round(b["plain_mrays_s"]),
+                                   "plain_sync_mrays_s": round(b["plain_sync_mrays_s"]),
+                                   "speedup_vs_plain": round(b["speedup"], 2),
+                                   "speedup_vs_plain_sync": round(b["speedup_vs_sync"], 2),
+                                   "frames_identical": b["frames_identical"]}
+
+        def served_summary(sv):
+            d = {r: [round(v["achieved_hz"]), round(v["frame_p50_ms"], 2), round(v["frame_p99_ms"], 2),
+                     round(v["mrays_s"])] for r, v in sv["rates"].items()}
+            d["plain_sync_mrays_s"] = round(sv["plain"]["mrays_s"])
+            d["best_vs_plain_sync"] = round(sv["speedup_vs_plain_sync"], 2)
+            return d
+        line["served_summary"] = {"fields": "offered Hz: [served Hz, frame p50 ms, frame p99 ms, Mrays/s]",
+                                  "host_frames": served_summary(line["served"]),
+                                  "device_frames": served_summary(line["served_device"])}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -450,6 +450,12 @@ typedef struct {
     uint32_t max_batch;      /* requests per launch (1..1024)                     */
     uint32_t streams;        /* launch streams (1..32)                            */
     uint32_t max_launches;   /* launches in flight at once                        */
+    uint32_t frames_on_device;  /* 0: frames are copied into pinned host memory;
+                                   1: frames stay in device memory the server
+                                   owns (vox_cuda_server_result gives a device
+                                   pointer; the frame holds its share of the
+                                   device budget until released) -- for clients
+                                   that use the frames on the GPU */
 } vox_cuda_server_config;
 
 typedef struct {
@@ -457,6 +463,12 @@ typedef struct {
     uint64_t bytes_in_use, peak_bytes;            /* device budget */
     uint64_t pending, inflight;
     uint64_t host_bytes_in_use, host_peak_bytes;  /* pinned-host budget */
+    /* where the worker thread's time goes (ns since creation): all of its
+     * work outside its waits; building and enqueueing launches; pinning new
+     * host result buffers (host_pins of them: the pool's misses); device
+     * allocations of job tables and frames.  frame_bytes_out: frame bytes
+     * copied to host memory. */
+    uint64_t worker_busy_ns, build_ns, host_pin_ns, host_pins, device_alloc_ns, frame_bytes_out;
 } vox_cuda_server_stats;
 
 typedef struct vox_cuda_server vox_cuda_server;
@@ -477,8 +489,10 @@ int vox_cuda_server_submit_balls(vox_cuda_server *srv, uint32_t tree_id, const f
 /* Wait up to timeout_ms for a request: its status, or VOX_CUDA_ETIMEOUT. */
 int vox_cuda_server_wait(vox_cuda_server *srv, uint64_t ticket, uint32_t timeout_ms);
 /* A finished request's result (w*h ARGB pixels, or n hit bytes) in server
- * memory, valid until vox_cuda_server_release; times_ns (may be NULL) gets
- * submission, launch and completion times (steady clock, ns). */
+ * memory -- pinned host memory, or for frames of a server with
+ * frames_on_device set, device memory of the server's device -- valid until
+ * vox_cuda_server_release; times_ns (may be NULL) gets submission, launch
+ * and completion times (steady clock, ns). */
 int vox_cuda_server_result(vox_cuda_server *srv, uint64_t ticket, const void **data, size_t *bytes,
                            uint64_t *times_ns);
 int vox_cuda_server_release(vox_cuda_server *srv, uint64_t ticket);

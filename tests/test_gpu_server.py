@@ -121,6 +121,38 @@ def test_mixed_requests_equal_requests_alone(setup):
     assert stats["launches"] >= 1
 
 
+def test_frames_on_device_equal_oracle(setup):
+    """A server whose frames stay in device memory: every frame (read from the
+    device pointer the server hands out) and every ball answer of a mixed
+    request stream equals the oracle's and the plain call's; a kept frame
+    holds its device bytes until it is released, and nothing of it goes
+    through host memory."""
+    vg, wl, hosts, trees, tex = setup
+    reqs = _requests(wl, 40, 5)
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, 1 << 32, 64, 16, 4, 8, 1))
+    ids = [srv.add_tree(t) for t in trees]
+    resident = srv.stats()["bytes_in_use"]
+    tickets = []
+    for q in reqs:
+        if q[0] == "frame":
+            tickets.append(srv.submit_frame(ids[q[1]], q[2], q[3], q[4]))
+        else:
+            tickets.append(srv.submit_balls(ids[q[1]], q[2], q[3]))
+    for t in tickets:
+        assert srv.wait(t, 60000) == 0
+    held = srv.stats()["bytes_in_use"] - resident
+    frame_bytes = sum(q[3] * q[4] * 4 for q in reqs if q[0] == "frame")
+    assert held >= frame_bytes                            # every finished frame is still on the device
+    for q, t in zip(reqs, tickets):
+        got, _ = srv.result(t, on_device=q[0] == "frame")
+        assert np.array_equal(got, _alone(trees, tex, q)), q[0]
+        assert np.array_equal(got, _oracle(tex, q)), q[0]
+        srv.release(t)
+    st = srv.stats()
+    assert st["bytes_in_use"] == resident and st["frame_bytes_out"] == 0
+    srv.close()
+
+
 def _pinned_class(nbytes):
     c = 4096
     while c < nbytes:

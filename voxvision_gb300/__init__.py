@@ -448,6 +448,17 @@ class FrameBatch:
             pass
 
 
+def device_bytes(ptr: int, nbytes: int):
+    """A torch uint8 tensor viewing `nbytes` of device memory at `ptr` (no
+    copy), through the CUDA array interface."""
+    import torch
+
+    class _View:
+        __cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False), "version": 2}
+
+    return torch.as_tensor(_View(), device="cuda")
+
+
 class Server:
     """vox_cuda_server: frame and ball requests from many threads, admitted by
     a device-memory budget and batched continuously onto the GPU."""
@@ -483,15 +494,19 @@ class Server:
     def wait(self, ticket: int, timeout_ms: int = 60000) -> int:
         return int(lib().vox_cuda_server_wait(self.h, ticket, timeout_ms))
 
-    def result(self, ticket: int, copy: bool = True):
-        """(array of the result, (t_submit, t_launch, t_done) ns)."""
+    def result(self, ticket: int, copy: bool = True, on_device: bool = False):
+        """(array of the result, (t_submit, t_launch, t_done) ns).  With
+        on_device (a frame of a server whose frames stay on the device) the
+        result is copied out of device memory."""
         data = C.c_void_p()
         nbytes = C.c_size_t()
         times = (C.c_uint64 * 3)()
         check(lib().vox_cuda_server_result(self.h, ticket, C.byref(data), C.byref(nbytes), times),
               "vox_cuda_server_result")
         arr = None
-        if copy:
+        if copy and on_device:
+            arr = device_bytes(data.value, nbytes.value).cpu().numpy()
+        elif copy:
             arr = np.ctypeslib.as_array((C.c_uint8 * nbytes.value).from_address(data.value)).copy()
         return arr, tuple(int(x) for x in times)
 

@@ -66,7 +66,7 @@ class ServerConfig(C.Structure):
     """vox_cuda_server_config (include/voxtrees_cuda.h)."""
     _fields_ = [("budget_bytes", C.c_uint64), ("host_budget_bytes", C.c_uint64), ("max_inflight", C.c_uint32),
                 ("max_batch", C.c_uint32),
-                ("streams", C.c_uint32), ("max_launches", C.c_uint32)]
+                ("streams", C.c_uint32), ("max_launches", C.c_uint32), ("frames_on_device", C.c_uint32)]
 
 
 class RenderConfig(C.Structure):
@@ -90,7 +90,8 @@ class ReplayResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "rejected", "launches", "bytes_in_use",
                                           "peak_bytes", "pending", "inflight", "host_bytes_in_use",
-                                          "host_peak_bytes")]
+                                          "host_peak_bytes", "worker_busy_ns", "build_ns", "host_pin_ns",
+                                          "host_pins", "device_alloc_ns", "frame_bytes_out")]
 
 
 _lib = None

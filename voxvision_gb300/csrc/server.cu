@@ -86,9 +86,13 @@ class PinnedPool {
             }
         }
         void *p = nullptr;
-        if (cudaMallocHost(&p, cls) != cudaSuccess) return nullptr;
-        return p;
+        uint64_t t0 = now_ns();
+        cudaError_t e = cudaMallocHost(&p, cls);
+        pin_ns.fetch_add(now_ns() - t0, std::memory_order_relaxed);
+        pins.fetch_add(1, std::memory_order_relaxed);
+        return e == cudaSuccess ? p : nullptr;
     }
+    std::atomic<uint64_t> pin_ns{0}, pins{0};   // time and count of new pinned buffers
     void put(void *p, size_t cls)
     {
         if (!p) return;
@@ -114,6 +118,8 @@ struct Request {
     uint64_t host_bytes = 0;        // charged to the pinned-host budget while admitted
     void *h_res = nullptr;          // pinned result, written in place by the kernels
     size_t h_cls = 0, res_bytes = 0;
+    void *d_res = nullptr;          // a frame kept in device memory (frames_on_device)
+    uint64_t dev_hold = 0;          // device bytes still charged after the launch ends (until release)
     void *h_in = nullptr;           // pinned ball inputs
     size_t h_in_cls = 0;
     uint64_t t_submit = 0, t_launch = 0, t_done = 0;
@@ -163,6 +169,9 @@ struct vox_cuda_server {
     bool failed = false;            // the worker stopped on a failure: requests are refused
     std::atomic<int> inject{0};     // host-side fault for the next launch (vox_cuda_server_inject)
     std::thread worker;
+    cudaMemPool_t pool = nullptr;   // device frames and job tables (keeps its memory mapped)
+    // worker time accounting (vox_cuda_server_stats)
+    std::atomic<uint64_t> busy_ns{0}, build_ns{0}, alloc_ns{0}, bytes_out{0};
 };
 
 namespace {
@@ -210,7 +219,8 @@ void retire(vox_cuda_server *s, std::vector<Launch *> &out)
         for (Request *r : L->reqs) {
             if (r->h_in) L->host_free.push_back({r->h_in, r->h_in_cls});
             r->h_in = nullptr;
-            s->used -= r->dev_bytes;
+            if (!r->d_res) r->dev_hold = 0;      // nothing of it stays on the device
+            s->used -= r->dev_bytes - r->dev_hold;
             s->host_used -= r->host_bytes;
             s->inflight_reqs--;
             r->done = true;
@@ -267,9 +277,23 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
         }
         size_t out_bytes = r->kind == FRAME ? (size_t)r->w * r->h * 4 : (size_t)r->n;
         r->res_bytes = out_bytes;
-        r->h_res = s->pinned.get(out_bytes, &r->h_cls);
+        const bool on_device = r->kind == FRAME && s->cfg.frames_on_device;
+        if (on_device) {   // the frame is drawn where the client will read it
+            uint64_t ta = now_ns();
+            cudaError_t e = cudaMallocFromPoolAsync(&r->d_res, out_bytes, s->pool, st);
+            s->alloc_ns.fetch_add(now_ns() - ta, std::memory_order_relaxed);
+            if (e != cudaSuccess) {
+                r->d_res = nullptr;
+                r->status = VOX_CUDA_ENOMEM;
+                continue;
+            }
+            r->dev_hold = r->dev_bytes - 256;    // the frame; its job-table share goes with the launch
+        } else {
+            r->h_res = s->pinned.get(out_bytes, &r->h_cls);
+        }
         void *d_res = nullptr;
-        if (!r->h_res || (r->kind != FRAME && cudaHostGetDevicePointer(&d_res, r->h_res, 0) != cudaSuccess)) {
+        if ((!on_device && !r->h_res) ||
+            (r->kind != FRAME && cudaHostGetDevicePointer(&d_res, r->h_res, 0) != cudaSuccess)) {
             r->status = VOX_CUDA_ENOMEM;
             continue;
         }
@@ -283,8 +307,8 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
             j.argb = nullptr;   // set once the launch's device frames exist
             jobs.push_back(j);
             frames.push_back(r);
-            frame_at.push_back(frame_bytes);
-            frame_bytes += (out_bytes + 255) & ~size_t(255);
+            frame_at.push_back(on_device ? SIZE_MAX : frame_bytes);
+            if (!on_device) frame_bytes += (out_bytes + 255) & ~size_t(255);
         } else {
             size_t n = r->n, in_bytes = n * 16;
             void *d_in = nullptr;
@@ -306,17 +330,25 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
         size_t tb = (frame_job_table_bytes((uint32_t)jobs.size()) + 255) & ~(size_t)255;
         L->h_table = s->pinned.get(tb, &L->h_table_cls);
         int rc = VOX_CUDA_ENOMEM;
-        if (L->h_table && cudaMallocAsync(&L->d_table, tb + 256, st) == cudaSuccess &&
-            cudaMallocAsync(&L->d_frames, frame_bytes, st) == cudaSuccess) {
+        uint64_t ta = now_ns();
+        bool got = L->h_table && cudaMallocFromPoolAsync(&L->d_table, tb + 256, s->pool, st) == cudaSuccess &&
+                   (frame_bytes == 0 || cudaMallocFromPoolAsync(&L->d_frames, frame_bytes, s->pool, st) == cudaSuccess);
+        s->alloc_ns.fetch_add(now_ns() - ta, std::memory_order_relaxed);
+        if (got) {
             for (size_t q = 0; q < jobs.size(); q++)
-                jobs[q].argb = reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_frames) + frame_at[q]);
+                jobs[q].argb = frame_at[q] == SIZE_MAX
+                                   ? static_cast<uint32_t *>(frames[q]->d_res)
+                                   : reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_frames) + frame_at[q]);
             uint32_t *counter = reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_table) + tb);
             rc = enqueue_frame_jobs(jobs.data(), (uint32_t)jobs.size(), L->h_table, L->d_table, counter,
                                     s->nsm, st);
-            for (size_t q = 0; q < frames.size() && rc == VOX_CUDA_OK; q++)   // results out after the kernel
+            for (size_t q = 0; q < frames.size() && rc == VOX_CUDA_OK; q++) {  // results out after the kernel
+                if (frames[q]->d_res) continue;                                  // stays on the device
                 if (cudaMemcpyAsync(frames[q]->h_res, jobs[q].argb, frames[q]->res_bytes, cudaMemcpyDeviceToHost,
                                     st) != cudaSuccess)
                     rc = VOX_CUDA_ECUDA;
+                s->bytes_out.fetch_add(frames[q]->res_bytes, std::memory_order_relaxed);
+            }
         }
         if (rc)
             for (Request *r : frames) r->status = rc;
@@ -370,8 +402,9 @@ void stop_on_failure(vox_cuda_server *s, std::vector<Request *> &batch)
     auto end = [&](Request *r, bool charged, bool keep_status) {
         if (r->done) return;
         if (!keep_status) r->status = VOX_CUDA_ENOMEM;
+        if (!r->d_res) r->dev_hold = 0;          // a kept frame stays charged until released
         if (charged) {
-            s->used -= r->dev_bytes;
+            s->used -= r->dev_bytes - r->dev_hold;
             s->host_used -= r->host_bytes;
             s->inflight_reqs--;
         }
@@ -430,16 +463,20 @@ void serve(vox_cuda_server *s, std::vector<Launch *> &retired, std::vector<Reque
                 s->building++;
             }
         }
+        uint64_t t0 = now_ns();
         for (Launch *L : retired) release_launch(s, L);
         retired.clear();
         if (!batch.empty()) {
+            uint64_t tb = now_ns();
             Launch *L = build_launch(s, batch, st);
+            s->build_ns.fetch_add(now_ns() - tb, std::memory_order_relaxed);
             batch.clear();
             std::lock_guard<std::mutex> lk(s->mu);
             s->building--;
             s->inflight.push_back(L);
             s->launches++;
         }
+        s->busy_ns.fetch_add(now_ns() - t0, std::memory_order_relaxed);
         if (quit) break;
     }
 }
@@ -479,9 +516,22 @@ try {
         delete s;
         return VOX_CUDA_ENODEV;
     }
-    if (cudaMalloc(&s->d_tex, 32768) != cudaSuccess) { delete s; return VOX_CUDA_ENOMEM; }
+    // A pool of its own for the launches' frames and job tables that keeps
+    // the memory it has mapped (release threshold: the device budget), so
+    // a launch after a quiet spell does not map memory again.
+    {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = s->device;
+        if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess) { delete s; return VOX_CUDA_ENOMEM; }
+        uint64_t keep = cfg.budget_bytes;
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (cudaMalloc(&s->d_tex, 32768) != cudaSuccess) { cudaMemPoolDestroy(s->pool); delete s; return VOX_CUDA_ENOMEM; }
     if (cudaMemcpy(s->d_tex, texture, 32768, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(s->d_tex);
+        cudaMemPoolDestroy(s->pool);
         delete s;
         return VOX_CUDA_ECUDA;
     }
@@ -490,6 +540,7 @@ try {
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
             for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
             cudaFree(s->d_tex);
+            cudaMemPoolDestroy(s->pool);
             delete s;
             return VOX_CUDA_ECUDA;
         }
@@ -568,7 +619,7 @@ try {
     r->w = w;
     r->h = h;
     r->dev_bytes = request_bytes(FRAME, w, h);
-    r->host_bytes = request_host_bytes(FRAME, w, h);
+    r->host_bytes = s->cfg.frames_on_device ? 0 : request_host_bytes(FRAME, w, h);
     return submit(s, r, ticket);
 } VOX_ABI_FAIL_INT
 
@@ -609,7 +660,7 @@ try {
     if (it == s->reqs.end()) return VOX_CUDA_EINVAL;
     Request *r = it->second;
     if (!r->done) return VOX_CUDA_ETIMEOUT;
-    if (data) *data = r->h_res;
+    if (data) *data = r->d_res ? r->d_res : r->h_res;
     if (bytes) *bytes = r->res_bytes;
     if (times_ns) {
         times_ns[0] = r->t_submit;
@@ -628,6 +679,10 @@ try {
     Request *r = it->second;
     if (!r->done) return VOX_CUDA_EINVAL;
     s->pinned.put(r->h_res, r->h_cls);
+    if (r->d_res) {   // its launch has ended: the frame is free on any stream
+        cudaFreeAsync(r->d_res, s->streams[0]);
+        s->used -= r->dev_hold;
+    }
     s->reqs.erase(it);
     delete r;
     return VOX_CUDA_OK;
@@ -655,6 +710,12 @@ try {
     st->inflight = s->inflight_reqs;
     st->host_bytes_in_use = s->host_used;
     st->host_peak_bytes = s->host_peak;
+    st->worker_busy_ns = s->busy_ns.load();
+    st->build_ns = s->build_ns.load();
+    st->host_pin_ns = s->pinned.pin_ns.load();
+    st->host_pins = s->pinned.pins.load();
+    st->device_alloc_ns = s->alloc_ns.load();
+    st->frame_bytes_out = s->bytes_out.load();
     return VOX_CUDA_OK;
 } VOX_ABI_FAIL_INT
 
@@ -669,6 +730,11 @@ try {
     if (s->worker.joinable()) s->worker.join();
     for (Launch *L : s->inflight) release_launch(s, L);   // left by a worker stopped on a failure
     s->inflight.clear();
+    for (auto &kv : s->reqs)
+        if (kv.second->d_res) {
+            cudaFreeAsync(kv.second->d_res, s->streams[0]);
+            kv.second->d_res = nullptr;
+        }
     for (cudaStream_t st : s->streams) {
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
@@ -678,6 +744,7 @@ try {
         delete kv.second;
     }
     cudaFree(s->d_tex);
+    if (s->pool) cudaMemPoolDestroy(s->pool);   // every launch's memory was freed on its synchronised stream
     delete s;
     return VOX_CUDA_OK;
 } VOX_ABI_FAIL_INT
