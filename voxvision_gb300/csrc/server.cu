@@ -57,7 +57,7 @@ uint64_t now_ns()
                std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Pinned host buffers by power-of-two size class, reused across requests.
+// Size class of a pinned buffer: the next power of two from 4 KiB.
 size_t pinned_class(size_t bytes)
 {
     size_t cls = 4096;
@@ -65,13 +65,48 @@ size_t pinned_class(size_t bytes)
     return cls;
 }
 
+// Pinned host buffers by power-of-two size class, reused across requests.
+// Buffers up to 64 MiB are carved from 128 MiB pinned slabs; a part of the
+// host budget is pinned in slabs when the server starts, and a refill thread
+// pins the next slab while the current one is being carved, so the worker
+// thread -- which admits and launches every request -- does not stop for
+// page-locking (14 GB/s on the Grace host: 4.5 ms for one 64 MiB buffer).
+// Larger buffers are pinned one by one.  Buffers go back to their class's
+// free list and slabs stay pinned until the pool is destroyed.
 class PinnedPool {
   public:
+    static constexpr size_t SLAB = size_t(128) << 20, MAX_CARVED = size_t(64) << 20;
+
     ~PinnedPool()
     {
-        for (auto &kv : free_)
-            for (void *p : kv.second) cudaFreeHost(p);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        if (refill_.joinable()) refill_.join();
+        for (void *p : slabs_) cudaFreeHost(p);
+        for (void *p : spares_) cudaFreeHost(p);
+        for (void *p : direct_) cudaFreeHost(p);
     }
+
+    // Pins `now` bytes (whole slabs) at once and starts the refill thread for
+    // device `dev`, which pins further slabs while fewer than `cap` bytes are
+    // in slabs.  Returns false if the first slabs cannot be pinned.
+    bool start(int dev, size_t now, size_t cap)
+    {
+        dev_ = dev;
+        cap_ = cap;
+        for (size_t got = 0; got + SLAB <= now; got += SLAB) {
+            void *p = nullptr;
+            if (cudaHostAlloc(&p, SLAB, cudaHostAllocDefault) != cudaSuccess) return false;
+            spares_.push_back(p);
+            pinned_ += SLAB;
+        }
+        refill_ = std::thread([this] { refill_loop(); });
+        return true;
+    }
+
     void *get(size_t bytes, size_t *cls_out)
     {
         size_t cls = pinned_class(bytes);
@@ -84,15 +119,33 @@ class PinnedPool {
                 v.pop_back();
                 return p;
             }
+            if (cls <= MAX_CARVED) {
+                if (cur_used_ + cls > SLAB && !spares_.empty()) {   // next slab, pinned ahead
+                    cur_ = static_cast<char *>(spares_.back());
+                    spares_.pop_back();
+                    slabs_.push_back(cur_);
+                    cur_used_ = 0;
+                    cv_.notify_all();
+                }
+                if (cur_ && cur_used_ + cls <= SLAB) {
+                    void *p = cur_ + cur_used_;
+                    cur_used_ += cls;
+                    return p;
+                }
+            }
         }
+        // no slab room ready (or a buffer larger than a slab carves): pin here
         void *p = nullptr;
         uint64_t t0 = now_ns();
         cudaError_t e = cudaMallocHost(&p, cls);
         pin_ns.fetch_add(now_ns() - t0, std::memory_order_relaxed);
         pins.fetch_add(1, std::memory_order_relaxed);
-        return e == cudaSuccess ? p : nullptr;
+        if (e != cudaSuccess) return nullptr;
+        std::lock_guard<std::mutex> lk(mu_);
+        direct_.push_back(p);
+        return p;
     }
-    std::atomic<uint64_t> pin_ns{0}, pins{0};   // time and count of new pinned buffers
+    std::atomic<uint64_t> pin_ns{0}, pins{0};   // time and count of buffers the worker pinned itself
     void put(void *p, size_t cls)
     {
         if (!p) return;
@@ -101,8 +154,34 @@ class PinnedPool {
     }
 
   private:
+    // Keeps one spare slab pinned while the pool lives.
+    void refill_loop()
+    {
+        cudaSetDevice(dev_);
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [this] { return stop_ || (spares_.empty() && pinned_ + SLAB <= cap_); });
+            if (stop_) return;
+            lk.unlock();
+            void *p = nullptr;
+            bool ok = cudaHostAlloc(&p, SLAB, cudaHostAllocDefault) == cudaSuccess;
+            lk.lock();
+            if (!ok) return;        // out of pinnable memory: the worker pins what it needs itself
+            spares_.push_back(p);
+            pinned_ += SLAB;
+        }
+    }
+
     std::mutex mu_;
+    std::condition_variable cv_;
     std::map<size_t, std::vector<void *>> free_;
+    std::vector<void *> slabs_, spares_, direct_;
+    char *cur_ = nullptr;
+    size_t cur_used_ = SLAB;
+    size_t pinned_ = 0, cap_ = 0;   // bytes in slabs, and the most the refill thread pins
+    int dev_ = 0;
+    bool stop_ = false;
+    std::thread refill_;
 };
 
 enum Kind { FRAME = 0, BALLS = 1 };
@@ -547,6 +626,13 @@ try {
         s->streams.push_back(st);
     }
     try {
+        // a quarter of the pinned-host budget (at most 2 GiB) pinned now, up
+        // to the budget in slabs as results need it
+        if (!s->pinned.start(s->device, std::min<uint64_t>(cfg.host_budget_bytes / 4, uint64_t(2) << 30),
+                             cfg.host_budget_bytes)) {
+            vox_cuda_server_destroy(s);
+            return VOX_CUDA_ENOMEM;
+        }
         // the worker's vectors never grow past these while it runs
         s->admitted.reserve(cfg.max_batch);
         s->inflight.reserve(cfg.max_launches);
