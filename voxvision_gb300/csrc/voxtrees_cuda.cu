@@ -236,9 +236,10 @@ __device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const floa
 // launch.  The results are the reference's by construction: the same
 // searches of the same rays, the same choices between them.
 
-// Root search of every pixel: {leaf record or VOXP_EMPTY, intersection point}.
-// Pixels outside [x0, x1) x [y0, y1) miss the tree's box (the rectangle of
-// frame_rect) and are written as misses without a search.
+// Root search of every pixel of the rectangle [x0, x1) x [y0, y1) (the
+// rectangle of frame_rect, whole 4x4 squares; every pixel outside it misses
+// the tree's box): {leaf record or VOXP_EMPTY, intersection point}, stored
+// row by row of the rectangle.
 template <int CAP, bool RAYS>
 __global__ void __launch_bounds__(128) root_hits_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
                                                         uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
@@ -246,11 +247,11 @@ __global__ void __launch_bounds__(128) root_hits_kernel(DevTree t, vox_cuda_came
                                                         uint32_t *__restrict__ status)
 {
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t px = blockIdx.x * TILE_W + (warp & 1) * 8 + (lane & 7);
-    uint32_t py = blockIdx.y * TILE_H + (warp >> 1) * 4 + (lane >> 3);
-    if (px >= w || py >= h) return;
+    uint32_t px = x0 + blockIdx.x * TILE_W + (warp & 1) * 8 + (lane & 7);
+    uint32_t py = y0 + blockIdx.y * TILE_H + (warp >> 1) * 4 + (lane >> 3);
+    if (px >= x1 || py >= y1) return;
     uint4 res = make_uint4(VOXP_EMPTY, 0u, 0u, 0u);
-    if (t.root != VOXP_EMPTY && px >= x0 && px < x1 && py >= y0 && py < y1) {
+    if (t.root != VOXP_EMPTY) {
         float dx, dy, dz;
         pixel_dir<RAYS>(cam, rays, w, (int)px, (int)py, dx, dy, dz);
         Counts c{0, 0, 0};
@@ -261,10 +262,12 @@ __global__ void __launch_bounds__(128) root_hits_kernel(DevTree t, vox_cuda_came
             res = make_uint4(hh.rec, __float_as_uint(hh.x), __float_as_uint(hh.y), __float_as_uint(hh.z));
         if (overflow) atomicOr(status, 1u);
     }
-    hits[(size_t)py * w + px] = res;
+    hits[(size_t)(py - y0) * (x1 - x0) + (px - x0)] = res;
 }
 
-// renderer.c:215-318 per 4x4 square over the root searches of root_hits_kernel.
+// renderer.c:215-318 per 4x4 square of the rectangle [x0, x1) x [y0, y1)
+// over the root searches of root_hits_kernel (the squares outside it draw
+// nothing: every search of theirs misses).
 template <int CAP, bool RAYS>
 __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
                                                              uint32_t h, unsigned int quality,
@@ -272,20 +275,21 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
                                                              uint32_t *__restrict__ argb,
                                                              uint32_t *__restrict__ status, vox::DevLights lights,
                                                              const float *__restrict__ rays,
-                                                             const uint4 *__restrict__ hits)
+                                                             const uint4 *__restrict__ hits, uint32_t x0,
+                                                             uint32_t y0, uint32_t x1, uint32_t y1)
 {
     // renderer.c:23-25 rendering order {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}, a nibble each
     constexpr uint64_t ORDER = 0xFEBADC9876325410ull;
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t sx = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);     // square coordinates
-    uint32_t sy = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
-    uint32_t ws = w >> 2, hs = h >> 2;
-    if (sx >= ws || sy >= hs) return;
+    uint32_t sx = (x0 >> 2) + blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);     // square coordinates
+    uint32_t sy = (y0 >> 2) + blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    if (sx >= (x1 >> 2) || sy >= (y1 >> 2)) return;
+    const uint32_t rw = x1 - x0;                                      // row length of the root searches
     const int xstart = (int)sx * 4, ystart = (int)sy * 4;
     const float ox = cam.position[0], oy = cam.position[1], oz = cam.position[2];
     const int rnd_mode = quality & VOX_CUDA_QUALITY_MODE_MASK;
     const int merge_mode = quality & VOX_CUDA_QUALITY_RM_MASK;
-    const uint4 *sq = hits + (size_t)ystart * w + xstart;             // the square's root searches
+    const uint4 *sq = hits + (size_t)(ystart - (int)y0) * rw + (xstart - (int)x0);   // the square's root searches
     uint32_t out[16];
 #pragma unroll
     for (int i = 0; i < 16; i++) out[i] = 0u;
@@ -309,7 +313,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
             ix = __uint_as_float(h1.y); iy = __uint_as_float(h1.z); iz = __uint_as_float(h1.w);
             iend = 15;
             out[0] = vox::hit_color(tex, t, lights, ix, iy, iz, overflow);
-            const uint4 h2 = sq[3 * (size_t)w + 3];
+            const uint4 h2 = sq[3 * (size_t)rw + 3];
             if (h2.x != VOXP_EMPTY) {
                 const float jx = __uint_as_float(h2.y), jy = __uint_as_float(h2.z), jz = __uint_as_float(h2.w);
                 out[15] = vox::hit_color(tex, t, lights, jx, jy, jz, overflow);
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda
                 }
             }
             if (from_root) {
-                const uint4 hr = sq[(size_t)py * w + px];
+                const uint4 hr = sq[(size_t)py * rw + px];
                 have_leaf = hr.x != VOXP_EMPTY;
                 if (have_leaf) {
                     leaf_rec = hr.x;
@@ -488,14 +492,23 @@ cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera 
         plan_frame(t, cam, w, h, g_render_cull.load() != 0, p);
         x0 = p.x0; y0 = p.y0; x1 = p.x1; y1 = p.y1;
     }
+    // pixels outside the rectangle are misses: the frame is cleared first and
+    // only the rectangle's squares are drawn
+    cudaError_t e = cudaSuccess;
+    if (x0 != 0 || y0 != 0 || x1 != w || y1 != h) {
+        e = cudaMemsetAsync(argb, 0, (size_t)w * h * 4, s);
+        if (e != cudaSuccess || x1 <= x0 || y1 <= y0) return e;
+    }
+    const uint32_t rw = x1 - x0, rh = y1 - y0;
     uint4 *hits = nullptr;
-    cudaError_t e = cudaMallocAsync(&hits, (size_t)w * h * sizeof(uint4), s);
+    e = cudaMallocAsync(&hits, (size_t)rw * rh * sizeof(uint4), s);
     if (e != cudaSuccess) return e;
     const int cap = t->cap_class;
     void (*roots)(DevTree, vox_cuda_camera, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
                   const float *, uint4 *, uint32_t *);
     void (*squares)(DevTree, vox_cuda_camera, uint32_t, uint32_t, unsigned int, const uint8_t *, uint32_t *,
-                    uint32_t *, vox::DevLights, const float *, const uint4 *);
+                    uint32_t *, vox::DevLights, const float *, const uint4 *, uint32_t, uint32_t, uint32_t,
+                    uint32_t);
     if (rays) {
         roots = cap == 0 ? root_hits_kernel<CAP0, true> : cap == 1 ? root_hits_kernel<CAP1, true>
                                                                    : root_hits_kernel<CAP2, true>;
@@ -507,12 +520,12 @@ cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera 
         squares = cap == 0 ? render_squares_kernel<CAP0, false>
                 : cap == 1 ? render_squares_kernel<CAP1, false> : render_squares_kernel<CAP2, false>;
     }
-    roots<<<dim3((w + TILE_W - 1) / TILE_W, (h + TILE_H - 1) / TILE_H), 128, 0, s>>>(
+    roots<<<dim3((rw + TILE_W - 1) / TILE_W, (rh + TILE_H - 1) / TILE_H), 128, 0, s>>>(
         t->dev, cam, w, h, x0, y0, x1, y1, rays, hits, t->d_status);
     count_launch();
-    const uint32_t ws = w / 4, hs = h / 4;
+    const uint32_t ws = rw / 4, hs = rh / 4;
     squares<<<dim3((ws + 15) / 16, (hs + 7) / 8), 128, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status,
-                                                               L, rays, hits);
+                                                               L, rays, hits, x0, y0, x1, y1);
     count_launch();
     e = cudaGetLastError();
     cudaFreeAsync(hits, s);
