@@ -981,7 +981,8 @@ def run_ours(args):
         line["editing"] = measure_editing(vg, vox)
         line["tree_build"] = measure_tree_build(vg)
         line["served"] = measure_served(vg, btrees, tex)
-        line["served_device"] = measure_served(vg, btrees, tex, frames_on_device=True)
+        line["served_device"] = measure_served(vg, btrees, tex, frames_on_device=True,
+                                               rates=(1000, 2000, 5000, 10000, 15000, 20000, 30000))
     if not args.no_cpu_baseline:
         # the CPU leg: the oracle checks every timed frame (the last launch's
         # nf device frames) over its own tree and cameras, then is timed
