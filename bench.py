@@ -633,7 +633,8 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
                           "mrays_s": rays / span / 1e6, "offered_hz": rate,
                           "achieved_hz": n / span,
                           "worker": {k: st1[k] - st0[k] for k in ("worker_busy_ns", "host_pin_ns", "host_pins",
-                                                                  "device_alloc_ns", "frame_bytes_out")}}
+                                                                  "device_alloc_ns", "frame_bytes_out",
+                                                                  "host_slabs")}}
     stats = srv.stats()
     srv.close()
     busy = {k: stats[k] for k in ("worker_busy_ns", "build_ns", "host_pin_ns", "host_pins", "device_alloc_ns",

@@ -467,8 +467,9 @@ typedef struct {
      * work outside its waits; building and enqueueing launches; pinning new
      * host result buffers (host_pins of them: the pool's misses); device
      * allocations of job tables and frames.  frame_bytes_out: frame bytes
-     * copied to host memory. */
-    uint64_t worker_busy_ns, build_ns, host_pin_ns, host_pins, device_alloc_ns, frame_bytes_out;
+     * copied to host memory.  host_slabs: 128 MiB slabs pinned for results,
+     * at creation and by the server's refill thread. */
+    uint64_t worker_busy_ns, build_ns, host_pin_ns, host_pins, device_alloc_ns, frame_bytes_out, host_slabs;
 } vox_cuda_server_stats;
 
 typedef struct vox_cuda_server vox_cuda_server;

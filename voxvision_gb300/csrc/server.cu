@@ -146,6 +146,11 @@ class PinnedPool {
         return p;
     }
     std::atomic<uint64_t> pin_ns{0}, pins{0};   // time and count of buffers the worker pinned itself
+    uint64_t slabs()
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        return pinned_ / SLAB;
+    }
     void put(void *p, size_t cls)
     {
         if (!p) return;
@@ -802,6 +807,7 @@ try {
     st->host_pins = s->pinned.pins.load();
     st->device_alloc_ns = s->alloc_ns.load();
     st->frame_bytes_out = s->bytes_out.load();
+    st->host_slabs = s->pinned.slabs();
     return VOX_CUDA_OK;
 } VOX_ABI_FAIL_INT
 
