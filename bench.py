@@ -634,11 +634,11 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
                           "achieved_hz": n / span,
                           "worker": {k: st1[k] - st0[k] for k in ("worker_busy_ns", "host_pin_ns", "host_pins",
                                                                   "device_alloc_ns", "frame_bytes_out",
-                                                                  "host_slabs")}}
+                                                                  "frame_bytes_full", "host_slabs")}}
     stats = srv.stats()
     srv.close()
     busy = {k: stats[k] for k in ("worker_busy_ns", "build_ns", "host_pin_ns", "host_pins", "device_alloc_ns",
-                                  "frame_bytes_out")}
+                                  "frame_bytes_out", "frame_bytes_full")}
     # the plain path: the same kind of frames, one synchronous call at a time
     # -- vox_cuda_render into a page-locked host frame, or with the frames on
     # the device vox_cuda_render_device into a device frame, then wait

@@ -467,9 +467,13 @@ typedef struct {
      * work outside its waits; building and enqueueing launches; pinning new
      * host result buffers (host_pins of them: the pool's misses); device
      * allocations of job tables and frames.  frame_bytes_out: frame bytes
-     * copied to host memory.  host_slabs: 128 MiB slabs pinned for results,
-     * at creation and by the server's refill thread. */
+     * copied to host memory; frame_bytes_full: the bytes of those frames
+     * (w*h*4 each) -- a result buffer the server reuses already holds zeros
+     * outside the rectangle of the frame it held last, so only the part of a
+     * frame that can differ is copied.  host_slabs: 128 MiB slabs pinned for
+     * results, at creation and by the server's refill thread. */
     uint64_t worker_busy_ns, build_ns, host_pin_ns, host_pins, device_alloc_ns, frame_bytes_out, host_slabs;
+    uint64_t frame_bytes_full;
 } vox_cuda_server_stats;
 
 typedef struct vox_cuda_server vox_cuda_server;

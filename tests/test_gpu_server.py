@@ -296,3 +296,44 @@ def test_injected_worker_failure_ends_requests_and_refuses_new_ones(setup):
     assert st["inflight"] == 0 and st["pending"] == 0
     assert st["bytes_in_use"] == resident and st["host_bytes_in_use"] == 0
     srv.close()
+
+
+def test_reused_result_buffers_hold_exact_frames(setup):
+    """Result buffers are reused, and a frame copies out only the box that
+    covers its tree's screen rectangle and what the buffer's previous frame
+    left there.  Requests one at a time (each buffer goes back before the
+    next request takes it) walk one 128 KiB buffer class through every case:
+    a new buffer, frames of the same size from other poses, a frame that
+    sees nothing (the old picture must be cleared), frames of another row
+    pitch or height in the same class, and a buffer last used for ball hits.
+    Every frame equals the plain call's and the oracle's, and fewer bytes
+    than the frames hold cross to the host."""
+    vg, wl, hosts, trees, tex = setup
+    from voxvision_gb300.cameras import HostCamera
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, 1 << 30, 16, 4, 1, 1))
+    ids = [srv.add_tree(t) for t in trees]
+
+    def frame(w, h, az, el=20.0, away=False, dist=1.5):
+        cam = HostCamera(0)
+        cam.set_window_size(w, h)
+        pos = wl.pose_position((32.0,) * 3, dist * 64 * 3 ** 0.5, az, el)
+        cam.set_position(pos)
+        cam.look_at(tuple(2 * np.asarray(pos) - 32.0) if away else (32.0,) * 3)
+        return ("frame", 0, cam.gpu_struct(), w, h, cam.state())
+
+    c, r = wl.balls(100000, 0.0, 64.0, 0.5, 8.0, 91)      # 100000 hit bytes: the same 128 KiB class
+    seq = [frame(160, 120, 0.3), frame(160, 120, 2.1, 40.0), frame(160, 120, 4.0, 5.0, dist=0.9),
+           frame(160, 120, 1.0, away=True), frame(160, 120, 5.5), frame(176, 176, 0.8),
+           frame(160, 120, 3.3, 30.0), frame(160, 200, 2.6, 10.0), frame(160, 120, 0.1, 45.0),
+           frame(160, 200, 4.4), ("balls", 0, c, r), frame(160, 120, 1.7, 25.0), frame(160, 120, 1.7, 25.0)]
+    for q in seq:
+        t = srv.submit_frame(ids[0], q[2], q[3], q[4]) if q[0] == "frame" else srv.submit_balls(ids[0], q[2], q[3])
+        assert srv.wait(t, 60000) == 0
+        got, _ = srv.result(t)
+        srv.release(t)
+        assert np.array_equal(got, _alone(trees, tex, q)), q[0]
+        assert np.array_equal(got, _oracle(tex, q)), q[0]
+    st = srv.stats()
+    assert st["frame_bytes_full"] == sum(q[3] * q[4] * 4 for q in seq if q[0] == "frame")
+    assert 0 < st["frame_bytes_out"] < st["frame_bytes_full"]
+    srv.close()

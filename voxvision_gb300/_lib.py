@@ -91,7 +91,8 @@ class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "rejected", "launches", "bytes_in_use",
                                           "peak_bytes", "pending", "inflight", "host_bytes_in_use",
                                           "host_peak_bytes", "worker_busy_ns", "build_ns", "host_pin_ns",
-                                          "host_pins", "device_alloc_ns", "frame_bytes_out", "host_slabs")]
+                                          "host_pins", "device_alloc_ns", "frame_bytes_out", "host_slabs",
+                                          "frame_bytes_full")]
 
 
 _lib = None

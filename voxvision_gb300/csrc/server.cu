@@ -11,7 +11,10 @@
  * kernel of batch.cu), each ball request into the ball kernel.  Frames are
  * drawn into device memory and copied into the pinned host buffers the
  * clients read as soon as their launch's kernel ends (frame stores straight
- * into host memory slow the frame kernel by a third); ball hits, one byte a
+ * into host memory slow the frame kernel by a third).  A frame is zero
+ * outside its tree's screen rectangle, and a reused buffer is zero outside
+ * the rectangle of the frame it held last, so only the box covering both
+ * crosses to the host (about a sixth of the bytes on a mixed load).  Ball hits, one byte a
  * query, are written in place by the ball kernel, which also reads its staged
  * inputs from pinned memory.  The device budget holds the resident trees,
  * the per-launch job tables and the frames being drawn; the pinned-host
@@ -65,6 +68,65 @@ size_t pinned_class(size_t bytes)
     return cls;
 }
 
+// What a pinned buffer may still hold from its last use.  Every byte below
+// `tail` that lies outside rectangle [x0, x1) x [y0, y1) of a frame w pixels
+// wide (row pitch w * 4 bytes) is zero; bytes from `tail` on may hold
+// anything.  A buffer of unknown contents -- new, or last used for ball
+// results or by a request that failed -- has w = 0 and tail = 0.
+struct Dirty {
+    uint32_t w = 0, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+    size_t tail = 0;
+};
+
+// The part of a w x h frame to copy into a buffer whose state is `d`, given
+// that the device frame is zero outside rectangle r ({x0, y0, x1, y1} of
+// frame_rect_of: no pixel outside it sees the tree).  Either the whole frame
+// (`full`), or the box [x0, x1) x [y0, y1), which covers the frame's
+// rectangle and what the buffer's last frame left non-zero (same row pitch),
+// or nothing (both empty).  `after` is the buffer's state once it is copied.
+struct FrameCopy {
+    bool full = false;
+    uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+};
+
+FrameCopy plan_frame_copy(const Dirty &d, uint32_t w, uint32_t h, const uint32_t r[4], Dirty &after)
+{
+    const size_t fb = (size_t)w * h * 4;
+    const uint32_t rx1 = std::min(r[2], w), ry1 = std::min(r[3], h);
+    const bool have = rx1 > r[0] && ry1 > r[1];
+    const bool had = d.w != 0 && d.x1 > d.x0 && d.y1 > d.y0;
+    FrameCopy c;
+    if (d.w == w && d.tail >= fb) {
+        // below fb the buffer is zero outside d's rectangle, in this pitch
+        const uint32_t oy1 = std::min(d.y1, h);
+        const bool old_in = had && oy1 > d.y0;
+        if (have || old_in) {
+            c.x0 = have ? r[0] : d.x0;
+            c.y0 = have ? r[1] : d.y0;
+            c.x1 = have ? rx1 : d.x1;
+            c.y1 = have ? ry1 : oy1;
+            if (have && old_in) {
+                c.x0 = std::min(c.x0, d.x0);
+                c.y0 = std::min(c.y0, d.y0);
+                c.x1 = std::max(c.x1, d.x1);
+                c.y1 = std::max(c.y1, oy1);
+            }
+        }
+        // rows of the old rectangle below the frame lie past fb
+        after.tail = (had && d.y1 > h) ? fb : d.tail;
+    } else {
+        c.full = true;
+        const size_t old_end = had ? (size_t)d.y1 * d.w * 4 : 0;
+        after.tail = (d.tail <= fb || old_end > fb) ? fb : d.tail;
+    }
+    after.w = w;
+    after.x0 = have ? r[0] : 0;
+    after.y0 = have ? r[1] : 0;
+    after.x1 = have ? rx1 : 0;
+    after.y1 = have ? ry1 : 0;
+    return c;
+}
+
 // Pinned host buffers by power-of-two size class, reused across requests.
 // Buffers up to 64 MiB are carved from 128 MiB pinned slabs; a part of the
 // host budget is pinned in slabs when the server starts, and a refill thread
@@ -72,7 +134,8 @@ size_t pinned_class(size_t bytes)
 // thread -- which admits and launches every request -- does not stop for
 // page-locking (14 GB/s on the Grace host: 4.5 ms for one 64 MiB buffer).
 // Larger buffers are pinned one by one.  Buffers go back to their class's
-// free list and slabs stay pinned until the pool is destroyed.
+// free list with their Dirty state, and slabs stay pinned until the pool is
+// destroyed.
 class PinnedPool {
   public:
     static constexpr size_t SLAB = size_t(128) << 20, MAX_CARVED = size_t(64) << 20;
@@ -107,15 +170,18 @@ class PinnedPool {
         return true;
     }
 
-    void *get(size_t bytes, size_t *cls_out)
+    // A buffer of at least `bytes`; *dirty (may be NULL) gets what it holds.
+    void *get(size_t bytes, size_t *cls_out, Dirty *dirty = nullptr)
     {
         size_t cls = pinned_class(bytes);
         *cls_out = cls;
+        if (dirty) *dirty = Dirty{};
         {
             std::lock_guard<std::mutex> lk(mu_);
             auto &v = free_[cls];
             if (!v.empty()) {
-                void *p = v.back();
+                void *p = v.back().first;
+                if (dirty) *dirty = v.back().second;
                 v.pop_back();
                 return p;
             }
@@ -151,11 +217,11 @@ class PinnedPool {
         std::lock_guard<std::mutex> lk(mu_);
         return pinned_ / SLAB;
     }
-    void put(void *p, size_t cls)
+    void put(void *p, size_t cls, const Dirty &dirty = Dirty{})
     {
         if (!p) return;
         std::lock_guard<std::mutex> lk(mu_);
-        free_[cls].push_back(p);
+        free_[cls].push_back({p, dirty});
     }
 
   private:
@@ -179,7 +245,7 @@ class PinnedPool {
 
     std::mutex mu_;
     std::condition_variable cv_;
-    std::map<size_t, std::vector<void *>> free_;
+    std::map<size_t, std::vector<std::pair<void *, Dirty>>> free_;
     std::vector<void *> slabs_, spares_, direct_;
     char *cur_ = nullptr;
     size_t cur_used_ = SLAB;
@@ -202,6 +268,7 @@ struct Request {
     uint64_t host_bytes = 0;        // charged to the pinned-host budget while admitted
     void *h_res = nullptr;          // pinned result, written in place by the kernels
     size_t h_cls = 0, res_bytes = 0;
+    Dirty h_dirty;                  // what h_res holds: as taken from the pool, then after this frame's copy
     void *d_res = nullptr;          // a frame kept in device memory (frames_on_device)
     uint64_t dev_hold = 0;          // device bytes still charged after the launch ends (until release)
     void *h_in = nullptr;           // pinned ball inputs
@@ -255,7 +322,7 @@ struct vox_cuda_server {
     std::thread worker;
     cudaMemPool_t pool = nullptr;   // device frames and job tables (keeps its memory mapped)
     // worker time accounting (vox_cuda_server_stats)
-    std::atomic<uint64_t> busy_ns{0}, build_ns{0}, alloc_ns{0}, bytes_out{0};
+    std::atomic<uint64_t> busy_ns{0}, build_ns{0}, alloc_ns{0}, bytes_out{0}, bytes_full{0};
 };
 
 namespace {
@@ -373,7 +440,7 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
             }
             r->dev_hold = r->dev_bytes - 256;    // the frame; its job-table share goes with the launch
         } else {
-            r->h_res = s->pinned.get(out_bytes, &r->h_cls);
+            r->h_res = s->pinned.get(out_bytes, &r->h_cls, r->kind == FRAME ? &r->h_dirty : nullptr);
         }
         void *d_res = nullptr;
         if ((!on_device && !r->h_res) ||
@@ -426,12 +493,35 @@ Launch *build_launch(vox_cuda_server *s, const std::vector<Request *> &batch, cu
             uint32_t *counter = reinterpret_cast<uint32_t *>(static_cast<char *>(L->d_table) + tb);
             rc = enqueue_frame_jobs(jobs.data(), (uint32_t)jobs.size(), L->h_table, L->d_table, counter,
                                     s->nsm, st);
-            for (size_t q = 0; q < frames.size() && rc == VOX_CUDA_OK; q++) {  // results out after the kernel
-                if (frames[q]->d_res) continue;                                  // stays on the device
-                if (cudaMemcpyAsync(frames[q]->h_res, jobs[q].argb, frames[q]->res_bytes, cudaMemcpyDeviceToHost,
-                                    st) != cudaSuccess)
-                    rc = VOX_CUDA_ECUDA;
-                s->bytes_out.fetch_add(frames[q]->res_bytes, std::memory_order_relaxed);
+            // results out after the kernel: only what differs from what the
+            // pinned buffer already holds (the frame is zero outside its
+            // tree's screen rectangle, and so is the buffer outside the
+            // rectangle of the frame it held last)
+            for (size_t q = 0; q < frames.size() && rc == VOX_CUDA_OK; q++) {
+                Request *r = frames[q];
+                if (r->d_res) continue;                                          // stays on the device
+                uint32_t rect[4];
+                double centre[2];
+                frame_rect_of(s->trees[r->tree], r->cam, r->w, r->h, rect, centre);
+                Dirty after;
+                const FrameCopy c = plan_frame_copy(r->h_dirty, r->w, r->h, rect, after);
+                const size_t pitch = (size_t)r->w * 4;
+                size_t moved = 0;
+                cudaError_t e = cudaSuccess;
+                if (c.full) {
+                    moved = r->res_bytes;
+                    e = cudaMemcpyAsync(r->h_res, jobs[q].argb, moved, cudaMemcpyDeviceToHost, st);
+                } else if (c.x1 > c.x0 && c.y1 > c.y0) {
+                    const size_t at = (size_t)c.y0 * pitch + (size_t)c.x0 * 4;
+                    moved = (size_t)(c.x1 - c.x0) * 4 * (c.y1 - c.y0);
+                    e = cudaMemcpy2DAsync(static_cast<char *>(r->h_res) + at, pitch,
+                                          reinterpret_cast<const char *>(jobs[q].argb) + at, pitch,
+                                          (size_t)(c.x1 - c.x0) * 4, c.y1 - c.y0, cudaMemcpyDeviceToHost, st);
+                }
+                if (e != cudaSuccess) rc = VOX_CUDA_ECUDA;
+                r->h_dirty = after;
+                s->bytes_out.fetch_add(moved, std::memory_order_relaxed);
+                s->bytes_full.fetch_add(r->res_bytes, std::memory_order_relaxed);
             }
         }
         if (rc)
@@ -769,7 +859,8 @@ try {
     if (it == s->reqs.end()) return VOX_CUDA_EINVAL;
     Request *r = it->second;
     if (!r->done) return VOX_CUDA_EINVAL;
-    s->pinned.put(r->h_res, r->h_cls);
+    // a frame copied without error leaves its buffer in a known state
+    s->pinned.put(r->h_res, r->h_cls, r->status == VOX_CUDA_OK ? r->h_dirty : Dirty{});
     if (r->d_res) {   // its launch has ended: the frame is free on any stream
         cudaFreeAsync(r->d_res, s->streams[0]);
         s->used -= r->dev_hold;
@@ -808,6 +899,7 @@ try {
     st->device_alloc_ns = s->alloc_ns.load();
     st->frame_bytes_out = s->bytes_out.load();
     st->host_slabs = s->pinned.slabs();
+    st->frame_bytes_full = s->bytes_full.load();
     return VOX_CUDA_OK;
 } VOX_ABI_FAIL_INT
 
