@@ -500,8 +500,10 @@ int vox_cuda_server_wait(vox_cuda_server *srv, uint64_t ticket, uint32_t timeout
 /* A finished request's result (w*h ARGB pixels, or n hit bytes) in server
  * memory -- pinned host memory, or for frames of a server with
  * frames_on_device set, device memory of the server's device -- valid until
- * vox_cuda_server_release; times_ns (may be NULL) gets submission, launch
- * and completion times (steady clock, ns). */
+ * vox_cuda_server_release and read-only: the server reuses a host frame's
+ * buffer and copies into it only what differs from the frame it held last.
+ * times_ns (may be NULL) gets submission, launch and completion times
+ * (steady clock, ns). */
 int vox_cuda_server_result(vox_cuda_server *srv, uint64_t ticket, const void **data, size_t *bytes,
                            uint64_t *times_ns);
 int vox_cuda_server_release(vox_cuda_server *srv, uint64_t ticket);
