@@ -84,6 +84,8 @@ def parse_args():
     p.add_argument("--reps", type=int, default=5, help="timed repetitions of --tree-build")
     p.add_argument("--quality", type=int, default=0, metavar="N",
                    help="only time every vox_render quality on N orbit frames (profiling runs)")
+    p.add_argument("--batched", action="store_true",
+                   help="only time the 64-frame mixed-camera batch against plain launches (profiling runs)")
     return p.parse_args()
 
 
@@ -1070,6 +1072,15 @@ def main():
         q = measure_quality(torch, vg, dt, ht.ptr, orbit_states(), tex, torch.from_numpy(tex).cuda(), flush,
                             cpu=not args.no_cpu_baseline, nframes=args.quality)
         print(json.dumps({"quality": q}), flush=True)
+        return
+    if args.batched:
+        import torch
+
+        import voxvision_gb300 as vg
+        vg.set_voxel_size((1, 1, 1))
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        tex = workloads().texture32(7)
+        print(json.dumps({"batched": measure_batched(torch, vg, flush, torch.from_numpy(tex).cuda())}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)
