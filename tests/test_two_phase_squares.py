@@ -1,9 +1,10 @@
 """The decomposition behind the GPU's FAST and ADAPTIVE frames
-(root_hits_kernel, then render_squares_kernel), checked on the CPU with the
-oracle's own search: every pixel's search from the root made first, then each
-square's sequence of renderer.c:215-318, making only the searches from a leaf
-and taking a pixel's root result wherever the reference searches from the
-root, gives the oracle's sequential frame pixel for pixel -- for random
+(render_squares_kernel), checked on the CPU with the oracle's own search:
+every pixel's search from the root made first; then, per 4x4 square, rounds
+in which every pixel still to be walked makes the search from the leaf the
+walk holds, followed by renderer.c:215-318's walk over those results, which
+ends the round wherever it moves to a leaf the round did not search from.
+This gives the oracle's sequential frame pixel for pixel -- for random
 cameras of both classes, every quality, and a non-unit voxel size.  No GPU
 is used."""
 import numpy as np
@@ -38,6 +39,7 @@ def two_phase(tree, state, w, h, quality, tex, voxel):
     leaf, _, pts, _ = tree.rays(np.tile(origin, (w * h, 1)), dirs.reshape(-1, 3), nthreads=1)
     leaf, pts = leaf.reshape(h, w), pts.reshape(h, w, 3)
     out = np.zeros((h, w), np.uint32)
+    rounds = 0
     rnd, merge_mode = quality & 3, quality & 12
     for ys in range(0, h, 4):
         for xs in range(0, w, 4):
@@ -64,27 +66,48 @@ def two_phase(tree, state, w, h, quality, tex, voxel):
                             merge = True if (mode == 1 and merge_mode == 8) else merge
                         else:
                             merge = False
-            prev = 0
-            for i in range(istart, iend):                        # renderer.c:286-315
-                p = ORDER[i]
-                py, px = ys + p // 4, xs + p % 4
-                m = merge and (i & 1)
-                if not m:
-                    from_root = True
-                    if mode == 1 and have:                      # phase 2: the search from the leaf
-                        lf, _, lp, _ = tree.rays(origin[None], dirs[py, px][None], root=int(pre[leaf_id]),
-                                                 nthreads=1)
-                        if lf[0] != MISS:
-                            leaf_id, inter, from_root = int(lf[0]), lp[0], False
-                    if from_root:                               # ... else the pixel's root result
-                        have = leaf[py, px] != MISS
-                        if have:
-                            leaf_id, inter = int(leaf[py, px]), pts[py, px]
-                if have:
-                    sq[p] = sq[prev] if m else _color(inter, tex, voxel)
-                prev = p
+            # the walk in rounds: searches from one leaf for every pixel still
+            # to come, then the reference's decisions over them
+            res = {}                                            # pixel -> (have, point, merged)
+            pos = istart
+            while pos < iend:
+                searched, frm = mode == 1 and have, leaf_id
+                found = {}
+                if searched:
+                    for i in range(pos, iend):
+                        if merge and (i & 1):
+                            continue
+                        p = ORDER[i]
+                        py, px = ys + p // 4, xs + p % 4
+                        lf, _, lp, _ = tree.rays(origin[None], dirs[py, px][None], root=int(pre[frm]), nthreads=1)
+                        found[p] = (lf[0] != MISS, lp[0], int(lf[0]))
+                stop = iend
+                i = pos
+                while i < stop:
+                    p = ORDER[i]
+                    py, px = ys + p // 4, xs + p % 4
+                    m = merge and (i & 1)
+                    if not m:
+                        from_root = True
+                        if mode == 1 and have and found[p][0]:   # the search from the leaf met a voxel
+                            inter, leaf_id, from_root = found[p][1], found[p][2], False
+                        if from_root:                           # ... else the pixel's root result
+                            have = leaf[py, px] != MISS
+                            if have:
+                                inter = pts[py, px]
+                                if mode == 1 and not (searched and int(leaf[py, px]) == frm):
+                                    stop = i + 1                # later pixels search from another leaf
+                                leaf_id = int(leaf[py, px])
+                    res[p] = (have, inter, m)
+                    i += 1
+                rounds += 1
+                pos = stop
+            colour = {p: _color(v[1], tex, voxel) for p, v in res.items() if v[0] and not v[2]}
+            for p, (hv, _, m) in res.items():
+                if hv:
+                    sq[p] = sq[ORDER[ORDER.index(p) - 1]] if m else colour[p]
             out[ys:ys + 4, xs:xs + 4] = sq.reshape(4, 4)
-    return out
+    return out, rounds
 
 
 @pytest.fixture(scope="module")
@@ -115,7 +138,7 @@ def test_two_phase_frames_equal_the_sequential_loop(scene, voxel):
             frames = {}
             for q in (0, 1, 2, 2 | 4, 2 | 8):
                 ref, _ = orc.render_quality(tree.ptr, st, w, h, q, tex, nthreads=1)
-                got = two_phase(tree, st, w, h, q, tex, voxel)
+                got, _ = two_phase(tree, st, w, h, q, tex, voxel)
                 assert np.array_equal(got, ref), (k, q)
                 checked += int((ref != 0).sum())
                 frames[q] = ref

@@ -139,6 +139,30 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// A clearing block of a frame launch (block index ntiles and up): the frame
+// outside the traced rectangle, rows dealt to the block's warps; a warp's
+// lanes store 16 bytes each when the frame is 16-byte aligned (row starts and
+// x0, x1 then are: w is a multiple of 16, x0 and x1 of 8).
+__device__ __forceinline__ void clear_outside(const FramePlan &p, uint32_t w, uint32_t h, uint32_t *argb,
+                                              uint32_t warp, uint32_t lane)
+{
+    const bool vec = (reinterpret_cast<uintptr_t>(argb) & 15u) == 0;
+    const uint32_t nw = (gridDim.x - p.ntiles) * 4u;
+    for (uint32_t y = (blockIdx.x - p.ntiles) * 4u + warp; y < h; y += nw) {
+        uint32_t *row = argb + (size_t)y * w;
+        uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
+        if (y >= p.y0 && y < p.y1) { b0 = p.x0; a1 = p.x1; b1 = w; }
+        if (vec) {
+            uint4 *r4 = reinterpret_cast<uint4 *>(row);
+            for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+            for (uint32_t i = a1 / 4 + lane; i < b1 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
+        } else {
+            for (uint32_t i = a0 + lane; i < b0; i += 32) row[i] = 0u;
+            for (uint32_t i = a1 + lane; i < b1; i += 32) row[i] = 0u;
+        }
+    }
+}
+
 template <int CAP, bool COUNT, int MINB, bool LIT>
 __global__ void __launch_bounds__(128, MINB) render_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
                                                      FramePlan p, const uint8_t *__restrict__ tex,
@@ -149,26 +173,8 @@ __global__ void __launch_bounds__(128, MINB) render_kernel(DevTree t, vox_cuda_c
     pdl_launch_dependents();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (blockIdx.x >= p.ntiles) {
-        // clearing blocks: rows dealt to their warps; a warp's lanes store 16
-        // bytes each when the frame is 16-byte aligned (row starts and x0, x1
-        // then are: w is a multiple of 16, x0 and x1 of 8)
         pdl_wait();
-        if (COUNT) return;
-        const bool vec = (reinterpret_cast<uintptr_t>(argb) & 15u) == 0;
-        const uint32_t nw = (gridDim.x - p.ntiles) * 4u;
-        for (uint32_t y = (blockIdx.x - p.ntiles) * 4u + warp; y < h; y += nw) {
-            uint32_t *row = argb + (size_t)y * w;
-            uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
-            if (y >= p.y0 && y < p.y1) { b0 = p.x0; a1 = p.x1; b1 = w; }
-            if (vec) {
-                uint4 *r4 = reinterpret_cast<uint4 *>(row);
-                for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
-                for (uint32_t i = a1 / 4 + lane; i < b1 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
-            } else {
-                for (uint32_t i = a0 + lane; i < b0; i += 32) row[i] = 0u;
-                for (uint32_t i = a1 + lane; i < b1; i += 32) row[i] = 0u;
-            }
-        }
+        if (!COUNT) clear_outside(p, w, h, argb, warp, lane);
         return;
     }
     uint32_t by = centre_out(blockIdx.x / p.ntx, p.cty, p.nty);
@@ -223,150 +229,174 @@ __device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const floa
     }
 }
 
-// FAST and ADAPTIVE frames in two launches.  In renderer.c a pixel's leaf is
-// either the previous pixel's leaf, when the ray meets a voxel there (the
-// search from the leaf, :297), or what the search from the root finds for
-// the pixel's own ray (:299, and every corner and BEST pixel); the second
-// never depends on the square's earlier pixels.  So the first launch makes
-// the root search of every pixel at once, one thread a pixel like the BEST
-// kernel (warps of 8x4 pixels), and the second walks each square's 16 pixels
-// in the reference's order and decisions, one thread a square, with only the
-// searches from a leaf (one leaf's voxels) left to make; wherever the
-// reference searches from the root it takes the pixel's result of the first
-// launch.  The results are the reference's by construction: the same
-// searches of the same rays, the same choices between them.
-
-// Root search of every pixel of the rectangle [x0, x1) x [y0, y1) (the
-// rectangle of frame_rect, whole 4x4 squares; every pixel outside it misses
-// the tree's box): {leaf record or VOXP_EMPTY, intersection point}, stored
-// row by row of the rectangle.
-template <int CAP, bool RAYS>
-__global__ void __launch_bounds__(128) root_hits_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
-                                                        uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
-                                                        const float *__restrict__ rays, uint4 *__restrict__ hits,
-                                                        uint32_t *__restrict__ status)
-{
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t px = x0 + blockIdx.x * TILE_W + (warp & 1) * 8 + (lane & 7);
-    uint32_t py = y0 + blockIdx.y * TILE_H + (warp >> 1) * 4 + (lane >> 3);
-    if (px >= x1 || py >= y1) return;
-    uint4 res = make_uint4(VOXP_EMPTY, 0u, 0u, 0u);
-    if (t.root != VOXP_EMPTY) {
-        float dx, dy, dz;
-        pixel_dir<RAYS>(cam, rays, w, (int)px, (int)py, dx, dy, dz);
-        Counts c{0, 0, 0};
-        RayHit hh;
-        bool overflow = false;
-        if (vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1], cam.position[2], dx, dy, dz,
-                                       hh, c, overflow))
-            res = make_uint4(hh.rec, __float_as_uint(hh.x), __float_as_uint(hh.y), __float_as_uint(hh.z));
-        if (overflow) atomicOr(status, 1u);
-    }
-    hits[(size_t)(py - y0) * (x1 - x0) + (px - x0)] = res;
-}
-
-// renderer.c:215-318 per 4x4 square of the rectangle [x0, x1) x [y0, y1)
-// over the root searches of root_hits_kernel (the squares outside it draw
-// nothing: every search of theirs misses).
+// FAST and ADAPTIVE frames, and with a ray buffer frames of every quality,
+// in one launch.  In renderer.c a pixel's leaf is either the previous
+// pixel's leaf, when the ray meets a voxel there (the search from the leaf,
+// :297), or what the search from the root finds for the pixel's own ray
+// (:299, and every corner and BEST pixel); the second never depends on the
+// square's earlier pixels.  So each half-warp holds one 4x4 square, a pixel
+// a lane (a warp is two squares side by side, 8x4 pixels, the BEST kernel's
+// warp tile): every lane first makes the root search of its own ray, then
+// the lanes still to be drawn make, at once, the search from the leaf the
+// square's walk currently holds.  The walk itself -- the reference's 16
+// pixels in its order, with its choices of mode, merging and leaf -- runs on
+// every lane of the square alike over those results (shuffled from the
+// pixel's lane), and wherever it changes to a leaf the round's searches were
+// not made from, a new round makes them for the pixels after it.  A square
+// takes one round per change of leaf, and the leaf rarely changes within a
+// square.  The results are the reference's by construction: the same
+// searches of the same rays, the same choices between them; searches made
+// for pixels the walk then reaches another way are dropped.
 template <int CAP, bool RAYS>
 __global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
-                                                             uint32_t h, unsigned int quality,
+                                                             uint32_t h, FramePlan fp, unsigned int quality,
                                                              const uint8_t *__restrict__ tex,
                                                              uint32_t *__restrict__ argb,
                                                              uint32_t *__restrict__ status, vox::DevLights lights,
-                                                             const float *__restrict__ rays,
-                                                             const uint4 *__restrict__ hits, uint32_t x0,
-                                                             uint32_t y0, uint32_t x1, uint32_t y1)
+                                                             const float *__restrict__ rays)
 {
-    // renderer.c:23-25 rendering order {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}, a nibble each
+    // renderer.c:23-25 rendering order {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}, a nibble
+    // each; the permutation is its own inverse, so it also maps a pixel to its place in the order
     constexpr uint64_t ORDER = 0xFEBADC9876325410ull;
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t sx = (x0 >> 2) + blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);     // square coordinates
-    uint32_t sy = (y0 >> 2) + blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
-    if (sx >= (x1 >> 2) || sy >= (y1 >> 2)) return;
-    const uint32_t rw = x1 - x0;                                      // row length of the root searches
-    const int xstart = (int)sx * 4, ystart = (int)sy * 4;
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    pdl_launch_dependents();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, p = lane & 15;
+    if (blockIdx.x >= fp.ntiles) {                  // the frame outside the rectangle: misses
+        pdl_wait();
+        clear_outside(fp, w, h, argb, warp, lane);
+        return;
+    }
+    if (RAYS) pdl_wait();                           // the ray buffer is stream-ordered memory
+    const int ip = (int)((ORDER >> (4 * p)) & 15u);                        // this pixel's place in the order
+    const uint32_t by = centre_out(blockIdx.x / fp.ntx, fp.cty, fp.nty);
+    const uint32_t bx = centre_out(blockIdx.x % fp.ntx, fp.ctx, fp.ntx);
+    const uint32_t xstart = fp.x0 + bx * TILE_W + (warp & 1) * 8 + (lane >> 4) * 4;
+    const uint32_t ystart = fp.y0 + by * TILE_H + (warp >> 1) * 4;
+    const bool valid = xstart < fp.x1 && ystart < fp.y1;                    // whole squares: all 16 lanes alike
+    const int px = (int)xstart + (p & 3), py = (int)ystart + (p >> 2);
     const float ox = cam.position[0], oy = cam.position[1], oz = cam.position[2];
     const int rnd_mode = quality & VOX_CUDA_QUALITY_MODE_MASK;
     const int merge_mode = quality & VOX_CUDA_QUALITY_RM_MASK;
-    const uint4 *sq = hits + (size_t)(ystart - (int)y0) * rw + (xstart - (int)x0);   // the square's root searches
-    uint32_t out[16];
-#pragma unroll
-    for (int i = 0; i < 16; i++) out[i] = 0u;
     Counts c{0, 0, 0};
     bool overflow = false;
-    bool have_leaf = false;      // `leaf != NULL` of renderer.c
-    uint32_t leaf_rec = 0;
-    float ix = 0.f, iy = 0.f, iz = 0.f;       // inter1
-    int block_mode = rnd_mode;
-    int istart = 0, iend = 16;
-    bool block_merge = false;
 
-    if (block_mode == VOX_CUDA_QUALITY_ADAPTIVE) {              // renderer.c:240-282
-        block_merge = (merge_mode == VOX_CUDA_QUALITY_RAY_MERGE);
+    // the root search of this pixel's ray
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    uint32_t rrec = VOXP_EMPTY;
+    float rx = 0.f, ry = 0.f, rz = 0.f;
+    if (valid) {
+        pixel_dir<RAYS>(cam, rays, w, px, py, dx, dy, dz);
+        RayHit hh;
+        if (t.root != VOXP_EMPTY && vox::trace_ray<CAP, false>(t, t.root, ox, oy, oz, dx, dy, dz, hh, c, overflow)) {
+            rrec = hh.rec;
+            rx = hh.x; ry = hh.y; rz = hh.z;
+        }
+    }
+
+    // the square's mode (renderer.c:240-282), alike on its 16 lanes
+    int mode = rnd_mode, istart = 0, iend = 16;
+    bool bmerge = false, have = false;       // `leaf != NULL` of renderer.c
+    uint32_t leaf = VOXP_EMPTY;
+    const uint32_t c1 = __shfl_sync(FULL, rrec, 0, 16), c2 = __shfl_sync(FULL, rrec, 15, 16);
+    const float ix = __shfl_sync(FULL, rx, 0, 16), iy = __shfl_sync(FULL, ry, 0, 16), iz = __shfl_sync(FULL, rz, 0, 16);
+    const float jx = __shfl_sync(FULL, rx, 15, 16), jy = __shfl_sync(FULL, ry, 15, 16), jz = __shfl_sync(FULL, rz, 15, 16);
+    const float d1x = __shfl_sync(FULL, dx, 0, 16), d1y = __shfl_sync(FULL, dy, 0, 16), d1z = __shfl_sync(FULL, dz, 0, 16);
+    const float d2x = __shfl_sync(FULL, dx, 15, 16), d2y = __shfl_sync(FULL, dy, 15, 16), d2z = __shfl_sync(FULL, dz, 15, 16);
+    bool res_have = false, res_merge = false;    // this pixel: drawn from a hit / copied from the previous pixel
+    float qx = rx, qy = ry, qz = rz;              // and its intersection point
+    if (rnd_mode == VOX_CUDA_QUALITY_ADAPTIVE) {
+        bmerge = (merge_mode == VOX_CUDA_QUALITY_RAY_MERGE);
         istart = 1;
-        const uint4 h1 = sq[0];
-        block_mode = VOX_CUDA_QUALITY_FAST;
-        have_leaf = h1.x != VOXP_EMPTY;
-        if (have_leaf) {
-            leaf_rec = h1.x;
-            ix = __uint_as_float(h1.y); iy = __uint_as_float(h1.z); iz = __uint_as_float(h1.w);
+        mode = VOX_CUDA_QUALITY_FAST;
+        have = c1 != VOXP_EMPTY;
+        leaf = c1;
+        if (p == 0) res_have = have;                                        // corner 1, drawn now
+        if (have) {
             iend = 15;
-            out[0] = vox::hit_color(tex, t, lights, ix, iy, iz, overflow);
-            const uint4 h2 = sq[3 * (size_t)rw + 3];
-            if (h2.x != VOXP_EMPTY) {
-                const float jx = __uint_as_float(h2.y), jy = __uint_as_float(h2.z), jz = __uint_as_float(h2.w);
-                out[15] = vox::hit_color(tex, t, lights, jx, jy, jz, overflow);
-                float d1x, d1y, d1z, d2x, d2y, d2z;
-                pixel_dir<RAYS>(cam, rays, w, xstart, ystart, d1x, d1y, d1z);
-                pixel_dir<RAYS>(cam, rays, w, xstart + 3, ystart + 3, d2x, d2y, d2z);
+            if (c2 != VOXP_EMPTY) {
+                if (p == 15) res_have = true;                               // corner 2, drawn now
                 float d1 = sqr3(ix, iy, iz, ox, oy, oz);
                 float d2 = sqr3(d1x, d1y, d1z, 0.f, 0.f, 0.f);
                 float criteria = __fmul_rn(__fdiv_rn(d1, d2), sqr3(d1x, d1y, d1z, d2x, d2y, d2z));
                 float dist = sqr3(ix, iy, iz, jx, jy, jz);
-                if ((double)__fdiv_rn(dist, criteria) > 1.69)          // LENGTH_THRESHOLD, renderer.c:197
-                    block_mode = VOX_CUDA_QUALITY_BEST;
-                if (d1 > 22500.0f)                                       // MAX_DIST^2, renderer.c:198
-                    block_merge = (block_mode == VOX_CUDA_QUALITY_FAST &&
-                                   merge_mode == VOX_CUDA_QUALITY_RAY_MERGE_ACCURATE) ? true : block_merge;
+                if ((double)__fdiv_rn(dist, criteria) > 1.69)               // LENGTH_THRESHOLD, renderer.c:197
+                    mode = VOX_CUDA_QUALITY_BEST;
+                if (d1 > 22500.0f)                                          // MAX_DIST^2, renderer.c:198
+                    bmerge = (mode == VOX_CUDA_QUALITY_FAST && merge_mode == VOX_CUDA_QUALITY_RAY_MERGE_ACCURATE)
+                                 ? true : bmerge;
                 else
-                    block_merge = false;
+                    bmerge = false;
             }
         }
     }
 
-    int prev_p = 0;
-    for (int i = istart; i < iend; i++) {                       // renderer.c:286-315
-        const int p = (int)((ORDER >> (4 * i)) & 15u);
-        const int py = p >> 2, px = p & 3;
-        const bool merge = block_merge && (i & 1);
-        if (!merge) {
-            bool from_root = true;
-            if (block_mode == VOX_CUDA_QUALITY_FAST && have_leaf) {
-                float dx, dy, dz;
-                pixel_dir<RAYS>(cam, rays, w, px + xstart, py + ystart, dx, dy, dz);
-                RayHit hh;
-                if (vox::trace_ray<CAP, false>(t, leaf_rec, ox, oy, oz, dx, dy, dz, hh, c, overflow)) {
-                    leaf_rec = hh.rec;
-                    ix = hh.x; iy = hh.y; iz = hh.z;
-                    from_root = false;
-                }
-            }
-            if (from_root) {
-                const uint4 hr = sq[(size_t)py * rw + px];
-                have_leaf = hr.x != VOXP_EMPTY;
-                if (have_leaf) {
-                    leaf_rec = hr.x;
-                    ix = __uint_as_float(hr.y); iy = __uint_as_float(hr.z); iz = __uint_as_float(hr.w);
-                }
+    // the walk (renderer.c:286-315) in rounds of searches from one leaf.  The
+    // walk's decisions need, per pixel, only whether its search from the
+    // round's leaf met a voxel, whether its root search did, and whether that
+    // found the round's leaf: three ballots a round, after which every lane
+    // of the square walks the same 16-bit masks; a pixel's point is its own
+    // lane's (from the leaf or from the root, as the walk decides).
+    const int seg = lane & 16;                    // first lane of this square
+    const unsigned nonempty = (__ballot_sync(FULL, rrec != VOXP_EMPTY) >> seg) & 0xFFFFu;
+    bool from_leaf = false;                       // this pixel's point is its search from the leaf
+    int pos = istart;                             // the next place in the order still to be walked
+    for (;;) {
+        const bool pending = valid && pos < iend;
+        if (!__any_sync(FULL, pending)) break;
+        const bool searched = mode == VOX_CUDA_QUALITY_FAST && have;      // this round's searches are from `leaf`
+        bool shit = false;
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        if (pending && searched && ip >= pos && ip < iend && !(bmerge && (ip & 1))) {
+            RayHit hh;
+            if (vox::trace_ray<CAP, false>(t, leaf, ox, oy, oz, dx, dy, dz, hh, c, overflow)) {
+                shit = true;
+                sx = hh.x; sy = hh.y; sz = hh.z;
             }
         }
-        if (have_leaf) out[p] = merge ? out[prev_p] : vox::hit_color(tex, t, lights, ix, iy, iz, overflow);
-        prev_p = p;
+        const unsigned hits = (__ballot_sync(FULL, shit) >> seg) & 0xFFFFu;
+        const unsigned same = (__ballot_sync(FULL, rrec == leaf) >> seg) & 0xFFFFu;
+        int stop = iend, next = -1;                 // where the round ends, and the pixel whose leaf comes next
+        for (int i = pos; pending && i < stop; i++) {
+            const int pi = (int)((ORDER >> (4 * i)) & 15u);
+            const unsigned bit = 1u << pi;
+            const bool merge = bmerge && (i & 1);
+            bool leafed = false;
+            if (!merge) {
+                if (mode == VOX_CUDA_QUALITY_FAST && have && (hits & bit)) {   // the search from the leaf met a voxel
+                    leafed = true;
+                } else {                                                       // ... else the pixel's root result
+                    have = (nonempty & bit) != 0;
+                    // later pixels search from this leaf: if this round searched from another, a new round
+                    if (have && mode == VOX_CUDA_QUALITY_FAST && !(searched && (same & bit))) {
+                        stop = i + 1;
+                        next = pi;
+                    }
+                }
+            }
+            if (p == pi) {
+                res_have = have;
+                res_merge = merge;
+                from_leaf = leafed;
+            }
+        }
+        if (from_leaf && ip >= pos && ip < stop) {
+            qx = sx; qy = sy; qz = sz;
+        }
+        // the leaf the walk holds now: unchanged, or the root result of pixel `next`
+        const uint32_t nl = __shfl_sync(FULL, rrec, next < 0 ? 0 : next, 16);
+        if (next >= 0) leaf = nl;
+        pos = stop;
     }
-#pragma unroll
-    for (int i = 0; i < 16; i++)
-        argb[(size_t)(ystart + (i >> 2)) * w + xstart + (i & 3)] = out[i];
+
+    // colours: a merged pixel takes the previous pixel's (renderer.c:309);
+    // the texture, the lights and the frame are stream-ordered memory
+    pdl_wait();
+    uint32_t color = 0u;
+    if (valid && res_have && !res_merge) color = vox::hit_color(tex, t, lights, qx, qy, qz, overflow);
+    const int prev = ip > 0 ? (int)((ORDER >> (4 * (ip - 1))) & 15u) : 0;
+    const uint32_t pcol = __shfl_sync(FULL, color, prev, 16);
+    if (res_merge) color = res_have ? pcol : 0u;
+    if (valid) argb[(size_t)py * w + px] = color;
     if (overflow) atomicOr(status, 1u);
 }
 
@@ -476,60 +506,56 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
     return cudaGetLastError();
 }
 
-// FAST / ADAPTIVE frames, and with a ray buffer frames of every quality: the
-// root searches of every pixel, then the squares.
+// FAST / ADAPTIVE frames, and with a ray buffer frames of every quality: one
+// launch over the squares of the rectangle where rays can meet the tree,
+// with blocks that clear the rest of the frame.
 cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s,
                                   const vox::DevLights *lights = nullptr, const float *rays = nullptr)
 {
     vox::DevLights L{};
     if (lights) L = *lights;
-    // the rectangle where rays can meet the tree's box (a camera class the
-    // device does not know: the whole frame)
-    uint32_t x0 = 0, y0 = 0, x1 = w, y1 = h;
+    // the rectangle where rays can meet the tree's box, whole 4x4 squares,
+    // and clearing blocks for the rest of the frame (a camera class the
+    // device does not know, whose rays come in a buffer: the whole frame)
+    FramePlan p;
     if (!rays) {
-        FramePlan p;
         plan_frame(t, cam, w, h, g_render_cull.load() != 0, p);
-        x0 = p.x0; y0 = p.y0; x1 = p.x1; y1 = p.y1;
+    } else {
+        p.x0 = p.y0 = 0;
+        p.x1 = w;
+        p.y1 = h;
+        p.ntx = (w + TILE_W - 1) / TILE_W;
+        p.nty = (h + TILE_H - 1) / TILE_H;
+        p.ctx = p.ntx / 2;
+        p.cty = p.nty / 2;
+        p.ntiles = p.ntx * p.nty;
+        p.nclear = 0;
     }
-    // pixels outside the rectangle are misses: the frame is cleared first and
-    // only the rectangle's squares are drawn
-    cudaError_t e = cudaSuccess;
-    if (x0 != 0 || y0 != 0 || x1 != w || y1 != h) {
-        e = cudaMemsetAsync(argb, 0, (size_t)w * h * 4, s);
-        if (e != cudaSuccess || x1 <= x0 || y1 <= y0) return e;
-    }
-    const uint32_t rw = x1 - x0, rh = y1 - y0;
-    uint4 *hits = nullptr;
-    e = cudaMallocAsync(&hits, (size_t)rw * rh * sizeof(uint4), s);
-    if (e != cudaSuccess) return e;
     const int cap = t->cap_class;
-    void (*roots)(DevTree, vox_cuda_camera, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
-                  const float *, uint4 *, uint32_t *);
-    void (*squares)(DevTree, vox_cuda_camera, uint32_t, uint32_t, unsigned int, const uint8_t *, uint32_t *,
-                    uint32_t *, vox::DevLights, const float *, const uint4 *, uint32_t, uint32_t, uint32_t,
-                    uint32_t);
-    if (rays) {
-        roots = cap == 0 ? root_hits_kernel<CAP0, true> : cap == 1 ? root_hits_kernel<CAP1, true>
-                                                                   : root_hits_kernel<CAP2, true>;
+    void (*squares)(DevTree, vox_cuda_camera, uint32_t, uint32_t, FramePlan, unsigned int, const uint8_t *,
+                    uint32_t *, uint32_t *, vox::DevLights, const float *);
+    if (rays)
         squares = cap == 0 ? render_squares_kernel<CAP0, true>
                 : cap == 1 ? render_squares_kernel<CAP1, true> : render_squares_kernel<CAP2, true>;
-    } else {
-        roots = cap == 0 ? root_hits_kernel<CAP0, false> : cap == 1 ? root_hits_kernel<CAP1, false>
-                                                                    : root_hits_kernel<CAP2, false>;
+    else
         squares = cap == 0 ? render_squares_kernel<CAP0, false>
                 : cap == 1 ? render_squares_kernel<CAP1, false> : render_squares_kernel<CAP2, false>;
-    }
-    roots<<<dim3((rw + TILE_W - 1) / TILE_W, (rh + TILE_H - 1) / TILE_H), 128, 0, s>>>(
-        t->dev, cam, w, h, x0, y0, x1, y1, rays, hits, t->d_status);
+    // overlapping the previous kernel of the stream, as the BEST frames do
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(p.ntiles + p.nclear);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = g_render_overlap.load() ? 1 : 0;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, squares, t->dev, cam, w, h, p, quality, tex, argb, t->d_status, L, rays);
     count_launch();
-    const uint32_t ws = rw / 4, hs = rh / 4;
-    squares<<<dim3((ws + 15) / 16, (hs + 7) / 8), 128, 0, s>>>(t->dev, cam, w, h, quality, tex, argb, t->d_status,
-                                                               L, rays, hits, x0, y0, x1, y1);
-    count_launch();
-    e = cudaGetLastError();
-    cudaFreeAsync(hits, s);
-    return e;
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
 }
 
 
