@@ -247,8 +247,18 @@ __device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const floa
 // square.  The results are the reference's by construction: the same
 // searches of the same rays, the same choices between them; searches made
 // for pixels the walk then reaches another way are dropped.
+// Register bound of render_squares_kernel: none by default (72 registers, 7
+// blocks of 128 threads per SM).  Bounds of 8 and 9 blocks (64 and 56
+// registers, with spills) drew the 1080p orbit's FAST and ADAPTIVE frames 1-3%
+// slower.
+#ifdef SQUARES_MIN_BLOCKS
+#define SQUARES_BOUNDS __launch_bounds__(128, SQUARES_MIN_BLOCKS)
+#else
+#define SQUARES_BOUNDS __launch_bounds__(128)
+#endif
+
 template <int CAP, bool RAYS>
-__global__ void __launch_bounds__(128) render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
+__global__ void SQUARES_BOUNDS render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
                                                              uint32_t h, FramePlan fp, unsigned int quality,
                                                              const uint8_t *__restrict__ tex,
                                                              uint32_t *__restrict__ argb,
