@@ -572,10 +572,10 @@ def measure_served(vg, trees, tex, rates=(1000, 2000, 5000, 10000, 15000, 20000)
     import ctypes as C
     from voxvision_gb300 import workloads as wl
     from voxvision_gb300.cameras import HostCamera
-    # 256 requests admitted at once (a few milliseconds of GPU work; more would
-    # only hold more result memory), up to 32 per launch, 16 launches in
-    # flight on 8 streams (the best of the configurations tried on the box)
-    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 24 << 30, 256, 32, 8, 16, 1 if frames_on_device else 0))
+    # the server's default configuration: 256 requests admitted at once (a few
+    # milliseconds of GPU work), up to 32 per launch, 32 launches in flight on
+    # 16 streams
+    srv = vg.Server(tex, vg.ServerConfig(40 << 30, 24 << 30, 256, 32, 16, 32, 1 if frames_on_device else 0))
     ids = [srv.add_tree(t[2]) for t in trees]
     rng = np.random.default_rng(seed)
     ball_pool = []

@@ -478,8 +478,8 @@ typedef struct {
 
 typedef struct vox_cuda_server vox_cuda_server;
 
-/* config NULL = 40 GiB device budget, 16 GiB pinned host budget, 1024 in
- * flight, 256 per launch, 4 streams, 8 launches in flight, frames copied to
+/* config NULL = 40 GiB device budget, 16 GiB pinned host budget, 256 in
+ * flight, 32 per launch, 16 streams, 32 launches in flight, frames copied to
  * host memory.  texture: host 32^3 bytes used for every frame.  Half the
  * pinned-host budget (at most 8 GiB) is page-locked here, in 128 MiB slabs
  * that results are carved from (about 0.6 s for 8 GiB); a thread of the

@@ -85,7 +85,8 @@ def test_served_mixed_load_equals_oracle(mixed, on_device):
     and every ball answer equals the oracle's."""
     vg, jobs, oracle_cams, otrees, tex_h, devs, sides = mixed
     from voxvision_gb300 import workloads as wl
-    srv = vg.Server(tex_h, vg.ServerConfig(40 << 30, 8 << 30, 256, 32, 8, 16, 1 if on_device else 0))
+    # the server's default shape: 256 admitted, 32 a launch, 16 streams, 32 launches in flight
+    srv = vg.Server(tex_h, vg.ServerConfig(40 << 30, 8 << 30, 256, 32, 16, 32, 1 if on_device else 0))
     ids = [srv.add_tree(d) for d in devs]
     tree_of_job = [ti for ti, _ in oracle_cams]
     reqs = []

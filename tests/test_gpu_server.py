@@ -337,3 +337,25 @@ def test_reused_result_buffers_hold_exact_frames(setup):
     assert st["frame_bytes_full"] == sum(q[3] * q[4] * 4 for q in seq if q[0] == "frame")
     assert 0 < st["frame_bytes_out"] < st["frame_bytes_full"]
     srv.close()
+
+
+def test_default_configuration_serves(setup):
+    """A server created with no configuration (the defaults: 40 GiB device
+    and 16 GiB pinned-host budgets, half of the latter pinned at creation in
+    128 MiB slabs, 16 streams, 32 launches in flight) serves a frame and a
+    ball batch exactly."""
+    vg, wl, hosts, trees, tex = setup
+    srv = vg.Server(tex)
+    ids = [srv.add_tree(t) for t in trees]
+    req = _frame_request(wl, az=1.1)
+    c, r = wl.balls(3000, 0.0, 64.0, 0.5, 8.0, 31)
+    t1 = srv.submit_frame(ids[0], req[2], req[3], req[4])
+    t2 = srv.submit_balls(ids[0], c, r)
+    assert srv.wait(t1) == 0 and srv.wait(t2) == 0
+    assert np.array_equal(srv.result(t1)[0], _alone(trees, tex, req))
+    assert np.array_equal(srv.result(t2)[0], trees[0].balls(c, r))
+    srv.release(t1)
+    srv.release(t2)
+    st = srv.stats()
+    assert st["host_slabs"] >= (8 << 30) // (128 << 20)
+    srv.close()
