@@ -411,9 +411,9 @@ QUALITIES = {"best": 0, "fast": 1, "adaptive": 2, "adaptive_ray_merge": 2 | 4,
 def measure_quality(torch, vg, dt, ht_ptr, states, tex, d_tex, flush, cpu=True, nframes=24):
     """The orbit at 1080p (every 5th frame) in every quality vox_render offers,
     through vox_cuda_render_quality_device (BEST: the frame kernel; FAST and
-    ADAPTIVE: every pixel's root search, then each 4x4 square's sequence of
-    renderer.c:215-318), one call per frame back to back, in pixels per
-    second.  With the CPU-baseline leg on (no --no-cpu-baseline), frame 0 of
+    ADAPTIVE: the squares kernel, each 4x4 square's sequence of
+    renderer.c:215-318 on half a warp), one call per frame back to back, in
+    pixels per second.  With the CPU-baseline leg on (no --no-cpu-baseline), frame 0 of
     each quality is checked against the oracle and the oracle's restatement
     of the same loop times a few frames of each on every host core."""
     sp = torch.cuda.current_stream().cuda_stream
@@ -444,6 +444,46 @@ def measure_quality(torch, vg, dt, ht_ptr, states, tex, d_tex, flush, cpu=True, 
             e["vs_cpu"] = e["value"] / e["cpu_value"]
         res[name] = e
     return res
+
+
+def measure_dropin(vg, ht_ptr, nframes=24):
+    """The drop-in renderer as a voxvision program drives it: a 1080p context
+    (vox_make_context_headless) over the library's host tree, the built-in
+    simple camera moved along the orbit, and per frame one synchronous
+    vox_render (the frame drawn into the context's page-locked frame) and one
+    vox_redraw (the frame copied to the buffer vox_context_pixels returns),
+    host-timed, in the default ADAPTIVE quality and in BEST."""
+    import ctypes as C
+    from voxvision_gb300.cameras import orbit_camera
+    L = vg.lib()
+    ctx = L.vox_make_context_headless(W, H)
+    picked = list(range(0, NFRAMES, max(1, NFRAMES // nframes)))[:nframes]
+    cams = [orbit_camera(f, NFRAMES, W, H, CENTRE, RADIUS) for f in picked]
+    L.vox_context_set_scene(ctx, ht_ptr)
+    out = {"frames": len(cams), "resolution": f"{W}x{H}",
+           "call": "vox_render then vox_redraw per frame, a vox_make_context_headless context"}
+    for name, q in (("adaptive", QUALITIES["adaptive"]), ("best", QUALITIES["best"])):
+        L.vox_context_set_quality(ctx, q)
+        render_ms, redraw_ms = [], []
+        for rep in range(4):
+            for cam in cams:
+                L.vox_context_set_camera(ctx, cam.obj)
+                t0 = time.perf_counter()
+                L.vox_render(ctx)
+                t1 = time.perf_counter()
+                L.vox_redraw(ctx)
+                t2 = time.perf_counter()
+                if L.vox_context_status(ctx):
+                    raise vg.VoxCudaError(L.vox_context_status(ctx), "vox_render")
+                if rep:                       # the first pass warms up
+                    render_ms.append((t1 - t0) * 1e3)
+                    redraw_ms.append((t2 - t1) * 1e3)
+        out[name] = {"quality": q, "render_ms": float(np.median(render_ms)),
+                     "render_p99_ms": float(np.percentile(render_ms, 99)),
+                     "redraw_ms": float(np.median(redraw_ms)),
+                     "mpixels_s": W * H / (float(np.median(render_ms)) * 1e-3) / 1e6}
+    L.vox_destroy_context(ctx)
+    return out
 
 
 def measure_editing(vg, vox, edits=1000, seed=16):
@@ -979,6 +1019,7 @@ def run_ours(args):
         btrees = build_batch_trees(vg)
         line["quality"] = measure_quality(torch, vg, dt, ht.ptr, states, tex, d_tex, flush,
                                           cpu=not args.no_cpu_baseline)
+        line["dropin"] = measure_dropin(vg, ht.ptr)
         line["incoherent"] = measure_incoherent(torch, vg, dt, flush)
         line["batched"] = measure_batched(torch, vg, flush, d_tex, btrees)
         line["editing"] = measure_editing(vg, vox)

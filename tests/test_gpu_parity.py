@@ -326,6 +326,46 @@ def test_renderer_context_api(tree256):
     L.vox_destroy_context(ctx)
 
 
+def test_renderer_context_frames_in_sequence(tree256):
+    """A context's frame is its own, so each vox_render clears only what the
+    previous frame drew outside the new tree rectangle.  A sequence of
+    cameras that moves the rectangle around -- other sides of the orbit, a
+    near camera whose rectangle is the whole frame, one looking away (empty
+    rectangle) -- in BEST, ADAPTIVE and FAST quality: every frame is the
+    oracle's, with no pixel left from an earlier one."""
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera
+    ht, dt = tree256
+    L = vg().lib()
+    W, H = 320, 240
+    ctx = L.vox_make_context_headless(W, H)
+    cam = HostCamera(0)
+    L.vox_context_set_camera(ctx, cam.obj)
+    L.vox_context_set_scene(ctx, ht.ptr)
+    centre = np.float32([128, 128, 128])
+    poses = [(665.0, 0.3, 20.0, False), (665.0, 2.4, 40.0, False), (230.0, 1.0, 10.0, False),
+             (665.0, 4.0, 5.0, True), (900.0, 5.1, 30.0, False), (665.0, 2.4, 40.0, False), (400.0, 0.7, 25.0, False)]
+    tex = wl.texture32(7)
+    drawn = 0
+    for k, (r, az, el, away) in enumerate(poses):
+        pos = wl.pose_position(centre, r, az, el)
+        cam.set_position(pos)
+        cam.look_at(tuple(2 * np.asarray(pos) - centre) if away else tuple(centre))
+        q = (0, 2, 1)[k % 3]
+        assert L.vox_context_set_quality(ctx, q) == 1
+        L.vox_render(ctx)
+        assert L.vox_context_status(ctx) == 0
+        L.vox_redraw(ctx)
+        px = np.ctypeslib.as_array(C.cast(L.vox_context_pixels(ctx), C.POINTER(C.c_uint32)), (H * W,))
+        ref, _ = orc.render_quality(ht.ptr, cam.state(), W, H, q, tex)
+        assert np.array_equal(px.reshape(H, W), ref), (k, q)
+        drawn += int((ref != 0).sum())
+        if away:
+            assert not ref.any()
+    assert drawn > 10000
+    L.vox_destroy_context(ctx)
+
+
 def test_errors_and_empty_tree():
     _reset_voxel()
     dt = vg().DeviceTree(None)

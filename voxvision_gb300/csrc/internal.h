@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "flatten.h"
+#include "frame_memo.h"
 #include "pool_layout.h"
 #include "traverse.cuh"
 #include "../../include/voxtrees_cuda.h"
@@ -112,6 +113,8 @@ struct FramePlan {
     uint32_t x0, y0, x1, y1;     // traced rectangle, multiples of 8 x 4
     uint32_t ntx, nty, ctx, cty; // tiles across / down, tile where the centre projects
     uint32_t ntiles, nclear;     // tracing blocks, clearing blocks
+    uint32_t cx0, cy0, cx1, cy1; // where the frame may hold non-zero pixels before the launch: the
+                                 // clearing blocks zero this rectangle outside the traced one
 };
 
 }  // namespace vox
@@ -129,6 +132,9 @@ void frame_rect_of(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t 
  * inside the rectangle. */
 void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h, bool cull,
                 vox::FramePlan &p);
+/* The clearing blocks of a plan (plan_frame calls it without a memo). */
+void plan_clearing(vox::FramePlan &p, const vox::FrameMemo *memo);
+
 
 /* The batched frame kernel over a job table the caller allocated for one
  * launch (batch.cu): fills h_table (pinned, frame_job_table_bytes(njobs)

@@ -25,6 +25,7 @@
 
 #include "../../include/voxrnd.h"
 #include "../../include/voxtrees_cuda.h"
+#include "frame_memo.h"
 #include "lights_internal.h"
 
 #define EXPORT extern "C" __attribute__((visibility("default")))
@@ -56,6 +57,8 @@ struct vox_rnd_ctx {
     uint64_t d_lights_version = 0;                 // the manager's version that copy holds
     float *h_rays = nullptr;                       // pixel directions of a host-computed camera (pinned)
     float *d_rays = nullptr;                       // their device copy
+    vox::FrameMemo memo{false, 0, 0, 0, 0};        // what the frame still holds of the last one
+    vox::FrameMemo shown{true, 0, 0, 0, 0};        // what `pixels` holds (zeroed at creation)
 };
 
 namespace {
@@ -234,11 +237,17 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
         if (rc) { ctx->status = rc; return; }
         vox_dot origin;
         ctx->camera->iface->get_position(ctx->camera, origin);   // renderer.c:231
-        rc = vox_cuda_render_rays_device(ctx->tree, origin, ctx->d_rays, ctx->w, ctx->h, ctx->quality, ctx->d_tex,
-                                         lights, target, ctx->stream);
+        vox_cuda_camera at;
+        std::memset(&at, 0, sizeof at);
+        at.kind = VOX_CUDA_CAMERA_SIMPLE;   // only its position is read
+        for (int a = 0; a < 3; a++) at.position[a] = origin[a];
+        rc = render_frame_memo(ctx->tree, &at, ctx->d_rays, ctx->w, ctx->h, ctx->quality, ctx->d_tex, lights,
+                               target, ctx->stream, &ctx->memo);
     } else {
-        rc = vox_cuda_render_lit_device(ctx->tree, &cam, ctx->w, ctx->h, ctx->quality, ctx->d_tex, lights, target,
-                                        ctx->stream);
+        // the frame is the context's own: the next one clears only what this
+        // one drew outside the new tree rectangle
+        rc = render_frame_memo(ctx->tree, &cam, nullptr, ctx->w, ctx->h, ctx->quality, ctx->d_tex, lights, target,
+                               ctx->stream, &ctx->memo);
     }
     if (rc) { ctx->status = rc; return; }
     size_t bytes = (size_t)ctx->w * ctx->h * 4;
@@ -251,9 +260,26 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
     ctx->status = VOX_CUDA_OK;
 }
 
+// The last frame into the buffer vox_context_pixels returns.  Both frames
+// are zero outside their tree rectangles when their memos are valid, so only
+// the box covering both rectangles is copied.
 EXPORT void vox_redraw(struct vox_rnd_ctx *ctx)
 {
-    std::memcpy(ctx->pixels, ctx->h_stage, (size_t)ctx->w * ctx->h * 4);
+    const size_t w = ctx->w;
+    const vox::FrameMemo &now = ctx->memo, &was = ctx->shown;
+    if (!now.valid || !was.valid) {
+        std::memcpy(ctx->pixels, ctx->h_stage, w * ctx->h * 4);
+    } else {
+        uint32_t x0 = ctx->w, y0 = ctx->h, x1 = 0, y1 = 0;
+        for (const vox::FrameMemo *m : {&now, &was})
+            if (m->x1 > m->x0 && m->y1 > m->y0) {
+                x0 = std::min(x0, m->x0); y0 = std::min(y0, m->y0);
+                x1 = std::max(x1, m->x1); y1 = std::max(y1, m->y1);
+            }
+        for (uint32_t y = y0; y < y1 && x1 > x0; y++)
+            std::memcpy(ctx->pixels + y * w + x0, ctx->h_stage + y * w + x0, (size_t)(x1 - x0) * 4);
+    }
+    ctx->shown = now;
 }
 
 EXPORT const uint32_t *vox_context_pixels(const struct vox_rnd_ctx *ctx) { return ctx->pixels; }

@@ -40,6 +40,7 @@ using vox::centre_out;
 using vox::DevTree;
 using vox::RayHit;
 using vox::FramePlan;
+using vox::FrameMemo;
 
 namespace {
 
@@ -139,19 +140,24 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-// A clearing block of a frame launch (block index ntiles and up): the frame
-// outside the traced rectangle, rows dealt to the block's warps; a warp's
-// lanes store 16 bytes each when the frame is 16-byte aligned (row starts and
-// x0, x1 then are: w is a multiple of 16, x0 and x1 of 8).
+// A clearing block of a frame launch (block index ntiles and up): the
+// clearing rectangle of the plan outside the traced one, rows dealt to the
+// block's warps; a warp's lanes store 16 bytes each when the frame is 16-byte
+// aligned (row starts and every bound then are: w is a multiple of 16, the
+// rectangles' x bounds of 8 or w).
 __device__ __forceinline__ void clear_outside(const FramePlan &p, uint32_t w, uint32_t h, uint32_t *argb,
                                               uint32_t warp, uint32_t lane)
 {
     const bool vec = (reinterpret_cast<uintptr_t>(argb) & 15u) == 0;
     const uint32_t nw = (gridDim.x - p.ntiles) * 4u;
-    for (uint32_t y = (blockIdx.x - p.ntiles) * 4u + warp; y < h; y += nw) {
+    for (uint32_t y = p.cy0 + (blockIdx.x - p.ntiles) * 4u + warp; y < p.cy1; y += nw) {
         uint32_t *row = argb + (size_t)y * w;
-        uint32_t a0 = 0, b0 = w, a1 = 0, b1 = 0;          // full row, or its two margins
-        if (y >= p.y0 && y < p.y1) { b0 = p.x0; a1 = p.x1; b1 = w; }
+        uint32_t a0 = p.cx0, b0 = p.cx1, a1 = 0, b1 = 0;  // the row's part of the clearing rectangle,
+        if (y >= p.y0 && y < p.y1) {                       // or its two margins beside the traced one
+            b0 = min(p.cx1, max(p.cx0, p.x0));
+            a1 = max(p.cx0, min(p.cx1, p.x1));
+            b1 = p.cx1;
+        }
         if (vec) {
             uint4 *r4 = reinterpret_cast<uint4 *>(row);
             for (uint32_t i = a0 / 4 + lane; i < b0 / 4; i += 32) r4[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -473,11 +479,13 @@ constexpr int MINB_ALONE = 8, MINB_PIPELINED = 12;
 template <bool COUNT>
 cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                           const uint8_t *tex, uint32_t *argb, unsigned long long *counts, cudaStream_t s,
-                          bool pipelined = false, const vox::DevLights *lights = nullptr)
+                          bool pipelined = false, const vox::DevLights *lights = nullptr,
+                          vox::FrameMemo *memo = nullptr)
 {
     // the counting kernel counts the reference's work: every pixel traced
     FramePlan p;
     plan_frame(t, cam, w, h, !COUNT && g_render_cull.load(), p);
+    if (memo) plan_clearing(p, memo);
     void (*kern)(DevTree, vox_cuda_camera, uint32_t, uint32_t, FramePlan, const uint8_t *, uint32_t *,
                  unsigned long long *, uint32_t *, vox::DevLights);
     vox::DevLights L{};
@@ -512,8 +520,9 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
     cfg.numAttrs = g_render_overlap.load() ? 1 : 0;
     cudaError_t e = cudaLaunchKernelEx(&cfg, kern, t->dev, cam, w, h, p, tex, argb, counts, t->d_status, L);
     count_launch();
-    if (e != cudaSuccess) return e;
-    return cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (memo) *memo = FrameMemo{e == cudaSuccess, p.x0, p.y0, p.x1, p.y1};
+    return e;
 }
 
 // FAST / ADAPTIVE frames, and with a ray buffer frames of every quality: one
@@ -521,7 +530,8 @@ cudaError_t launch_render(const vox_cuda_tree *t, const vox_cuda_camera &cam, ui
 // with blocks that clear the rest of the frame.
 cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, uint32_t h,
                                   unsigned int quality, const uint8_t *tex, uint32_t *argb, cudaStream_t s,
-                                  const vox::DevLights *lights = nullptr, const float *rays = nullptr)
+                                  const vox::DevLights *lights = nullptr, const float *rays = nullptr,
+                                  vox::FrameMemo *memo = nullptr)
 {
     vox::DevLights L{};
     if (lights) L = *lights;
@@ -541,7 +551,11 @@ cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera 
         p.cty = p.nty / 2;
         p.ntiles = p.ntx * p.nty;
         p.nclear = 0;
+        p.cx0 = p.cy0 = 0;
+        p.cx1 = w;
+        p.cy1 = h;
     }
+    if (memo) plan_clearing(p, memo);
     const int cap = t->cap_class;
     void (*squares)(DevTree, vox_cuda_camera, uint32_t, uint32_t, FramePlan, unsigned int, const uint8_t *,
                     uint32_t *, uint32_t *, vox::DevLights, const float *);
@@ -564,8 +578,9 @@ cudaError_t launch_render_squares(const vox_cuda_tree *t, const vox_cuda_camera 
     cfg.numAttrs = g_render_overlap.load() ? 1 : 0;
     cudaError_t e = cudaLaunchKernelEx(&cfg, squares, t->dev, cam, w, h, p, quality, tex, argb, t->d_status, L, rays);
     count_launch();
-    if (e != cudaSuccess) return e;
-    return cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (memo) *memo = FrameMemo{e == cudaSuccess, p.x0, p.y0, p.x1, p.y1};
+    return e;
 }
 
 
@@ -750,9 +765,23 @@ void plan_frame(const vox_cuda_tree *t, const vox_cuda_camera &cam, uint32_t w, 
     double tx = (c[0] - p.x0) / TILE_W, ty = (c[1] - p.y0) / TILE_H;
     p.ctx = (p.ntx && tx >= 0) ? (uint32_t)std::min(tx, p.ntx - 1.0) : 0;   // NaN -> 0
     p.cty = (p.nty && ty >= 0) ? (uint32_t)std::min(ty, p.nty - 1.0) : 0;
-    // clearing blocks: one warp per row up to 64 blocks, none when nothing is left
-    uint64_t outside = (uint64_t)w * h - (uint64_t)(p.x1 - p.x0) * (p.y1 - p.y0);
-    p.nclear = outside ? std::min<uint32_t>(64u, (h + 3) / 4) : 0;
+    p.cx0 = 0; p.cy0 = 0; p.cx1 = w; p.cy1 = h;
+    plan_clearing(p, nullptr);
+}
+
+// The clearing blocks of a plan: the frame outside the traced rectangle, or
+// with a valid memo only the part of the memo's rectangle outside it; one
+// warp a row, up to 64 blocks, none when nothing is left (a launch with no
+// tracing block still gets one block, which finds nothing to do).
+void plan_clearing(FramePlan &p, const FrameMemo *memo)
+{
+    if (memo && memo->valid) {
+        p.cx0 = memo->x0; p.cy0 = memo->y0; p.cx1 = memo->x1; p.cy1 = memo->y1;
+    }
+    const bool empty = p.cx1 <= p.cx0 || p.cy1 <= p.cy0;
+    const bool covered = p.x1 > p.x0 && p.y1 > p.y0 && p.cx0 >= p.x0 && p.cx1 <= p.x1 && p.cy0 >= p.y0 &&
+                         p.cy1 <= p.y1;
+    p.nclear = (empty || covered) ? 0u : std::min<uint32_t>(64u, (p.cy1 - p.cy0 + 3) / 4);
     if (p.ntiles + p.nclear == 0) p.nclear = 1;
 }
 
@@ -1644,17 +1673,25 @@ struct vox_cuda_lights {
     vox::DevLights dev{};
 };
 
-static int render_any_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
-                             unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights,
-                             uint32_t *argb, void *stream)
+int render_frame_memo(const vox_cuda_tree *t, const vox_cuda_camera *cam, const float *dirs, uint32_t w, uint32_t h,
+                      unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights, uint32_t *argb,
+                      cudaStream_t s, FrameMemo *memo)
 {
+    // (a call refused here writes nothing: the memo still holds)
     int rc = check_render_args(t, cam, w, h, tex, argb);
     if (rc) return rc;
     if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
     const vox::DevLights *L = lights ? &lights->dev : nullptr;
-    if ((quality & VOX_CUDA_QUALITY_MODE_MASK) == VOX_CUDA_QUALITY_BEST)
-        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true, L));
-    return status_of(launch_render_squares(t, *cam, w, h, quality, tex, argb, as_stream(stream), L));
+    if (!dirs && (quality & VOX_CUDA_QUALITY_MODE_MASK) == VOX_CUDA_QUALITY_BEST)
+        return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, s, true, L, memo));
+    return status_of(launch_render_squares(t, *cam, w, h, quality, tex, argb, s, L, dirs, memo));
+}
+
+static int render_any_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                             unsigned int quality, const uint8_t *tex, const vox_cuda_lights *lights,
+                             uint32_t *argb, void *stream)
+{
+    return render_frame_memo(t, cam, nullptr, w, h, quality, tex, lights, argb, as_stream(stream), nullptr);
 }
 
 EXPORT int vox_cuda_render_quality_device(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w,
@@ -1685,11 +1722,7 @@ try {
     std::memset(&cam, 0, sizeof cam);
     cam.kind = VOX_CUDA_CAMERA_SIMPLE;   // only its position is read
     for (int a = 0; a < 3; a++) cam.position[a] = origin[a];
-    int rc = check_render_args(t, &cam, w, h, tex, argb);
-    if (rc) return rc;
-    if (!valid_quality(quality)) return VOX_CUDA_EINVAL;
-    return status_of(launch_render_squares(t, cam, w, h, quality, tex, argb, as_stream(stream),
-                                           lights ? &lights->dev : nullptr, dirs));
+    return render_frame_memo(t, &cam, dirs, w, h, quality, tex, lights, argb, as_stream(stream), nullptr);
 } VOX_ABI_FAIL_INT
 
 static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
