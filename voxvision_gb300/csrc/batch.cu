@@ -61,18 +61,6 @@ struct BatchJobDev {
 // Rows of the frame outside the traced rectangle that one clearing item zeroes.
 constexpr uint32_t CLEAR_ROWS = 8;
 
-// Queue index -> frame: the last job whose base is <= item (frames with no
-// item of that kind share their base with the next frame and are skipped).
-__device__ __forceinline__ uint32_t find_job(const uint32_t *base, uint32_t njobs, uint32_t tile)
-{
-    uint32_t lo = 0, hi = njobs;
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (base[mid] <= tile) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
 // One tile of TW x TH pixels of frame J (its `local`-th tile, taken outward
 // from where the tree's centre projects): ray, search, colour, store.
 template <int CAP, int TW, int TH>
@@ -133,18 +121,28 @@ __device__ __forceinline__ void run_clear(const BatchJobDev &J, uint32_t c, uint
 #define BATCH_MIN_BLOCKS 8
 #endif
 
+// Queue index -> frame: the last job whose tile (or clearing) base is <=
+// item (frames with no item of that kind share their base with the next
+// frame and are skipped), searched in the job table itself through L1.  The
+// kernels keep no copy of the bases in shared memory: with none, L1 has the
+// whole of its space, and the orbit draws 0.4% faster (7.19 against 7.22 ms).
+__device__ __forceinline__ uint32_t find_job(const BatchJobDev *jobs, uint32_t njobs, uint32_t item, bool clear)
+{
+    uint32_t lo = 0, hi = njobs;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint32_t b = clear ? __ldg(&jobs[mid].clear_base) : __ldg(&jobs[mid].tile_base);
+        if (b <= item) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 template <int CAP, int TW, int TH>
 __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) batch_kernel(const BatchHead *__restrict__ head, uint32_t grab,
                                                     uint32_t *__restrict__ counter)
 {
-    __shared__ uint32_t tbase[MAX_JOBS], cbase[MAX_JOBS];
     const BatchJobDev *jobs = reinterpret_cast<const BatchJobDev *>(head + 1);
     const uint32_t njobs = head->njobs, ntiles = head->total_tiles, total = ntiles + head->total_clear;
-    for (uint32_t i = threadIdx.x; i < njobs; i += blockDim.x) {
-        tbase[i] = jobs[i].tile_base;
-        cbase[i] = jobs[i].clear_base;
-    }
-    __syncthreads();
     const uint32_t lane = threadIdx.x & 31;
     for (;;) {
         uint32_t t0 = 0;
@@ -154,11 +152,11 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) batch_kernel(const Batc
         uint32_t t1 = min(t0 + grab, total);
         for (uint32_t item = t0; item < t1; item++) {
             if (item < ntiles) {
-                const BatchJobDev &J = jobs[find_job(tbase, njobs, item)];
+                const BatchJobDev &J = jobs[find_job(jobs, njobs, item, false)];
                 run_tile<CAP, TW, TH>(J, item - J.tile_base, lane);
             } else {
                 uint32_t c = item - ntiles;
-                const BatchJobDev &J = jobs[find_job(cbase, njobs, c)];
+                const BatchJobDev &J = jobs[find_job(jobs, njobs, c, true)];
                 run_clear(J, c - J.clear_base, lane);
             }
         }
@@ -176,11 +174,8 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const Bat
                                                      uint32_t *__restrict__ counter, uint32_t *__restrict__ done,
                                                      uint32_t *flags, uint32_t epoch)
 {
-    __shared__ uint32_t base[MAX_JOBS];
     const BatchJobDev *jobs = reinterpret_cast<const BatchJobDev *>(head + 1);
     const uint32_t njobs = head->njobs, total = head->total_tiles;
-    for (uint32_t i = threadIdx.x; i < njobs; i += blockDim.x) base[i] = jobs[i].tile_base;
-    __syncthreads();
     const uint32_t lane = threadIdx.x & 31;
     for (;;) {
         uint32_t t0 = 0;
@@ -189,7 +184,7 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const Bat
         if (t0 >= total) break;
         uint32_t t1 = min(t0 + grab, total);
         for (uint32_t item = t0; item < t1; item++) {
-            uint32_t j = find_job(base, njobs, item);
+            uint32_t j = find_job(jobs, njobs, item, false);
             const BatchJobDev &J = jobs[j];
             uint32_t local = item - J.tile_base, ntile = J.ntx * J.nty;
             if (local < ntile) run_tile<CAP, TW, TH>(J, local, lane);
@@ -197,7 +192,7 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const Bat
             __syncwarp();
             if (lane == 0) {
                 __threadfence();   // this warp's stores (ordered before by the warp barrier), then the count
-                uint32_t items = (j + 1 < njobs ? base[j + 1] : total) - J.tile_base;
+                uint32_t items = (j + 1 < njobs ? __ldg(&jobs[j + 1].tile_base) : total) - J.tile_base;
                 if (atomicAdd(&done[j], 1u) + 1u == items) {
                     __threadfence_system();
                     *(volatile uint32_t *)&flags[j] = epoch;
