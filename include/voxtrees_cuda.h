@@ -334,8 +334,10 @@ int vox_cuda_frame_rect(const float *bbox, const vox_cuda_camera *camera, uint32
  * BEST runs the per-pixel kernel above; FAST and ADAPTIVE (with or without
  * ray merging) follow each 4x4 square's sequence of renderer.c:215-318 (its
  * Z-order, the previous pixel's leaf as the search root, the corner test),
- * with every pixel's search from the root made beforehand in parallel.
- * These allocate w*h*16 bytes of stream-ordered scratch for the call.
+ * a square on half a warp: every pixel's search from the root, then the
+ * searches from the square's leaf for the pixels still to come.  The
+ * _device calls allocate nothing; the host-buffer calls allocate a w*h*4
+ * byte stream-ordered frame when `argb` is not page-locked.
  * Pixels the reference leaves undrawn are 0.  EINVAL for a combination
  * vox_context_set_quality rejects.
  * Replaces vox_render + vox_redraw (src/voxrnd/renderer.c:200-327). */
