@@ -483,9 +483,10 @@ typedef struct vox_cuda_server vox_cuda_server;
 /* config NULL = 40 GiB device budget, 16 GiB pinned host budget, 256 in
  * flight, 32 per launch, 16 streams, 32 launches in flight, frames copied to
  * host memory.  texture: host 32^3 bytes used for every frame.  Half the
- * pinned-host budget (at most 8 GiB) is page-locked here, in 128 MiB slabs
- * that results are carved from (about 0.6 s for 8 GiB); a thread of the
- * server keeps two more slabs pinned ahead of need, up to the budget. */
+ * pinned-host budget (at most 8 GiB; with frames_on_device an eighth, at most
+ * 1 GiB) is page-locked here, in 128 MiB slabs that results are carved from
+ * (about 0.6 s for 8 GiB); a thread of the server keeps two more slabs pinned
+ * ahead of need, up to the budget. */
 int vox_cuda_server_create(const vox_cuda_server_config *config, const uint8_t *texture,
                            vox_cuda_server **out);
 /* Make a tree available to requests (charged to the budget while the server

@@ -741,8 +741,11 @@ try {
         // served stalls the worker: at 20 kHz each further 128 MiB slab
         // pinned during a trace went with a frame p99 of 15-76 ms, against
         // 1-3 ms for traces that pinned nothing.
-        if (!s->pinned.start(s->device, std::min<uint64_t>(cfg.host_budget_bytes / 2, uint64_t(8) << 30),
-                             cfg.host_budget_bytes)) {
+        // With frames kept on the device only ball inputs and hits live in
+        // pinned memory: an eighth of the budget (at most 1 GiB) then.
+        const uint64_t now = cfg.frames_on_device ? std::min<uint64_t>(cfg.host_budget_bytes / 8, uint64_t(1) << 30)
+                                                  : std::min<uint64_t>(cfg.host_budget_bytes / 2, uint64_t(8) << 30);
+        if (!s->pinned.start(s->device, now, cfg.host_budget_bytes)) {
             vox_cuda_server_destroy(s);
             return VOX_CUDA_ENOMEM;
         }
