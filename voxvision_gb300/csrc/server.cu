@@ -14,9 +14,9 @@
  * into host memory slow the frame kernel by a third).  A frame is zero
  * outside its tree's screen rectangle, and a reused buffer is zero outside
  * the rectangle of the frame it held last, so only the box covering both
- * crosses to the host (about a sixth of the bytes on a mixed load).  Ball hits, one byte a
- * query, are written in place by the ball kernel, which also reads its staged
- * inputs from pinned memory.  The device budget holds the resident trees,
+ * crosses to the host (about a sixth of the bytes on a mixed load).  Ball
+ * hits, one byte a query, are written in place by the ball kernel, which
+ * also reads its staged inputs from pinned memory.  The device budget holds the resident trees,
  * the per-launch job tables and the frames being drawn; the pinned-host
  * budget holds the results and staged inputs.
  * Requests that arrive while earlier launches are still on the GPU go out
@@ -134,9 +134,9 @@ FrameCopy plan_frame_copy(const Dirty &d, uint32_t w, uint32_t h, const uint32_t
 // -- which admits and launches every request -- does not stop for
 // page-locking (14 GB/s on the Grace host: 4.5 ms for one 64 MiB buffer).
 // With no slab room ready, a free buffer of a larger class serves before the
-// worker pins one itself.  Larger buffers are pinned one by one.  Buffers go back to their class's
-// free list with their Dirty state, and slabs stay pinned until the pool is
-// destroyed.
+// worker pins one itself.  Larger buffers are pinned one by one.  Buffers go
+// back to their class's free list with their Dirty state, and slabs stay
+// pinned until the pool is destroyed.
 class PinnedPool {
   public:
     static constexpr size_t SLAB = size_t(128) << 20, MAX_CARVED = size_t(64) << 20, SPARES = 2;
