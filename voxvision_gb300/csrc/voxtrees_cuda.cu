@@ -235,6 +235,16 @@ __device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const floa
     }
 }
 
+// Register bound of render_squares_kernel: none by default (72 registers, 7
+// blocks of 128 threads per SM).  Bounds of 8 and 9 blocks (64 and 56
+// registers, with spills) drew the 1080p orbit's FAST and ADAPTIVE frames 1-3%
+// slower.
+#ifdef SQUARES_MIN_BLOCKS
+#define SQUARES_BOUNDS __launch_bounds__(128, SQUARES_MIN_BLOCKS)
+#else
+#define SQUARES_BOUNDS __launch_bounds__(128)
+#endif
+
 // FAST and ADAPTIVE frames, and with a ray buffer frames of every quality,
 // in one launch.  In renderer.c a pixel's leaf is either the previous
 // pixel's leaf, when the ray meets a voxel there (the search from the leaf,
@@ -246,30 +256,19 @@ __device__ __forceinline__ void pixel_dir(const vox_cuda_camera &cam, const floa
 // the lanes still to be drawn make, at once, the search from the leaf the
 // square's walk currently holds.  The walk itself -- the reference's 16
 // pixels in its order, with its choices of mode, merging and leaf -- runs on
-// every lane of the square alike over those results (shuffled from the
-// pixel's lane), and wherever it changes to a leaf the round's searches were
-// not made from, a new round makes them for the pixels after it.  A square
-// takes one round per change of leaf, and the leaf rarely changes within a
-// square.  The results are the reference's by construction: the same
-// searches of the same rays, the same choices between them; searches made
-// for pixels the walk then reaches another way are dropped.
-// Register bound of render_squares_kernel: none by default (72 registers, 7
-// blocks of 128 threads per SM).  Bounds of 8 and 9 blocks (64 and 56
-// registers, with spills) drew the 1080p orbit's FAST and ADAPTIVE frames 1-3%
-// slower.
-#ifdef SQUARES_MIN_BLOCKS
-#define SQUARES_BOUNDS __launch_bounds__(128, SQUARES_MIN_BLOCKS)
-#else
-#define SQUARES_BOUNDS __launch_bounds__(128)
-#endif
-
+// every lane of the square alike over ballots of those results, and
+// wherever it changes to a leaf the round's searches were not made from, a
+// new round makes them for the pixels after it.  A square takes one round
+// per change of leaf, and the leaf rarely changes within a square.  The
+// results are the reference's by construction: the same searches of the
+// same rays, the same choices between them; searches made for pixels the
+// walk then reaches another way are dropped.
 template <int CAP, bool RAYS>
-__global__ void SQUARES_BOUNDS render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w,
-                                                             uint32_t h, FramePlan fp, unsigned int quality,
-                                                             const uint8_t *__restrict__ tex,
-                                                             uint32_t *__restrict__ argb,
-                                                             uint32_t *__restrict__ status, vox::DevLights lights,
-                                                             const float *__restrict__ rays)
+__global__ void SQUARES_BOUNDS render_squares_kernel(DevTree t, vox_cuda_camera cam, uint32_t w, uint32_t h,
+                                                     FramePlan fp, unsigned int quality,
+                                                     const uint8_t *__restrict__ tex, uint32_t *__restrict__ argb,
+                                                     uint32_t *__restrict__ status, vox::DevLights lights,
+                                                     const float *__restrict__ rays)
 {
     // renderer.c:23-25 rendering order {0, 1, 4, 5, 2, 3, 6, 7, 8, 9, 12, 13, 10, 11, 14, 15}, a nibble
     // each; the permutation is its own inverse, so it also maps a pixel to its place in the order
