@@ -359,3 +359,38 @@ def test_default_configuration_serves(setup):
     st = srv.stats()
     assert st["host_slabs"] >= (8 << 30) // (128 << 20)
     srv.close()
+
+
+def test_smaller_request_takes_a_larger_free_buffer(setup):
+    """With no pinned slabs to carve from (a pinned-host budget below one
+    slab, so every buffer is pinned on its own), a request whose size class
+    has no free buffer takes a free buffer of a larger class instead of
+    pinning another, and every frame drawn into such a buffer -- after one
+    of another row pitch -- is the plain call's and the oracle's."""
+    vg, wl, hosts, trees, tex = setup
+    from voxvision_gb300.cameras import HostCamera
+    srv = vg.Server(tex, vg.ServerConfig(1 << 34, 16 << 20, 4, 4, 1, 1))
+    ids = [srv.add_tree(t) for t in trees]
+
+    def frame(w, h, az):
+        cam = HostCamera(0)
+        cam.set_window_size(w, h)
+        cam.set_position(wl.pose_position((32.0,) * 3, 1.5 * 64 * 3 ** 0.5, az, 20.0))
+        cam.look_at((32.0,) * 3)
+        return ("frame", 0, cam.gpu_struct(), w, h, cam.state())
+
+    seq = [frame(640, 480, 0.4), frame(320, 240, 1.3), frame(640, 480, 2.2), frame(320, 240, 3.1),
+           frame(320, 240, 4.0)]
+    for q in seq:
+        t = srv.submit_frame(ids[0], q[2], q[3], q[4])
+        assert srv.wait(t, 60000) == 0
+        got, _ = srv.result(t)
+        srv.release(t)
+        assert np.array_equal(got, _alone(trees, tex, q))
+        assert np.array_equal(got, _oracle(tex, q))
+    st = srv.stats()
+    assert st["host_slabs"] == 0
+    # the first frame's result and job table are pinned; every later request
+    # reuses them (the 320x240 frames the 640x480 frame's larger buffer)
+    assert st["host_pins"] <= 3
+    srv.close()
