@@ -938,7 +938,8 @@ def run_ours(args):
     cam_arr = (vg.CameraStruct * nf)(*cams)
     htex = np.ascontiguousarray(tex)
     htex_p = htex.ctypes.data_as(C.c_void_p)
-    vg.check(L.vox_cuda_render_frames(dt.h, cam_arr, nf, W, H, htex_p, frame_ptrs, sp), "vox_cuda_render_frames")
+    for _ in range(max(1, args.warmup)):
+        vg.check(L.vox_cuda_render_frames(dt.h, cam_arr, nf, W, H, htex_p, frame_ptrs, sp), "vox_cuda_render_frames")
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
