@@ -114,9 +114,10 @@ __device__ __forceinline__ void run_clear(const BatchJobDev &J, uint32_t c, uint
 }
 
 // Register bound of the persistent kernels: 8 resident blocks of 128 threads
-// per SM (64 registers, a few bytes spilled).  On the 120-frame 1080p orbit
-// this draws 12% faster than the unbounded build (68 registers, 7 blocks);
-// 10 and 12 blocks (48 and 40 registers) spill more and draw slower.
+// per SM (at most 64 registers; the 8x4 batch kernel now fits in 62 with
+// nothing spilled).  On the 120-frame 1080p orbit this drew 12% faster than
+// the unbounded build (68 registers, 7 blocks); 10 and 12 blocks (48 and 40
+// registers) spill more and draw slower.
 #ifndef BATCH_MIN_BLOCKS
 #define BATCH_MIN_BLOCKS 8
 #endif
