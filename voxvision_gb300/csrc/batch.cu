@@ -7,8 +7,9 @@
  * do.  Here all the frames' tiles sit in one work queue.  Persistent warps
  * (a fixed number of blocks per SM) take tiles from a global counter until it
  * runs out, so the tail of one frame overlaps the body of the others and no
- * SM waits.  Frames are queued largest first and each frame's tiles outward
- * from where its tree projects, so long-running tiles start early.
+ * SM waits.  Frames are queued by tree (largest tree first) and largest
+ * first within a tree, and each frame's tiles outward from where its tree
+ * projects, so long-running tiles start early.
  *
  * Every ray is the same search as vox_cuda_render's (traverse.cuh), so each
  * frame is bit-identical to a plain vox_cuda_render call.
@@ -388,10 +389,16 @@ try {
     }
     b->jobs.assign(jobs, jobs + njobs);
     for (uint32_t i = 0; i < njobs; i++) b->cap_class = std::max(b->cap_class, jobs[i].tree->cap_class);
-    // largest frames first
     b->order.resize(njobs);
     std::iota(b->order.begin(), b->order.end(), 0u);
+    // frames of the largest tree first (their tiles run longest), each tree's
+    // largest frames first: one tree's frames at a time keep its nodes in L2
+    // (the mixed set: 2.79 ms against 2.81 with the largest frames of all
+    // trees first)
     std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t x, uint32_t y) {
+        if (jobs[x].tree->dev.n_units != jobs[y].tree->dev.n_units)
+            return jobs[x].tree->dev.n_units > jobs[y].tree->dev.n_units;
+        if (jobs[x].tree != jobs[y].tree) return jobs[x].tree < jobs[y].tree;
         return (uint64_t)jobs[x].w * jobs[x].h > (uint64_t)jobs[y].w * jobs[y].h;
     });
     if (config) b->cfg = *config;
