@@ -151,6 +151,10 @@ int enqueue_frame_jobs(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_t
 size_t ray_order_bytes(size_t n);
 cudaError_t ray_order(const vox_cuda_tree *t, const float *o, const float *d, size_t n, void *scratch,
                       uint32_t **order, cudaStream_t s);
+/* The same for a ball batch: grouped by the cell of the centre on a 16^3
+ * grid over the tree's box (scratch of ray_order_bytes(n) bytes). */
+cudaError_t ball_order(const vox_cuda_tree *t, const float *centres, size_t n, void *scratch, uint32_t **order,
+                       cudaStream_t s);
 
 /* Frames one after another in one persistent launch (batch.cu), each
  * announced when complete: flags[j] (host memory the device can write)

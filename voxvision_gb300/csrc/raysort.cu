@@ -9,16 +9,17 @@
  * box on an 8x8x8 grid over it (Morton order), makes the searches of a warp
  * start at the same part of the tree and walk it the same way: 16M random
  * rays over the 256^3 tree take 2.8 ms, sorting included, against 5.4 ms in
- * the given order.  (Ball batches are not reordered:
- * 1M random balls searched in centre order take 0.31 ms instead of 0.48 ms
- * when sorted beforehand, but sorting them here costs as much as it saves.)
+ * the given order.  Ball batches of 262,144 or more are grouped the same way
+ * by the cell of their centre on a 16x16x16 grid over the tree's box: 1M
+ * random balls take 0.40 ms, sorting included, against 0.47 ms.
  *
- * The order is a counting sort on those 12-bit keys: per block of
- * RAYS_PER_BLOCK rays a histogram in shared memory, the position of each
- * (key, block) pair from a prefix over blocks and keys, then each ray's slot
- * in `order`; the search kernel reads the j-th ray of the order from where
- * it was given and writes its result there.  Rays of one (key, block) pair
- * land in any order among themselves; that, too, changes no result.
+ * The order is a counting sort on those 12-bit keys: per block of up to
+ * 65,536 items (fewer for smaller batches, so that every SM gets blocks) a
+ * histogram in shared memory, the position of each (key, block) pair from a
+ * prefix over blocks and keys, then each item's slot in `order`; the search
+ * kernel reads the j-th item of the order from where it was given and writes
+ * its result there.  Items of one (key, block) pair land in any order among
+ * themselves; that, too, changes no result.
  * (Copying the rays into order instead makes a 16M-ray batch slower: each
  * ray's six floats become scattered partial-sector stores.)
  */
@@ -33,7 +34,17 @@ namespace {
 constexpr int KEY_BITS = 12;
 constexpr uint32_t NKEYS = 1u << KEY_BITS;
 constexpr int SORT_THREADS = 1024;
-constexpr uint32_t RAYS_PER_BLOCK = 65536;
+
+// Items one block keys and places: 65,536 for large batches (256 blocks for
+// 16M rays), fewer for smaller ones so that a batch of a million still
+// spreads over the SMs (8,192 at least, which keeps the per-block
+// histograms small beside the items).
+size_t items_per_block(size_t n)
+{
+    size_t per = (n + 255) / 256;
+    per = per < 8192 ? 8192 : (per > 65536 ? 65536 : per);
+    return per;
+}
 
 struct KeyFrame {
     float lo[3], inv[3];   // cell = floor((p - lo) * inv), clamped to the grid
@@ -78,16 +89,18 @@ __device__ __forceinline__ uint32_t ray_key(const float *o, const float *d, size
     return (oct << 9) | morton_cell<3>(p, 0, f);
 }
 
-// Keys of a block's rays and the block's histogram (block-major).
-__global__ void __launch_bounds__(SORT_THREADS) k_keys(const float *o, const float *d, size_t n, KeyFrame f,
-                                                        uint16_t *keys, uint32_t *hist)
+// Keys of a block's items and the block's histogram (block-major): rays
+// (d given) by ray_key, balls (d NULL) by the cell of their centre on a
+// 16^3 grid over the tree's box.
+__global__ void __launch_bounds__(SORT_THREADS) k_keys(const float *o, const float *d, size_t n, size_t per,
+                                                        KeyFrame f, uint16_t *keys, uint32_t *hist)
 {
     __shared__ uint32_t h[NKEYS];
     for (uint32_t k = threadIdx.x; k < NKEYS; k += SORT_THREADS) h[k] = 0;
     __syncthreads();
-    size_t b0 = (size_t)blockIdx.x * RAYS_PER_BLOCK, b1 = b0 + RAYS_PER_BLOCK < n ? b0 + RAYS_PER_BLOCK : n;
+    size_t b0 = (size_t)blockIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
     for (size_t i = b0 + threadIdx.x; i < b1; i += SORT_THREADS) {
-        uint32_t k = ray_key(o, d, i, f);
+        uint32_t k = d ? ray_key(o, d, i, f) : morton_cell<4>(o, i, f);
         keys[i] = (uint16_t)k;
         atomicAdd(&h[k], 1u);
     }
@@ -135,14 +148,14 @@ __global__ void __launch_bounds__(1024) k_key_starts(uint32_t *total)
 }
 
 // Each ray's slot in the traced order.
-__global__ void __launch_bounds__(SORT_THREADS) k_place(const uint16_t *keys, size_t n, const uint32_t *hist,
-                                                         const uint32_t *start, uint32_t *order)
+__global__ void __launch_bounds__(SORT_THREADS) k_place(const uint16_t *keys, size_t n, size_t per,
+                                                         const uint32_t *hist, const uint32_t *start, uint32_t *order)
 {
     __shared__ uint32_t base[NKEYS];
     for (uint32_t k = threadIdx.x; k < NKEYS; k += SORT_THREADS)
         base[k] = start[k] + hist[(size_t)blockIdx.x * NKEYS + k];
     __syncthreads();
-    size_t b0 = (size_t)blockIdx.x * RAYS_PER_BLOCK, b1 = b0 + RAYS_PER_BLOCK < n ? b0 + RAYS_PER_BLOCK : n;
+    size_t b0 = (size_t)blockIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
     for (size_t i = b0 + threadIdx.x; i < b1; i += SORT_THREADS) order[atomicAdd(&base[keys[i]], 1u)] = (uint32_t)i;
 }
 
@@ -152,14 +165,15 @@ static size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
 size_t ray_order_bytes(size_t n)
 {
-    size_t nb = (n + RAYS_PER_BLOCK - 1) / RAYS_PER_BLOCK;
+    size_t nb = (n + items_per_block(n) - 1) / items_per_block(n);
     return up256(n * 2) + up256(n * 4) + nb * NKEYS * 4 + NKEYS * 4 + 256;
 }
 
-cudaError_t ray_order(const vox_cuda_tree *t, const float *o, const float *d, size_t n, void *scratch,
-                      uint32_t **order, cudaStream_t s)
+// The order of n rays (d given) or balls (d NULL) in `scratch`.
+static cudaError_t sort_order(const vox_cuda_tree *t, const float *o, const float *d, size_t n, void *scratch,
+                              uint32_t **order, cudaStream_t s)
 {
-    size_t nb = (n + RAYS_PER_BLOCK - 1) / RAYS_PER_BLOCK;
+    const size_t per = items_per_block(n), nb = (n + per - 1) / per;
     char *p = static_cast<char *>(scratch);
     uint16_t *keys = reinterpret_cast<uint16_t *>(p);
     p += up256(n * 2);
@@ -167,18 +181,32 @@ cudaError_t ray_order(const vox_cuda_tree *t, const float *o, const float *d, si
     p += up256(n * 4);
     uint32_t *hist = reinterpret_cast<uint32_t *>(p);
     uint32_t *total = hist + nb * NKEYS;
-    // entry cells: 8 per axis over the tree's box
+    // cells over the tree's box: 8 per axis for rays' entry points, 16 for
+    // balls' centres
+    const float cells = d ? 8.0f : 16.0f;
     KeyFrame f;
     for (int a = 0; a < 3; a++) {
         f.blo[a] = t->bbox[a];
         f.bhi[a] = t->bbox[3 + a];
         f.lo[a] = t->bbox[a];
-        f.inv[a] = 8.0f / fmaxf(t->bbox[3 + a] - t->bbox[a], 1e-30f);
+        f.inv[a] = cells / fmaxf(t->bbox[3 + a] - t->bbox[a], 1e-30f);
     }
-    k_keys<<<(unsigned)nb, SORT_THREADS, 0, s>>>(o, d, n, f, keys, hist);
+    k_keys<<<(unsigned)nb, SORT_THREADS, 0, s>>>(o, d, n, per, f, keys, hist);
     k_key_blocks<<<NKEYS / 256, 256, 0, s>>>(hist, (uint32_t)nb, total);
     k_key_starts<<<1, 1024, 0, s>>>(total);
-    k_place<<<(unsigned)nb, SORT_THREADS, 0, s>>>(keys, n, hist, total, *order);
+    k_place<<<(unsigned)nb, SORT_THREADS, 0, s>>>(keys, n, per, hist, total, *order);
     for (int i = 0; i < 4; i++) count_launch();
     return cudaGetLastError();
+}
+
+cudaError_t ray_order(const vox_cuda_tree *t, const float *o, const float *d, size_t n, void *scratch,
+                      uint32_t **order, cudaStream_t s)
+{
+    return sort_order(t, o, d, n, scratch, order, s);
+}
+
+cudaError_t ball_order(const vox_cuda_tree *t, const float *centres, size_t n, void *scratch, uint32_t **order,
+                       cudaStream_t s)
+{
+    return sort_order(t, centres, nullptr, n, scratch, order, s);
 }

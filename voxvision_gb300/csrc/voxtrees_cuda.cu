@@ -104,12 +104,14 @@ __global__ void __launch_bounds__(256) ball_kernel(DevTree t, const float *__res
                                                    const float *__restrict__ rad, size_t n,
                                                    uint8_t *__restrict__ hit,
                                                    unsigned long long *__restrict__ counts,
-                                                   uint32_t *__restrict__ status)
+                                                   uint32_t *__restrict__ status,
+                                                   const uint32_t *__restrict__ order)
 {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     Counts c{0, 0, 0};
     bool overflow = false;
-    if (i < n) {
+    if (j < n) {
+        size_t i = order ? order[j] : j;   // the j-th ball searched (raysort.cu)
         bool h = vox::trace_ball<4 * CAP, COUNT>(t, ctr[3 * i], ctr[3 * i + 1], ctr[3 * i + 2], rad[i],
                                                  c, overflow);
         if (!COUNT) hit[i] = h ? 1 : 0;
@@ -449,19 +451,35 @@ cudaError_t launch_rays(const vox_cuda_tree *t, const float *o, const float *d, 
     return e;
 }
 
+// Batches of at least this many balls are searched grouped by centre cell.
+constexpr size_t BALL_SORT_MIN = 1 << 18;
+
 template <bool COUNT>
 cudaError_t launch_balls(const vox_cuda_tree *t, const float *c, const float *r, size_t n, uint8_t *hit,
                          unsigned long long *counts, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
+    void *scratch = nullptr;
+    uint32_t *order = nullptr;
+    if (!COUNT && n >= BALL_SORT_MIN && n <= 0xFFFFFFFFull) {
+        cudaError_t e = cudaMallocAsync(&scratch, ray_order_bytes(n), s);
+        if (e != cudaSuccess) return e;
+        e = ball_order(t, c, n, scratch, &order, s);
+        if (e != cudaSuccess) {
+            cudaFreeAsync(scratch, s);
+            return e;
+        }
+    }
     dim3 block(256), grid((unsigned)((n + 255) / 256));
     switch (t->cap_class) {
-    case 0: ball_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
-    case 1: ball_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
-    default: ball_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status); break;
+    case 0: ball_kernel<CAP0, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status, order); break;
+    case 1: ball_kernel<CAP1, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status, order); break;
+    default: ball_kernel<CAP2, COUNT><<<grid, block, 0, s>>>(t->dev, c, r, n, hit, counts, t->d_status, order); break;
     }
     count_launch();
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (scratch) cudaFreeAsync(scratch, s);
+    return e;
 }
 
 // Process-wide settings of the BEST frame kernel (vox_cuda_render_set_config).
