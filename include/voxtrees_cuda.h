@@ -247,10 +247,13 @@ int vox_cuda_render(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
                     uint32_t w, uint32_t h, const uint8_t *texture, uint32_t *argb,
                     void *stream);
 /* n BEST frames of one tree, camera cams[i] into the host buffer frames[i]
- * (w*h ARGB each), with `tex` copied in once: what n calls of
+ * (w*h ARGB each; the buffers must not overlap, and their contents are
+ * undefined until the call returns), with `tex` copied in once: what n calls of
  * vox_cuda_render give, drawn by one persistent launch (up to 1024 frames
  * and 2 GiB of device frames a launch) and each copied out on a second
- * stream as soon as it is complete, while the rest are drawn; the calling
+ * stream as soon as it is complete, while the rest are drawn (for the last
+ * four frames of a launch, the zeros outside the tree's screen rectangle
+ * are written early and only the rectangle follows); the calling
  * thread waits for each frame's completion (page-locked frames: the copies
  * run asynchronously; pageable ones hold the thread for their copy).  The
  * device frames are kept per thread for later calls.  Returns when all n

@@ -209,6 +209,43 @@ def test_host_frames_call_equals_single_frames(tree256):
         assert np.array_equal(img, ref), f"frame {i}: {(img != ref).sum()} pixels differ"
 
 
+def test_host_frames_call_last_frames_of_every_kind(tree64):
+    """The last frames of a vox_cuda_render_frames launch reach the host in
+    two parts (the zeros outside the traced rectangle early, the rectangle
+    once drawn): with those frames of every kind -- the tree in part of the
+    frame, the camera inside the tree (the whole frame traced), the camera
+    looking away (no rectangle) -- into garbage-filled pinned and pageable
+    buffers, every frame equals the oracle's."""
+    import ctypes as C
+    from voxvision_gb300 import workloads as wl
+    from voxvision_gb300.cameras import HostCamera, orbit_camera
+    ht, dt = tree64
+    tex = wl.texture32(13)
+    w, h = 320, 240
+    cams = [orbit_camera(f, 12, w, h, (32, 32, 32), 1.5 * 64 * 3 ** 0.5) for f in range(0, 12, 2)]
+    for pos, at in (((32.0, 30.0, 33.0), (60.0, 50.0, 40.0)),       # inside the tree
+                    ((150.0, -80.0, 90.0), (300.0, -300.0, 90.0)),  # looking away
+                    ((90.0, -40.0, 70.0), (32.0, 32.0, 32.0))):     # near, off to one side
+        c = HostCamera(0)
+        c.set_window_size(w, h)
+        c.set_position(pos)
+        c.look_at(np.array(at, np.float32))
+        cams.append(c)
+    for order in (cams, cams[::-1]):
+        bufs = [torch.full((h, w), GARBAGE, dtype=torch.int32).pin_memory() if i % 2 else
+                np.full((h, w), GARBAGE, np.uint32) for i in range(len(order))]
+        dt.render_frames([c.gpu_struct() for c in order], w, h, tex, bufs)
+        for i, (cam, b) in enumerate(zip(order, bufs)):
+            ref, _ = orc.render_best(ht.ptr, cam.state(), w, h, tex)
+            img = b if isinstance(b, np.ndarray) else b.numpy().view(np.uint32)
+            assert np.array_equal(img, ref), f"frame {i}: {(img != ref).sum()} pixels differ"
+    bb = np.zeros(6, np.float32)
+    vg().lib().vox_bounding_box(C.c_void_p(ht.ptr), bb.ctypes.data_as(C.c_void_p))
+    kinds = [vg().frame_rect(bb, c.gpu_struct(), w, h) for c in cams[-3:]]
+    assert kinds[0] == (0, 0, w, h) and kinds[1][2] <= kinds[1][0]
+    assert 0 < kinds[2][0] < kinds[2][2] < w and 0 < kinds[2][1] < kinds[2][3] < h
+
+
 def test_host_frames_call_reuses_device_frames(tree64):
     """More frames than the 2 GiB of device frames hold (36 frames of 4096^2):
     the slots are reused round robin, each only after its copy finished."""

@@ -162,6 +162,6 @@ cudaError_t ball_order(const vox_cuda_tree *t, const float *centres, size_t n, v
  * d_done: njobs counters the call zeroes on s.  At most 1024 jobs. */
 int enqueue_announced_frames(const vox_cuda_frame_job *jobs, uint32_t njobs, void *h_table, void *d_table,
                              uint32_t *d_counter, uint32_t *d_done, uint32_t *flags, uint32_t epoch, int nsm,
-                             cudaStream_t s);
+                             cudaStream_t s, uint32_t *rects);
 
 #endif
