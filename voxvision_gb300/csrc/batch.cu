@@ -25,6 +25,7 @@
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -62,12 +63,19 @@ struct BatchJobDev {
 // Rows of the frame outside the traced rectangle that one clearing item zeroes.
 constexpr uint32_t CLEAR_ROWS = 8;
 
+struct NoHook {
+    __device__ void operator()() const {}
+};
+
 // One tile of TW x TH pixels of frame J (its `local`-th tile, taken outward
-// from where the tree's centre projects): ray, search, colour, store.
-template <int CAP, int TW, int TH>
-__device__ __forceinline__ void run_tile(const BatchJobDev &J, uint32_t local, uint32_t lane)
+// from where the tree's centre projects): ray, search, colour, store.  With
+// a hook, the warp calls it (converged) between its first rays' searches and
+// their stores.
+template <int CAP, int TW, int TH, class Hook = NoHook>
+__device__ __forceinline__ void run_tile(const BatchJobDev &J, uint32_t local, uint32_t lane, Hook hook = Hook())
 {
     constexpr int RPT = TW * TH / 32;   // rays per thread per tile
+    constexpr bool HOOK = !std::is_same<Hook, NoHook>::value;
     uint32_t ty = vox::centre_out(local / J.ntx, J.cty, J.nty);
     uint32_t tx = vox::centre_out(local % J.ntx, J.ctx, J.ntx);
     const DevTree t = J.tree;
@@ -77,17 +85,36 @@ __device__ __forceinline__ void run_tile(const BatchJobDev &J, uint32_t local, u
     for (int r = 0; r < RPT; r++) {
         uint32_t p = lane + 32u * (uint32_t)r;
         uint32_t px = J.x0 + tx * TW + p % TW, py = J.y0 + ty * TH + p / TW;
-        if (px < x1 && py < y1) {
-            float dx, dy, dz;
-            vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
-            RayHit hh;
-            vox::Counts c{0, 0, 0};
-            bool overflow = false, hit = false;
-            if (t.root != VOXP_EMPTY)
-                hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1], cam.position[2], dx,
-                                                 dy, dz, hh, c, overflow);
-            J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
-            if (overflow) atomicOr(J.status, 1u);
+        if constexpr (!HOOK) {
+            if (px < x1 && py < y1) {
+                float dx, dy, dz;
+                vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
+                RayHit hh;
+                vox::Counts c{0, 0, 0};
+                bool overflow = false, hit = false;
+                if (t.root != VOXP_EMPTY)
+                    hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1], cam.position[2],
+                                                     dx, dy, dz, hh, c, overflow);
+                J.argb[(size_t)py * w + px] = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
+                if (overflow) atomicOr(J.status, 1u);
+            }
+        } else {
+            const bool in = px < x1 && py < y1;
+            uint32_t v = 0u;
+            if (in) {
+                float dx, dy, dz;
+                vox::screen2world(cam, (int)px, (int)py, dx, dy, dz);
+                RayHit hh;
+                vox::Counts c{0, 0, 0};
+                bool overflow = false, hit = false;
+                if (t.root != VOXP_EMPTY)
+                    hit = vox::trace_ray<CAP, false>(t, t.root, cam.position[0], cam.position[1], cam.position[2],
+                                                     dx, dy, dz, hh, c, overflow);
+                v = hit ? vox::texel_color(J.tex, t, hh.x, hh.y, hh.z) : 0u;
+                if (overflow) atomicOr(J.status, 1u);
+            }
+            if (r == 0) hook();
+            if (in) J.argb[(size_t)py * w + px] = v;
         }
     }
 }
@@ -170,7 +197,11 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) batch_kernel(const Batc
 // a frame's last item stores `epoch` into flags[job] in host memory, after
 // every store of the frame is visible device-wide (the copy engine may read
 // the frame as soon as the host sees the flag).  done[] counts finished items
-// per frame and starts at zero.
+// per frame and starts at zero.  A warp counts each item when it is about to
+// store the next one's pixels (after the next tile's searches, before its
+// stores; before a clearing item), or when it leaves: the fence before the
+// count then finds the item's stores long complete instead of waiting for
+// them (the 120-frame 1080p orbit call 7.41 against 7.43 ms).
 template <int CAP, int TW, int TH>
 __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const BatchHead *__restrict__ head, uint32_t grab,
                                                      uint32_t *__restrict__ counter, uint32_t *__restrict__ done,
@@ -179,6 +210,19 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const Bat
     const BatchJobDev *jobs = reinterpret_cast<const BatchJobDev *>(head + 1);
     const uint32_t njobs = head->njobs, total = head->total_tiles;
     const uint32_t lane = threadIdx.x & 31;
+    uint32_t pending = 0xFFFFFFFFu;   // the frame of the last item, not yet counted
+    auto count = [&]() {
+        __syncwarp();
+        if (lane == 0 && pending != 0xFFFFFFFFu) {
+            __threadfence();   // this warp's stores (ordered before by the warp barrier), then the count
+            const uint32_t j = pending;
+            uint32_t items = (j + 1 < njobs ? __ldg(&jobs[j + 1].tile_base) : total) - __ldg(&jobs[j].tile_base);
+            if (atomicAdd(&done[j], 1u) + 1u == items) {
+                __threadfence_system();
+                *(volatile uint32_t *)&flags[j] = epoch;
+            }
+        }
+    };
     for (;;) {
         uint32_t t0 = 0;
         if (lane == 0) t0 = atomicAdd(counter, grab);
@@ -189,19 +233,16 @@ __global__ void __launch_bounds__(128, BATCH_MIN_BLOCKS) frames_kernel(const Bat
             uint32_t j = find_job(jobs, njobs, item, false);
             const BatchJobDev &J = jobs[j];
             uint32_t local = item - J.tile_base, ntile = J.ntx * J.nty;
-            if (local < ntile) run_tile<CAP, TW, TH>(J, local, lane);
-            else run_clear(J, local - ntile, lane);
-            __syncwarp();
-            if (lane == 0) {
-                __threadfence();   // this warp's stores (ordered before by the warp barrier), then the count
-                uint32_t items = (j + 1 < njobs ? __ldg(&jobs[j + 1].tile_base) : total) - J.tile_base;
-                if (atomicAdd(&done[j], 1u) + 1u == items) {
-                    __threadfence_system();
-                    *(volatile uint32_t *)&flags[j] = epoch;
-                }
+            if (local < ntile) {
+                run_tile<CAP, TW, TH>(J, local, lane, count);
+            } else {
+                count();
+                run_clear(J, local - ntile, lane);
             }
+            pending = j;
         }
     }
+    count();
 }
 
 // One frame's table entry for tile shape tw x th: the traced rectangle (the
