@@ -969,7 +969,8 @@ def run_ours(args):
            "h2d_bytes_per_step": 32768 + nf * C.sizeof(vg.CameraStruct), "d2h_bytes_per_step": nf * W * H * 4,
            "call": "vox_cuda_render_frames (host texture and cameras in; each frame drawn on the device and "
                    "copied into its own page-locked host buffer on a second stream while the next frames are "
-                   "drawn; returns when all are in host memory)",
+                   "drawn, the last four as their zeros early and their traced rectangle when drawn; returns "
+                   "when all are in host memory)",
            "per_call_value": job_rate(rays_step * args.steps, world, single_s) / 1e6,
            "per_call": "vox_cuda_render, one synchronous call per frame (same frames, one host frame)"}
     del host_frames
