@@ -237,10 +237,12 @@ int vox_cuda_ball_batch_device(const vox_cuda_tree *tree, const float *centres,
  * lookup fused in one kernel, written to a linear w x h ARGB8888 frame
  * (pixel (x, y) at argb[y * w + x]; misses are 0).  texture: the 32^3 u8
  * colour texture (index x*1024 + y*32 + z).  w must be a multiple of 16 and
- * h of 4 (renderer.c:97-100).  vox_cuda_render: a page-locked frame
- * (cudaHostAlloc, cudaHostRegister) is drawn in place by the kernel, whose
- * stores cross the host link while the frame is traced; a pageable one is
- * drawn on the device and copied out.
+ * h of 4 (renderer.c:97-100).  vox_cuda_render draws the frame into a
+ * stream-ordered device frame of w*h*4 bytes; while the kernel runs, a
+ * second stream of the calling thread copies zeros into the host frame
+ * outside the tree's screen rectangle, and the rectangle follows the kernel
+ * (page-locked host frames take the copies at full speed; pageable ones
+ * work too).
  * Replaces vox_render + vox_redraw with quality VOX_QUALITY_BEST
  * (src/voxrnd/renderer.c:200-327). */
 int vox_cuda_render(const vox_cuda_tree *tree, const vox_cuda_camera *camera,
@@ -339,8 +341,8 @@ int vox_cuda_frame_rect(const float *bbox, const vox_cuda_camera *camera, uint32
  * Z-order, the previous pixel's leaf as the search root, the corner test),
  * a square on half a warp: every pixel's search from the root, then the
  * searches from the square's leaf for the pixels still to come.  The
- * _device calls allocate nothing; the host-buffer calls allocate a w*h*4
- * byte stream-ordered frame when `argb` is not page-locked.
+ * _device calls allocate nothing; the host-buffer calls draw into a w*h*4
+ * byte stream-ordered device frame, sent to `argb` as vox_cuda_render's.
  * Pixels the reference leaves undrawn are 0.  EINVAL for a combination
  * vox_context_set_quality rejects.
  * Replaces vox_render + vox_redraw (src/voxrnd/renderer.c:200-327). */

@@ -1331,20 +1331,6 @@ try {
     return status_of(launch_render<false>(t, *cam, w, h, tex, argb, nullptr, as_stream(stream), true));
 } VOX_ABI_FAIL_INT
 
-// The device's address of a host buffer that the GPU can write in place:
-// page-locked host memory (cudaHostAlloc, cudaHostRegister, torch pinned
-// tensors), which is mapped into the device's address space; nullptr for
-// pageable memory.
-static void *device_alias(void *host)
-{
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
-}
-
 // Per host thread and device: what the synchronous host-buffer frame calls
 // reuse from one call to the next.  A call returns only after its stream has
 // finished with these, so the next call of the same thread may use them
@@ -1391,9 +1377,10 @@ struct HostCallState {
 
 // Staging frames (`bytes` for `slots` frames), `tables` bytes of pinned job
 // tables, a device job table of `table` bytes, completion counters and flags
-// for `group` frames, and `zeros` bytes of device zeros (grow only; the zeros
-// are written when allocated, on stream s, which is then drained, so that no
-// kernel has to run before a copy reads them).
+// for `group` frames, and the copy stream with `zeros` bytes of device zeros
+// (host_call_copies; all grow only).
+static cudaError_t host_call_copies(HostCallState *hc, size_t zeros, cudaStream_t s);
+
 static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots, size_t tables, size_t table,
                                  uint32_t group, size_t zeros, cudaStream_t s)
 {
@@ -1423,8 +1410,7 @@ static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots
             return e;
         }
     }
-    if (!hc->copy) e = cudaStreamCreateWithFlags(&hc->copy, cudaStreamNonBlocking);
-    if (e == cudaSuccess && !hc->fin) e = cudaEventCreateWithFlags(&hc->fin, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = host_call_copies(hc, zeros, s);
     while (e == cudaSuccess && hc->drawn.size() < slots) {
         cudaEvent_t a = nullptr, b = nullptr;
         e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming);
@@ -1468,22 +1454,6 @@ static cudaError_t stage_reserve(HostCallState *hc, size_t bytes, uint32_t slots
         e = cudaMalloc(&hc->d_stage, bytes);
         if (e == cudaSuccess) hc->stage_bytes = bytes;
         else hc->d_stage = nullptr;
-    }
-    if (e == cudaSuccess && hc->zero_bytes < zeros) {
-        if (hc->d_zero) {
-            cudaDeviceSynchronize();   // an earlier call's copies may still read the old zeros
-            cudaFree(hc->d_zero);
-            hc->d_zero = nullptr;
-            hc->zero_bytes = 0;
-        }
-        e = cudaMalloc(&hc->d_zero, zeros);
-        if (e == cudaSuccess) e = cudaMemsetAsync(hc->d_zero, 0, zeros, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e == cudaSuccess) hc->zero_bytes = zeros;
-        else if (hc->d_zero) {
-            cudaFree(hc->d_zero);
-            hc->d_zero = nullptr;
-        }
     }
     return e;
 }
@@ -1541,46 +1511,6 @@ static int host_call_finish(HostCallState *hc, const vox_cuda_tree *t, cudaStrea
     return VOX_CUDA_OK;
 }
 
-// Host-buffer frame: the texture is copied in; a page-locked frame is drawn
-// in place (the kernel's stores cross the host link while the frame is
-// traced, and no copy follows), a pageable one is drawn into device scratch
-// and copied out.
-EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
-                           const uint8_t *tex, uint32_t *argb, void *stream)
-try {
-    int rc = check_render_args(t, cam, w, h, tex, argb);
-    if (rc) return rc;
-    cudaStream_t s = as_stream(stream);
-    size_t npx = (size_t)w * h;
-    HostCallState *hc = host_call_state();
-    if (!hc) return VOX_CUDA_ENOMEM;
-    uint32_t *in_place = static_cast<uint32_t *>(device_alias(argb));
-    Scratch sc(s);
-    if (!in_place && sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    uint32_t *d_argb = in_place ? in_place : static_cast<uint32_t *>(sc.p);
-    cudaError_t e = host_call_texture(hc, tex, s);
-    if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, hc->d_tex, d_argb, nullptr, s);
-    if (e == cudaSuccess && !in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
-    return host_call_finish(hc, t, s, e);
-} VOX_ABI_FAIL_INT
-
-// Host-buffer frames of one tree: the texture copied in once; all frames
-// drawn by one persistent launch into device frames, one after another, each
-// announced when complete; the calling thread waits for each announcement and
-// has the frame copied out on a second stream at once, while later frames are
-// still drawn; one synchronisation at the end.  Up to STAGE_BYTES of device
-// frames (at most 1024 frames) go into one launch; beyond that, launches
-// follow one another, reusing the device frames once copied out.
-static constexpr size_t STAGE_BYTES = size_t(2) << 30;
-static constexpr uint32_t LAUNCH_FRAMES = 1024;
-// Frames at the end of a launch sent to the host in two parts (copy_outside
-// early, the traced rectangle when drawn): the copy engine moves 184 GB/s to
-// host memory, a 1080p frame in 46 us, and the last three or so frames of a
-// launch complete within that of each other.  On the 120-frame 1080p orbit
-// the call took 7.60 ms with whole-frame copies throughout (the copies
-// running 0.15 ms past the kernel's end) and 7.44 ms with this.
-static constexpr uint32_t TAIL_FRAMES = 4;
-
 // The parts of host frame `f` (w x h) outside the traced rectangle r (x0, y0,
 // x1, y1; empty: the whole frame), which the finished frame holds as zeros,
 // written from the device zero buffer `zero` (at least w * h pixels).
@@ -1602,6 +1532,103 @@ static cudaError_t copy_outside(uint32_t *f, const uint32_t *zero, uint32_t w, u
                               cudaMemcpyDeviceToHost, cs);
     return e;
 }
+
+// The copy stream, its event and `zeros` bytes of device zeros of the
+// calling thread's host calls (grow only; the zeros are written when
+// allocated, on stream s, which is then drained, so that no kernel has to run
+// before a copy reads them).
+static cudaError_t host_call_copies(HostCallState *hc, size_t zeros, cudaStream_t s)
+{
+    cudaError_t e = cudaSuccess;
+    if (!hc->copy) e = cudaStreamCreateWithFlags(&hc->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !hc->fin) e = cudaEventCreateWithFlags(&hc->fin, cudaEventDisableTiming);
+    if (e == cudaSuccess && hc->zero_bytes < zeros) {
+        if (hc->d_zero) {
+            cudaDeviceSynchronize();   // an earlier call's copies may still read the old zeros
+            cudaFree(hc->d_zero);
+            hc->d_zero = nullptr;
+            hc->zero_bytes = 0;
+        }
+        e = cudaMalloc(&hc->d_zero, zeros);
+        if (e == cudaSuccess) e = cudaMemsetAsync(hc->d_zero, 0, zeros, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) hc->zero_bytes = zeros;
+        else if (hc->d_zero) {
+            cudaFree(hc->d_zero);
+            hc->d_zero = nullptr;
+        }
+    }
+    return e;
+}
+
+// A single-frame host call's frame, drawn into device memory at d_argb with
+// traced rectangle m, into the host buffer argb: the zeros outside the
+// rectangle from the copy stream, which starts at once and runs beside the
+// kernel, then the rectangle once the kernel is done (on s, which also waits
+// for the zeros).  A 1080p orbit frame, BEST / ADAPTIVE: 140 / 167 us into a
+// page-locked frame against 148 / 176 drawn in place over the host link,
+// 147 / 175 us into a pageable one against 183 / 211 with the whole frame
+// copied after the kernel.
+static cudaError_t host_frame_out(HostCallState *hc, uint32_t *argb, const uint32_t *d_argb, uint32_t w, uint32_t h,
+                                  const FrameMemo &m, cudaStream_t s)
+{
+    const size_t npx = (size_t)w * h;
+    if (!m.valid) return cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+    const uint32_t r[4] = {m.x0, m.y0, m.x1, m.y1};
+    cudaError_t e = copy_outside(argb, hc->d_zero, w, h, r, hc->copy);
+    if (e == cudaSuccess) e = cudaEventRecord(hc->fin, hc->copy);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, hc->fin, 0);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(hc->copy);   // no copy may still write argb once the call has returned
+        return e;
+    }
+    if (e == cudaSuccess && r[2] > r[0] && r[3] > r[1]) {
+        size_t off = (size_t)r[1] * w + r[0];
+        e = cudaMemcpy2DAsync(argb + off, (size_t)w * 4, d_argb + off, (size_t)w * 4, (size_t)(r[2] - r[0]) * 4,
+                              r[3] - r[1], cudaMemcpyDeviceToHost, s);
+    }
+    return e;
+}
+
+// Host-buffer frame: the texture is copied in, the frame drawn into device
+// scratch and copied out in two parts (host_frame_out).
+EXPORT int vox_cuda_render(const vox_cuda_tree *t, const vox_cuda_camera *cam, uint32_t w, uint32_t h,
+                           const uint8_t *tex, uint32_t *argb, void *stream)
+try {
+    int rc = check_render_args(t, cam, w, h, tex, argb);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    size_t npx = (size_t)w * h;
+    HostCallState *hc = host_call_state();
+    if (!hc) return VOX_CUDA_ENOMEM;
+    if (host_call_copies(hc, npx * 4, s) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    Scratch sc(s);
+    if (sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    uint32_t *d_argb = static_cast<uint32_t *>(sc.p);
+    FrameMemo m{false, 0, 0, 0, 0};
+    cudaError_t e = host_call_texture(hc, tex, s);
+    if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, hc->d_tex, d_argb, nullptr, s, false, nullptr, &m);
+    if (e == cudaSuccess) e = host_frame_out(hc, argb, d_argb, w, h, m, s);
+    return host_call_finish(hc, t, s, e);
+} VOX_ABI_FAIL_INT
+
+// Host-buffer frames of one tree: the texture copied in once; all frames
+// drawn by one persistent launch into device frames, one after another, each
+// announced when complete; the calling thread waits for each announcement and
+// has the frame copied out on a second stream at once, while later frames are
+// still drawn; one synchronisation at the end.  Up to STAGE_BYTES of device
+// frames (at most 1024 frames) go into one launch; beyond that, launches
+// follow one another, reusing the device frames once copied out.
+static constexpr size_t STAGE_BYTES = size_t(2) << 30;
+static constexpr uint32_t LAUNCH_FRAMES = 1024;
+// Frames at the end of a launch sent to the host in two parts (copy_outside
+// early, the traced rectangle when drawn): the copy engine moves 184 GB/s to
+// host memory, a 1080p frame in 46 us, and the last three or so frames of a
+// launch complete within that of each other.  On the 120-frame 1080p orbit
+// the call took 7.60 ms with whole-frame copies throughout (the copies
+// running 0.15 ms past the kernel's end) and 7.44 ms with this.
+static constexpr uint32_t TAIL_FRAMES = 4;
+
 
 // Waits for flags[j] == epoch; gives up when the stream holding the launch
 // has finished or failed without it, or after `limit_s` seconds.
@@ -1822,18 +1849,19 @@ static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     size_t npx = (size_t)w * h;
     HostCallState *hc = host_call_state();
     if (!hc) return VOX_CUDA_ENOMEM;
-    uint32_t *in_place = static_cast<uint32_t *>(device_alias(argb));
+    if (host_call_copies(hc, npx * 4, s) != cudaSuccess) return VOX_CUDA_ENOMEM;
     Scratch sc(s);
-    if (!in_place && sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    uint32_t *d_argb = in_place ? in_place : static_cast<uint32_t *>(sc.p);
+    if (sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
+    uint32_t *d_argb = static_cast<uint32_t *>(sc.p);
     cudaError_t e = host_call_texture(hc, tex, s);
     if (e == cudaSuccess) {
-        rc = render_any_device(t, cam, w, h, quality, hc->d_tex, lights, d_argb, stream);
+        FrameMemo m{false, 0, 0, 0, 0};
+        rc = render_frame_memo(t, cam, nullptr, w, h, quality, hc->d_tex, lights, d_argb, s, &m);
         if (rc) {
             host_call_finish(hc, t, s, cudaErrorUnknown);
             return rc;
         }
-        if (!in_place) e = cudaMemcpyAsync(argb, d_argb, npx * 4, cudaMemcpyDeviceToHost, s);
+        e = host_frame_out(hc, argb, d_argb, w, h, m, s);
     }
     return host_call_finish(hc, t, s, e);
 }
