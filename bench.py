@@ -450,9 +450,9 @@ def measure_dropin(vg, ht_ptr, nframes=24):
     """The drop-in renderer as a voxvision program drives it: a 1080p context
     (vox_make_context_headless) over the library's host tree, the built-in
     simple camera moved along the orbit, and per frame one synchronous
-    vox_render (the frame drawn into the context's page-locked frame) and one
-    vox_redraw (the frame copied to the buffer vox_context_pixels returns),
-    host-timed, in the default ADAPTIVE quality and in BEST."""
+    vox_render (the frame drawn into the context's device frame) and one
+    vox_redraw (the frame copied to the page-locked buffer vox_context_pixels
+    returns), host-timed, in the default ADAPTIVE quality and in BEST."""
     import ctypes as C
     from voxvision_gb300.cameras import orbit_camera
     L = vg.lib()

@@ -4,14 +4,14 @@
  *
  * vox_render (renderer.c:200-319) draws a whole frame: the scene tree is
  * uploaded once per vox_context_set_scene, the camera state is read from the
- * built-in camera object, and one fused kernel draws the ARGB frame straight
- * into the context's page-locked frame.  A camera of any other class (one
+ * built-in camera object, and one fused kernel draws the ARGB frame into the
+ * context's device frame.  A camera of any other class (one
  * whose iface is not the built-in simple or doom camera's) is asked for every
  * pixel's direction through its own screen2world on the host threads, as the
  * reference's tasks ask it, and the frame is drawn from that ray buffer.
- * vox_redraw (renderer.c:321-327)
- * then brings the frame to the host buffer returned by vox_context_pixels.  Instead of an SDL
- * surface the context owns a headless frame.
+ * vox_redraw (renderer.c:321-327) then copies the frame into the page-locked
+ * host buffer returned by vox_context_pixels.  Instead of an SDL surface the
+ * context owns a headless frame.
  */
 #include <cuda_runtime.h>
 
@@ -46,10 +46,8 @@ struct vox_rnd_ctx {
     bool tex_dirty = true;
     uint8_t texture[32768];
     uint8_t *d_tex = nullptr;
-    uint32_t *d_frame = nullptr;
-    uint32_t *h_stage = nullptr;                   // pinned copy of the frame
-    uint32_t *d_stage = nullptr;                   // the device's address of h_stage (frames drawn in place)
-    uint32_t *pixels = nullptr;                    // what vox_context_pixels returns
+    uint32_t *d_frame = nullptr;                   // the frame vox_render draws (device; zeroed at creation)
+    uint32_t *pixels = nullptr;                    // what vox_context_pixels returns (page-locked)
     cudaStream_t stream = nullptr;
     int status = VOX_CUDA_OK;
     struct vox_light_manager *lights = nullptr;    // renderer.h:66
@@ -57,7 +55,7 @@ struct vox_rnd_ctx {
     uint64_t d_lights_version = 0;                 // the manager's version that copy holds
     float *h_rays = nullptr;                       // pixel directions of a host-computed camera (pinned)
     float *d_rays = nullptr;                       // their device copy
-    vox::FrameMemo memo{false, 0, 0, 0, 0};        // what the frame still holds of the last one
+    vox::FrameMemo memo{true, 0, 0, 0, 0};         // what d_frame holds (zeroed at creation)
     vox::FrameMemo shown{true, 0, 0, 0, 0};        // what `pixels` holds (zeroed at creation)
 };
 
@@ -84,11 +82,10 @@ void release(vox_rnd_ctx *c)
     if (c->tree) vox_cuda_tree_free(c->tree);
     if (c->d_tex) cudaFree(c->d_tex);
     if (c->d_frame) cudaFree(c->d_frame);
-    if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->pixels) cudaFreeHost(c->pixels);
     if (c->h_rays) cudaFreeHost(c->h_rays);
     if (c->d_rays) cudaFree(c->d_rays);
     if (c->stream) cudaStreamDestroy(c->stream);
-    std::free(c->pixels);
 }
 
 // Every pixel's direction from the camera's own screen2world, rows dealt to
@@ -137,17 +134,18 @@ EXPORT struct vox_rnd_ctx *vox_make_context_headless(unsigned int width, unsigne
     c->h = height;
     default_texture(c->texture);
     size_t bytes = (size_t)width * height * 4;
-    c->pixels = static_cast<uint32_t *>(std::calloc((size_t)width * height, 4));
+    void *px = nullptr;
+    if (cudaMallocHost(&px, bytes) != cudaSuccess) px = nullptr;
+    c->pixels = static_cast<uint32_t *>(px);
     if (!c->pixels || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&c->d_tex, 32768) != cudaSuccess || cudaMalloc(&c->d_frame, bytes) != cudaSuccess ||
-        cudaMallocHost(&c->h_stage, bytes) != cudaSuccess) {
+        cudaMemsetAsync(c->d_frame, 0, bytes, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
         release(c);
         delete c;
         return nullptr;
     }
-    void *alias = nullptr;
-    if (cudaHostGetDevicePointer(&alias, c->h_stage, 0) == cudaSuccess) c->d_stage = static_cast<uint32_t *>(alias);
-    else cudaGetLastError();
+    std::memset(c->pixels, 0, bytes);
     return c;
 }
 
@@ -224,10 +222,7 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
         if (rc) { ctx->status = rc; return; }
         ctx->d_lights_version = ctx->lights->version;
     }
-    // one frame waited on: drawn straight into the pinned frame when the device
-    // can address it (its stores cross the host link while the frame is
-    // traced; no copy follows), else into device memory and copied
-    uint32_t *target = ctx->d_stage ? ctx->d_stage : ctx->d_frame;
+    uint32_t *target = ctx->d_frame;
     const vox_cuda_lights *lights = ctx->lights ? ctx->d_lights : nullptr;
     int rc;
     if (kind < 0) {
@@ -250,25 +245,23 @@ EXPORT void vox_render(struct vox_rnd_ctx *ctx)
                                ctx->stream, &ctx->memo);
     }
     if (rc) { ctx->status = rc; return; }
-    size_t bytes = (size_t)ctx->w * ctx->h * 4;
-    if ((!ctx->d_stage &&
-         cudaMemcpyAsync(ctx->h_stage, ctx->d_frame, bytes, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess) ||
-        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         ctx->status = VOX_CUDA_ECUDA;
         return;
     }
     ctx->status = VOX_CUDA_OK;
 }
 
-// The last frame into the buffer vox_context_pixels returns.  Both frames
-// are zero outside their tree rectangles when their memos are valid, so only
-// the box covering both rectangles is copied.
+// The last frame into the buffer vox_context_pixels returns, by the copy
+// engine.  Both frames are zero outside their tree rectangles when their
+// memos are valid, so only the box covering both rectangles is copied.
 EXPORT void vox_redraw(struct vox_rnd_ctx *ctx)
 {
-    const size_t w = ctx->w;
+    const size_t w = ctx->w, row = w * 4;
     const vox::FrameMemo &now = ctx->memo, &was = ctx->shown;
+    cudaError_t e = cudaSuccess;
     if (!now.valid || !was.valid) {
-        std::memcpy(ctx->pixels, ctx->h_stage, w * ctx->h * 4);
+        e = cudaMemcpyAsync(ctx->pixels, ctx->d_frame, row * ctx->h, cudaMemcpyDeviceToHost, ctx->stream);
     } else {
         uint32_t x0 = ctx->w, y0 = ctx->h, x1 = 0, y1 = 0;
         for (const vox::FrameMemo *m : {&now, &was})
@@ -276,8 +269,18 @@ EXPORT void vox_redraw(struct vox_rnd_ctx *ctx)
                 x0 = std::min(x0, m->x0); y0 = std::min(y0, m->y0);
                 x1 = std::max(x1, m->x1); y1 = std::max(y1, m->y1);
             }
-        for (uint32_t y = y0; y < y1 && x1 > x0; y++)
-            std::memcpy(ctx->pixels + y * w + x0, ctx->h_stage + y * w + x0, (size_t)(x1 - x0) * 4);
+        if (x1 > x0) {
+            size_t off = (size_t)y0 * w + x0;
+            e = cudaMemcpy2DAsync(ctx->pixels + off, row, ctx->d_frame + off, row, (size_t)(x1 - x0) * 4, y1 - y0,
+                                  cudaMemcpyDeviceToHost, ctx->stream);
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(ctx->stream);
+        ctx->status = VOX_CUDA_ECUDA;
+        ctx->shown = vox::FrameMemo{false, 0, 0, 0, 0};   // unknown: the next redraw copies all
+        return;
     }
     ctx->shown = now;
 }
