@@ -21,7 +21,9 @@
  * its result there.  Items of one (key, block) pair land in any order among
  * themselves; that, too, changes no result.
  * (Copying the rays into order instead makes a 16M-ray batch slower: each
- * ray's six floats become scattered partial-sector stores.)
+ * ray's six floats become scattered partial-sector stores.  Finer keys are
+ * slower too: the entry point's cell on a 16^3 grid, 2.84-2.87 ms, and the
+ * direction's dominant axis added to the key, 2.99 ms, against 2.77-2.78.)
  */
 #include <cuda_runtime.h>
 
