@@ -90,6 +90,40 @@ def test_balls_match_reference_golden(case):
     _reset_voxel()
 
 
+@pytest.mark.parametrize("case", TREE_CASES)
+def test_small_host_batches_match_reference_golden(case):
+    """Host batches of up to 256 queries take the page-locked small-batch
+    path (the drop-in single queries' path): the golden rays, leaf-rooted
+    rays and balls in batches of 1, 37 and 256 give the reference's answers,
+    and the points of misses keep the caller's values."""
+    g = load(case)
+    ht, ptr = _host_tree(g)
+    dt = vg().DeviceTree(ptr)
+    L = vg().lib()
+    for size in (1, 37, 256):
+        for i in range(0, min(len(g["ray_origins"]), 3 * size), size):
+            o = np.ascontiguousarray(g["ray_origins"][i:i + size]); d = np.ascontiguousarray(g["ray_dirs"][i:i + size])
+            n = len(o)
+            leaf = np.empty(n, np.uint32); slot = np.empty(n, np.uint8); pts = np.full((n, 3), 7.0, np.float32)
+            assert L.vox_cuda_ray_batch(dt.h, o.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p), None, n,
+                                        leaf.ctypes.data_as(C.c_void_p), slot.ctypes.data_as(C.c_void_p),
+                                        pts.ctypes.data_as(C.c_void_p), None) == 0
+            assert np.array_equal(leaf, g["ray_leaf"][i:i + n])
+            hit = leaf != MISS
+            assert same_points(pts, g["ray_points"][i:i + n], hit)[0]
+            assert np.all(pts[~hit] == 7.0)
+        if "root_ids" in g:
+            for i in range(0, min(len(g["root_origins"]), 2 * size), size):
+                leaf, _, pts = dt.rays(g["root_origins"][i:i + size], g["root_dirs"][i:i + size],
+                                       roots=g["root_ids"][i:i + size])
+                assert np.array_equal(leaf, g["root_leaf"][i:i + size])
+                assert same_points(pts, g["root_points"][i:i + size], leaf != MISS)[0]
+        for i in range(0, min(len(g["ball_centres"]), 3 * size), size):
+            hit = dt.balls(g["ball_centres"][i:i + size], g["ball_radii"][i:i + size])
+            assert np.array_equal(hit, g["ball_hit"][i:i + size])
+    _reset_voxel()
+
+
 def test_regression_ray_of_reference_tests():
     """tests.c:600-659 -- the ray from (-2,-2,0) along (1,1,-1) hits."""
     g = load("g676d50c")
