@@ -483,6 +483,31 @@ def measure_dropin(vg, ht_ptr, nframes=24):
                      "redraw_ms": float(np.median(redraw_ms)),
                      "mpixels_s": W * H / (float(np.median(render_ms)) * 1e-3) / 1e6}
     L.vox_destroy_context(ctx)
+    # the reference's single queries, one call each (host-timed; the first
+    # call of each kind uploads the tree, untimed)
+    rng = np.random.default_rng(17)
+    n = 2000
+    org = rng.uniform(-100.0, 356.0, (n, 3)).astype(np.float32)
+    tgt = rng.uniform(64.0, 192.0, (n, 3)).astype(np.float32)
+    dirs = (tgt - org).astype(np.float32)
+    res = np.zeros(3, np.float32)
+    rp = res.ctypes.data_as(C.c_void_p)
+    L.vox_ray_tree_intersection(C.c_void_p(ht_ptr), org[0].ctypes.data_as(C.c_void_p),
+                                dirs[0].ctypes.data_as(C.c_void_p), rp)
+    t0 = time.perf_counter()
+    hits = 0
+    for i in range(n):
+        hits += bool(L.vox_ray_tree_intersection(C.c_void_p(ht_ptr), org[i].ctypes.data_as(C.c_void_p),
+                                                 dirs[i].ctypes.data_as(C.c_void_p), rp))
+    t1 = time.perf_counter()
+    for i in range(n):
+        L.vox_tree_ball_collidep(C.c_void_p(ht_ptr), tgt[i].ctypes.data_as(C.c_void_p), 3.0)
+    t2 = time.perf_counter()
+    L.vox_cuda_forget_tree(C.c_void_p(ht_ptr))
+    out["single_queries"] = {"calls": n, "ray_us": (t1 - t0) / n * 1e6, "ball_us": (t2 - t1) / n * 1e6,
+                             "ray_hits": hits,
+                             "call": "vox_ray_tree_intersection / vox_tree_ball_collidep (radius 3) on the "
+                                     "256^3 tree, rays from U[-100,356)^3 towards U[64,192)^3, seed 17"}
     return out
 
 
