@@ -32,7 +32,6 @@
  * submission with VOX_CUDA_EBUDGET.
  */
 #include <cuda_runtime.h>
-#include <sys/mman.h>
 
 #include <algorithm>
 #include <atomic>
@@ -128,33 +127,6 @@ FrameCopy plan_frame_copy(const Dirty &d, uint32_t w, uint32_t h, const uint32_t
     return c;
 }
 
-// A 128 MiB slab of page-locked memory: anonymous memory advised for huge
-// pages, faulted in, then registered with CUDA (instead of cudaHostAlloc).
-// Served at 20 kHz with host frames after host-memory-heavy work in the same
-// process (the 512^3 tree builds), servers whose slabs cudaHostAlloc pinned
-// then had spells of late copies in 4 of 15 traces (p99 19-77 ms), servers
-// with slabs made this way in none of 5 (p99 1.7-1.9 ms); a server pinned
-// before that work had none in 6 either.
-static void *slab_alloc(size_t bytes)
-{
-    void *p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-    if (p == MAP_FAILED) return nullptr;
-    madvise(p, bytes, MADV_HUGEPAGE);   // advice only: refused or ignored, the slab still works
-    std::memset(p, 0, bytes);
-    if (cudaHostRegister(p, bytes, cudaHostRegisterDefault) != cudaSuccess) {
-        cudaGetLastError();
-        munmap(p, bytes);
-        return nullptr;
-    }
-    return p;
-}
-
-static void slab_free(void *p, size_t bytes)
-{
-    cudaHostUnregister(p);
-    munmap(p, bytes);
-}
-
 // Pinned host buffers by power-of-two size class, reused across requests.
 // Buffers up to 64 MiB are carved from 128 MiB pinned slabs; a part of the
 // host budget is pinned in slabs when the server starts, and a refill thread
@@ -177,8 +149,8 @@ class PinnedPool {
         }
         cv_.notify_all();
         if (refill_.joinable()) refill_.join();
-        for (void *p : slabs_) slab_free(p, SLAB);
-        for (void *p : spares_) slab_free(p, SLAB);
+        for (void *p : slabs_) cudaFreeHost(p);
+        for (void *p : spares_) cudaFreeHost(p);
         for (void *p : direct_) cudaFreeHost(p);
     }
 
@@ -190,8 +162,8 @@ class PinnedPool {
         dev_ = dev;
         cap_ = cap;
         for (size_t got = 0; got + SLAB <= now; got += SLAB) {
-            void *p = slab_alloc(SLAB);
-            if (!p) return false;
+            void *p = nullptr;
+            if (cudaHostAlloc(&p, SLAB, cudaHostAllocDefault) != cudaSuccess) return false;
             spares_.push_back(p);
             pinned_ += SLAB;
         }
@@ -274,8 +246,8 @@ class PinnedPool {
             cv_.wait(lk, [this] { return stop_ || (spares_.size() < SPARES && pinned_ + SLAB <= cap_); });
             if (stop_) return;
             lk.unlock();
-            void *p = slab_alloc(SLAB);
-            bool ok = p != nullptr;
+            void *p = nullptr;
+            bool ok = cudaHostAlloc(&p, SLAB, cudaHostAllocDefault) == cudaSuccess;
             lk.lock();
             if (!ok) return;        // out of pinnable memory: the worker pins what it needs itself
             spares_.push_back(p);
