@@ -1363,6 +1363,8 @@ struct HostCallState {
     size_t stage_bytes = 0;
     uint32_t *d_zero = nullptr;          // device zeros, the source of copy_outside
     size_t zero_bytes = 0;
+    uint32_t *d_frame = nullptr;         // the single-frame calls' device frame (host_call_frame)
+    size_t frame_bytes = 0;
     unsigned char *h_tables = nullptr;   // pinned: one job table per chunk of frames
     size_t tables_bytes = 0;
     void *d_table = nullptr;             // device: the job table of the chunk being drawn, its queue head
@@ -1381,6 +1383,7 @@ struct HostCallState {
         if (h_tex) cudaFreeHost(h_tex);
         if (d_stage) cudaFree(d_stage);
         if (d_zero) cudaFree(d_zero);
+        if (d_frame) cudaFree(d_frame);
         if (h_tables) cudaFreeHost(h_tables);
         if (h_small) cudaFreeHost(h_small);
         if (d_table) cudaFree(d_table);
@@ -1658,6 +1661,24 @@ static cudaError_t host_call_copies(HostCallState *hc, size_t zeros, cudaStream_
     return e;
 }
 
+// The calling thread's device frame for its single-frame host calls, at
+// least `bytes` (grow only; a call returns only after its stream finished
+// with it).  Kept rather than taken from the stream-ordered pool each call
+// (which returns freed memory at every synchronisation): 1-2.5 us a 1080p
+// call.
+static uint32_t *host_call_frame(HostCallState *hc, size_t bytes)
+{
+    if (hc->frame_bytes >= bytes) return hc->d_frame;
+    if (hc->d_frame) cudaFree(hc->d_frame);
+    hc->d_frame = nullptr;
+    hc->frame_bytes = 0;
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    hc->d_frame = static_cast<uint32_t *>(p);
+    hc->frame_bytes = bytes;
+    return hc->d_frame;
+}
+
 // A single-frame host call's frame, drawn into device memory at d_argb with
 // traced rectangle m, into the host buffer argb: the zeros outside the
 // rectangle from the copy stream, which starts at once and runs beside the
@@ -1699,9 +1720,8 @@ try {
     HostCallState *hc = host_call_state();
     if (!hc) return VOX_CUDA_ENOMEM;
     if (host_call_copies(hc, npx * 4, s) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    Scratch sc(s);
-    if (sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    uint32_t *d_argb = static_cast<uint32_t *>(sc.p);
+    uint32_t *d_argb = host_call_frame(hc, npx * 4);
+    if (!d_argb) return VOX_CUDA_ENOMEM;
     FrameMemo m{false, 0, 0, 0, 0};
     cudaError_t e = host_call_texture(hc, tex, s);
     if (e == cudaSuccess) e = launch_render<false>(t, *cam, w, h, hc->d_tex, d_argb, nullptr, s, false, nullptr, &m);
@@ -1947,9 +1967,8 @@ static int render_any_host(const vox_cuda_tree *t, const vox_cuda_camera *cam, u
     HostCallState *hc = host_call_state();
     if (!hc) return VOX_CUDA_ENOMEM;
     if (host_call_copies(hc, npx * 4, s) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    Scratch sc(s);
-    if (sc.get(npx * 4) != cudaSuccess) return VOX_CUDA_ENOMEM;
-    uint32_t *d_argb = static_cast<uint32_t *>(sc.p);
+    uint32_t *d_argb = host_call_frame(hc, npx * 4);
+    if (!d_argb) return VOX_CUDA_ENOMEM;
     cudaError_t e = host_call_texture(hc, tex, s);
     if (e == cudaSuccess) {
         FrameMemo m{false, 0, 0, 0, 0};
