@@ -238,7 +238,8 @@ int vox_cuda_ball_batch_device(const vox_cuda_tree *tree, const float *centres,
  * (pixel (x, y) at argb[y * w + x]; misses are 0).  texture: the 32^3 u8
  * colour texture (index x*1024 + y*32 + z).  w must be a multiple of 16 and
  * h of 4 (renderer.c:97-100).  vox_cuda_render draws the frame into a
- * stream-ordered device frame of w*h*4 bytes; while the kernel runs, a
+ * device frame the calling thread keeps (w*h*4 bytes, grown as larger frames
+ * come, freed when the thread ends); while the kernel runs, a
  * second stream of the calling thread copies zeros into the host frame
  * outside the tree's screen rectangle, and the rectangle follows the kernel
  * (page-locked host frames take the copies at full speed; pageable ones
@@ -341,8 +342,9 @@ int vox_cuda_frame_rect(const float *bbox, const vox_cuda_camera *camera, uint32
  * Z-order, the previous pixel's leaf as the search root, the corner test),
  * a square on half a warp: every pixel's search from the root, then the
  * searches from the square's leaf for the pixels still to come.  The
- * _device calls allocate nothing; the host-buffer calls draw into a w*h*4
- * byte stream-ordered device frame, sent to `argb` as vox_cuda_render's.
+ * _device calls allocate nothing; the host-buffer calls draw into the
+ * calling thread's device frame and send it to `argb` as vox_cuda_render
+ * does.
  * Pixels the reference leaves undrawn are 0.  EINVAL for a combination
  * vox_context_set_quality rejects.
  * Replaces vox_render + vox_redraw (src/voxrnd/renderer.c:200-327). */
